@@ -1,0 +1,13 @@
+"""hsrq3in_gb300 -- robust level-3 inverse iteration on GB300 (sm_103a).
+
+The product is the C-ABI shared library ``libhsrq3in_gb300.so`` declared in
+``include/hsrq3in_gb300.h``; this package builds it (``build.py``), binds it
+(``_lib.py``), wraps it for numpy and torch callers (``api.py``), and ships
+the seeded workload generators (``generators.py``).
+"""
+from .api import (HsrError, fp64_peak, inverse_iteration, inverse_iteration_device,  # noqa: F401
+                  last_launch_count, tiled_inverse_iteration)
+from ._lib import lib_path, load  # noqa: F401
+
+__all__ = ["HsrError", "fp64_peak", "inverse_iteration", "inverse_iteration_device",
+           "last_launch_count", "tiled_inverse_iteration", "lib_path", "load"]

@@ -1,0 +1,81 @@
+"""ctypes binding of libhsrq3in_gb300.so (the C ABI in include/hsrq3in_gb300.h).
+
+The shared library is the product; this module only declares its entry
+points.  Loading fails loudly when the library has not been built -- there is
+no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+HSR_OK = 0
+HSR_ERR_ARG = -1
+HSR_ERR_NOMEM = -2
+HSR_ERR_CUDA = -3
+HSR_ERR_DEVICE = -4
+HSR_ERR_NOT_CONVERGED = 1
+
+# Every symbol include/hsrq3in_gb300.h declares.
+EXPORTS = [
+    "hsr_last_status", "hsr_status_string", "tiled_inverse_iteration",
+    "hsr_inverse_iteration_ex", "hsr_inverse_iteration_device",
+    "hsr_last_launch_count", "hsr_release_workspace", "hsr_probe_fp64_peak",
+    "hsr_version",
+]
+
+
+class Options(C.Structure):
+    _fields_ = [("intscale", C.c_int), ("user_rhs", C.c_int),
+                ("max_restarts", C.c_int), ("hbm_budget_bytes", C.c_double)]
+
+
+class ColumnInfo(C.Structure):
+    _fields_ = [("status", C.POINTER(C.c_int)), ("perturbed", C.POINTER(C.c_ubyte)),
+                ("scale", C.POINTER(C.c_double)), ("tile_scales", C.POINTER(C.c_double)),
+                ("norm", C.POINTER(C.c_double))]
+
+
+_LIB = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False) -> C.CDLL:
+    """Load the CUDA library; raise if it is missing (no fallback)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if not os.path.exists(path):
+        if build_if_missing:
+            _build.build()
+        else:
+            raise RuntimeError("libhsrq3in_gb300.so is not built (%s); run "
+                               "__graft_entry__.build() first" % path)
+    lib = C.CDLL(path)
+    lib.hsr_last_status.restype = C.c_int
+    lib.hsr_status_string.restype = C.c_char_p
+    lib.hsr_status_string.argtypes = [C.c_int]
+    lib.tiled_inverse_iteration.restype = None
+    lib.tiled_inverse_iteration.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                            C.c_int, C.c_int, C.c_void_p, C.c_int]
+    lib.hsr_inverse_iteration_ex.restype = C.c_int
+    lib.hsr_inverse_iteration_ex.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                             C.c_int, C.c_int, C.c_void_p, C.c_int,
+                                             C.POINTER(Options), C.POINTER(ColumnInfo)]
+    lib.hsr_inverse_iteration_device.restype = C.c_int
+    lib.hsr_inverse_iteration_device.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                                 C.c_int, C.c_void_p, C.c_int, C.POINTER(Options),
+                                                 C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.hsr_last_launch_count.restype = C.c_long
+    lib.hsr_release_workspace.restype = None
+    lib.hsr_probe_fp64_peak.restype = C.c_int
+    lib.hsr_probe_fp64_peak.argtypes = [C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.hsr_version.restype = C.c_char_p
+    _LIB = lib
+    return lib

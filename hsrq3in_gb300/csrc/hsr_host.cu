@@ -1,0 +1,562 @@
+// hsr_host.cu -- C ABI and host orchestration of the GB300 inverse iteration.
+//
+// The drop-in tiled_inverse_iteration (inverse_iteration.h:19-22) copies H and
+// the shifts to the device, runs the sweep of tile columns, the convergence
+// check and the restart rounds (inverse_iteration.c:176-205, restated with the
+// intended semantics), and copies vr and wr back.  Workspaces are cached per
+// host thread and grow on demand.
+#include "hsr_kernels.h"
+#include "../../include/hsrq3in_gb300.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+namespace hsr {
+namespace {
+
+thread_local int g_last_status = HSR_OK;
+thread_local long g_launches = 0;
+
+#define HSR_CK(x)                                  \
+    do {                                           \
+        cudaError_t e_ = (x);                      \
+        if (e_ != cudaSuccess) {                   \
+            last_cuda_error() = e_;                \
+            return HSR_ERR_CUDA;                   \
+        }                                          \
+    } while (0)
+#define HSR_LAUNCH(x)                              \
+    do {                                           \
+        ++g_launches;                              \
+        HSR_CK(x);                                 \
+    } while (0)
+
+cudaError_t &last_cuda_error() {
+    static thread_local cudaError_t e = cudaSuccess;
+    return e;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point, so the
+// library does not link libcuda directly.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+// 2-D FP64 tensor map: inner extent `inner` (contiguous), outer extent
+// `outer`, row pitch `ld` elements, box {bx, by}; out-of-range reads are 0.
+bool make_map(CUtensorMap *m, const double *base, unsigned long long inner, unsigned long long outer,
+              unsigned long long ld, unsigned bx, unsigned by) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {inner, outer};
+    cuuint64_t strides[1] = {ld * sizeof(double)};
+    cuuint32_t box[2] = {bx, by};
+    cuuint32_t es[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double *>(base), dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+inline long long round_up(long long x, long long m) { return (x + m - 1) / m * m; }
+
+// Device buffer that only grows.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t b) {
+        if (b <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e == cudaSuccess) bytes = b;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+struct Workspace {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    DevBuf H, X, wr, R, Cr, Sr, beta, ynorm, W, Zs, vecs, Zslow, slow, pert, fr, bits, err, colnorm,
+        status, scale, tmpX, perm, gscratch, probe;
+    ~Workspace() { release(); }
+    void release() {
+        DevBuf *all[] = {&H, &X, &wr, &R, &Cr, &Sr, &beta, &ynorm, &W, &Zs, &vecs, &Zslow, &slow, &pert,
+                         &fr, &bits, &err, &colnorm, &status, &scale, &tmpX, &perm, &gscratch, &probe};
+        for (DevBuf *b : all) b->release();
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+};
+
+Workspace &ws() {
+    static thread_local Workspace w;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (w.device != dev) {
+        w.release();
+        w.device = dev;
+    }
+    return w;
+}
+
+// One solve over a column range: the sweep J = T-1 .. 0, finalize, normalize.
+struct Solver {
+    int n, T, tlsz, is;
+    std::vector<int> fr;
+    const double *H;
+    long long ldh;
+    double *X;      // column 0 of the whole block
+    long long ldx;
+    double *wr;     // device shifts of the whole block
+    int S;          // columns of the whole block
+    int Scap;       // columns per pass (workspace capacity)
+    int Spad;
+    double smlnum;
+    cudaStream_t st;
+    Workspace *w;
+    CUtensorMap tmH, tmW, tmZ;
+    double *eps3_dev;
+    int *d_status;     // [S] per final column
+    double *d_colnorm; // [S]
+    double *d_scale;   // [S] or null
+    unsigned char *d_pert;  // [S]
+};
+
+DevProblem problem_for(const Solver &s, int off, int cnt) {
+    Workspace &w = *s.w;
+    DevProblem P{};
+    P.n = s.n;
+    P.T = s.T;
+    P.S = cnt;
+    P.Spad = s.Spad;
+    P.tlsz = s.tlsz;
+    P.fr = w.fr.as<int>();
+    P.H = s.H;
+    P.ldh = s.ldh;
+    P.wr = s.wr + off;
+    P.X = s.X + (size_t)off * s.ldx;
+    P.ldx = s.ldx;
+    P.R = w.R.as<double>();
+    P.ldr = round_up(s.n, 4);
+    P.Cr = w.Cr.as<double>();
+    P.Sr = w.Sr.as<double>();
+    P.beta = w.beta.as<double>();
+    P.ynorm = w.ynorm.as<double>();
+    P.Hn = w.bits.as<double>();
+    P.hn = w.bits.as<double>() + (size_t)s.T * s.T;
+    P.W = w.W.as<double>();
+    P.Zs = w.Zs.as<double>();
+    double *v = w.vecs.as<double>();
+    P.pi = v;
+    P.ytil = v + s.Spad;
+    P.z2n = v + 2 * (size_t)s.Spad;
+    P.zlast = v + 3 * (size_t)s.Spad;
+    P.Zslow = w.Zslow.as<double>();
+    P.slow = w.slow.as<unsigned char>();
+    P.pert = s.d_pert + off;
+    P.smlnum = s.smlnum;
+    P.is = s.is;
+    P.err = w.err.as<int>();
+    return P;
+}
+
+// Runs columns [off, off+cnt) through one pass; mode as launch_init.
+int run_pass(Solver &s, int mode, int its, int off, int cnt) {
+    for (int c0 = 0; c0 < cnt; c0 += s.Scap) {
+        const int cc = std::min(s.Scap, cnt - c0);
+        DevProblem P = problem_for(s, off + c0, cc);
+        HSR_LAUNCH(launch_init(P, mode, s.eps3_dev, its, s.st));
+        if (mode == 2) ++g_launches;
+        const int b = s.tlsz;
+        const bool big = (size_t)(64 * b + 2 * (b + 1)) * sizeof(double) > 200 * 1024;
+        double *gs = big ? s.w->gscratch.as<double>() : nullptr;
+        for (int J = s.T - 1; J >= 0; --J) {
+            const int bj = s.fr[J + 1] - s.fr[J];
+            HSR_LAUNCH(launch_diag(P, J, bj, big ? gs : nullptr, s.st));
+            if (J == 0) break;
+            HSR_LAUNCH(launch_part1(P, J, s.st));
+            HSR_LAUNCH(launch_gemm(P, J, s.fr[J], s.tmH, s.tmW, s.tmZ, s.st));
+        }
+        HSR_LAUNCH(launch_finalize(P, s.d_colnorm + off + c0, s.d_status + off + c0,
+                                   s.d_scale ? s.d_scale + off + c0 : nullptr, s.st));
+        HSR_LAUNCH(launch_normalize(P, s.d_colnorm + off + c0, s.d_status + off + c0, s.st));
+    }
+    return HSR_OK;
+}
+
+void partition(int n, int T, int tlsz, std::vector<int> &p) {
+    p.assign(T + 1, 0);
+    for (int i = 1; i < T; ++i) p[i] = n - (T - i) * tlsz;
+    p[0] = 0;
+    p[T] = n;
+}
+
+// Core: device H (ldh even, aligned), device X (n x S, ldx), device wr.
+int solve_device(int n, const double *dH, long long ldh, int S, double *dwr, int tlsz, double *dX,
+                 long long ldx, const hsr_options *opt, cudaStream_t st, double *d_scale_user,
+                 int *d_status_user, std::vector<int> *h_status, std::vector<unsigned char> *h_pert,
+                 std::vector<double> *h_scale, std::vector<double> *h_norm, std::vector<double> *h_tile_scales) {
+    Workspace &w = ws();
+    hsr_options o{};
+    if (opt) o = *opt;
+    Solver s{};
+    s.n = n;
+    s.tlsz = tlsz;
+    s.T = (n + tlsz - 1) / tlsz;
+    s.is = o.intscale ? 1 : 0;
+    partition(n, s.T, tlsz, s.fr);
+    s.H = dH;
+    s.ldh = ldh;
+    s.X = dX;
+    s.ldx = ldx;
+    s.wr = dwr;
+    s.S = S;
+    s.st = st;
+    s.w = &w;
+    {
+        const double eps = DBL_EPSILON / 2;
+        s.smlnum = std::fmax(2 * DBL_MIN, DBL_MIN * ((double)n / eps));
+    }
+    const int T = s.T;
+    // Workspace per column: R, Cr, Sr, Zslow (~n each), W/Zs (tlsz each),
+    // beta/ynorm (T each), slow (T bytes).  Cap the pass width by the budget.
+    {
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        double budget = o.hbm_budget_bytes > 0 ? o.hbm_budget_bytes : 0.6 * (double)free_b;
+        const double per_col = 8.0 * (4.0 * round_up(n, 4) + 2.0 * tlsz + 2.0 * T + 8) + T;
+        long long cap = (long long)(budget / per_col);
+        cap = std::max<long long>(32, std::min<long long>(cap, S));
+        cap = std::min<long long>(cap, 65535);  // grid.y extent of the per-column kernels
+        s.Scap = (int)cap;
+    }
+    s.Spad = (int)round_up(s.Scap, 64);
+    const size_t Sp = (size_t)s.Spad;
+    const size_t ldr = (size_t)round_up(n, 4);
+    HSR_CK(w.R.ensure(ldr * Sp * 8));
+    HSR_CK(w.Cr.ensure((size_t)n * Sp * 8));
+    HSR_CK(w.Sr.ensure((size_t)n * Sp * 8));
+    HSR_CK(w.beta.ensure((size_t)T * Sp * 8));
+    HSR_CK(w.ynorm.ensure((size_t)T * Sp * 8));
+    HSR_CK(w.W.ensure((size_t)tlsz * Sp * 8));
+    HSR_CK(w.Zs.ensure((size_t)tlsz * Sp * 8));
+    HSR_CK(w.vecs.ensure(4 * Sp * 8));
+    HSR_CK(w.Zslow.ensure((size_t)T * tlsz * Sp * 8));
+    HSR_CK(w.slow.ensure((size_t)T * Sp));
+    HSR_CK(w.fr.ensure((size_t)(T + 1) * sizeof(int)));
+    HSR_CK(w.bits.ensure((2 * (size_t)T * T + 2) * 8));
+    HSR_CK(w.err.ensure(16));
+    HSR_CK(w.colnorm.ensure((size_t)S * 8));
+    HSR_CK(w.status.ensure((size_t)S * sizeof(int)));
+    HSR_CK(w.pert.ensure((size_t)S));
+    if (!d_scale_user && (h_scale || h_tile_scales)) HSR_CK(w.scale.ensure((size_t)S * 8));
+    if ((size_t)(64 * tlsz + 2 * (tlsz + 1)) * sizeof(double) > 200 * 1024)
+        HSR_CK(w.gscratch.ensure((size_t)((Sp + 31) / 32) * 64 * tlsz * 8));
+    HSR_CK(cudaMemsetAsync(w.W.p, 0, (size_t)tlsz * Sp * 8, st));
+    HSR_CK(cudaMemsetAsync(w.Zs.p, 0, (size_t)tlsz * Sp * 8, st));
+    HSR_CK(cudaMemsetAsync(w.err.p, 0, 16, st));
+    HSR_CK(cudaMemcpyAsync(w.fr.p, s.fr.data(), (T + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+    s.d_status = d_status_user ? d_status_user : w.status.as<int>();
+    s.d_colnorm = w.colnorm.as<double>();
+    s.d_scale = d_scale_user ? d_scale_user : (w.scale.bytes ? w.scale.as<double>() : nullptr);
+    s.d_pert = w.pert.as<unsigned char>();
+
+    if (!make_map(&s.tmH, dH, (unsigned long long)n, (unsigned long long)n, (unsigned long long)ldh, kGemmBM,
+                  kGemmKC) ||
+        !make_map(&s.tmW, w.W.as<double>(), Sp, (unsigned long long)tlsz, Sp, kGemmBN, kGemmKC) ||
+        !make_map(&s.tmZ, w.Zs.as<double>(), Sp, (unsigned long long)tlsz, Sp, kGemmBN, kGemmKC))
+        return HSR_ERR_CUDA;
+
+    // Norms and eps3.
+    unsigned long long *bits = w.bits.as<unsigned long long>();
+    HSR_CK(cudaMemsetAsync(bits, 0, (2 * (size_t)T * T + 2) * 8, st));
+    {
+        DevProblem P0 = problem_for(s, 0, std::min(S, s.Scap));
+        HSR_LAUNCH(launch_norms(P0, bits, bits + (size_t)T * T, bits + 2 * (size_t)T * T,
+                                w.err.as<int>() + 1, st));
+        ++g_launches;
+    }
+    double hinf = 0.0;
+    HSR_CK(cudaMemcpyAsync(&hinf, bits + 2 * (size_t)T * T, 8, cudaMemcpyDeviceToHost, st));
+    int nanflag[2] = {0, 0};
+    HSR_CK(cudaMemcpyAsync(nanflag, w.err.as<int>(), 8, cudaMemcpyDeviceToHost, st));
+    HSR_CK(cudaStreamSynchronize(st));
+    if (nanflag[1] & 1) hinf = NAN;
+    const double eps3 = hinf * (DBL_EPSILON / 2);
+    s.eps3_dev = reinterpret_cast<double *>(bits + 2 * (size_t)T * T + 1);
+    HSR_CK(cudaMemcpyAsync(s.eps3_dev, &eps3, 8, cudaMemcpyHostToDevice, st));
+
+    const bool user_rhs = o.user_rhs != 0;
+    if (S > 0) {
+        int rc = run_pass(s, user_rhs ? 2 : 0, 0, 0, S);
+        if (rc) return rc;
+    }
+
+    // Convergence and restarts (intended semantics of inverse_iteration.c:176-205).
+    std::vector<int> st_h(S);
+    std::vector<double> wr_h;
+    int front = 0, its = 0;
+    const int max_its = o.max_restarts < 0 ? n : std::min(o.max_restarts, n);
+    int result = HSR_OK;
+    while (S > 0) {
+        HSR_CK(cudaMemcpyAsync(st_h.data() + front, s.d_status + front, (S - front) * sizeof(int),
+                               cudaMemcpyDeviceToHost, st));
+        HSR_CK(cudaStreamSynchronize(st));
+        int all = 1;
+        for (int k = front; k < S; ++k)
+            if (!st_h[k]) all = 0;
+        if (all || user_rhs || its >= max_its) break;
+        // Stable partition of [front, S): converged first.
+        const int m = S - front;
+        std::vector<int> perm;
+        perm.reserve(m);
+        for (int k = 0; k < m; ++k)
+            if (st_h[front + k]) perm.push_back(k);
+        const int nc = (int)perm.size();
+        for (int k = 0; k < m; ++k)
+            if (!st_h[front + k]) perm.push_back(k);
+        HSR_CK(w.tmpX.ensure((size_t)n * m * 8));
+        HSR_CK(w.perm.ensure((size_t)m * sizeof(int)));
+        HSR_CK(cudaMemcpyAsync(w.perm.p, perm.data(), m * sizeof(int), cudaMemcpyHostToDevice, st));
+        HSR_LAUNCH(launch_gather_cols(w.tmpX.as<double>(), n, dX + (size_t)front * ldx, ldx, n,
+                                      w.perm.as<int>(), m, st));
+        HSR_CK(cudaMemcpy2DAsync(dX + (size_t)front * ldx, ldx * 8, w.tmpX.p, (size_t)n * 8, (size_t)n * 8, m,
+                                 cudaMemcpyDeviceToDevice, st));
+        // Permute the small per-column arrays on the host.
+        auto permute = [&](auto *dptr, size_t elem) -> int {
+            if (!dptr) return HSR_OK;
+            std::vector<unsigned char> a((size_t)m * elem), b((size_t)m * elem);
+            HSR_CK(cudaMemcpyAsync(a.data(), reinterpret_cast<unsigned char *>(dptr) + (size_t)front * elem,
+                                   (size_t)m * elem, cudaMemcpyDeviceToHost, st));
+            HSR_CK(cudaStreamSynchronize(st));
+            for (int j = 0; j < m; ++j) memcpy(&b[(size_t)j * elem], &a[(size_t)perm[j] * elem], elem);
+            HSR_CK(cudaMemcpyAsync(reinterpret_cast<unsigned char *>(dptr) + (size_t)front * elem, b.data(),
+                                   (size_t)m * elem, cudaMemcpyHostToDevice, st));
+            HSR_CK(cudaStreamSynchronize(st));
+            return HSR_OK;
+        };
+        int rc;
+        if ((rc = permute(dwr, 8))) return rc;
+        if ((rc = permute(s.d_scale, 8))) return rc;
+        if ((rc = permute(s.d_pert, 1))) return rc;
+        if ((rc = permute(s.d_status, sizeof(int)))) return rc;
+        if ((rc = permute(s.d_colnorm, 8))) return rc;
+        for (int j = 0; j < nc; ++j) st_h[front + j] = 1;
+        front += nc;
+        rc = run_pass(s, 1, its, front, S - front);
+        if (rc) return rc;
+        ++its;
+    }
+    int nonconv = 0;
+    for (int k = 0; k < S; ++k) nonconv += !st_h[k];
+    if (nonconv) result = HSR_ERR_NOT_CONVERGED;
+
+    int errw = 0;
+    HSR_CK(cudaMemcpyAsync(&errw, w.err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    HSR_CK(cudaStreamSynchronize(st));
+    if (errw) return HSR_ERR_DEVICE;
+    if (h_status) *h_status = st_h;
+    if (h_pert) {
+        h_pert->resize(S);
+        HSR_CK(cudaMemcpy(h_pert->data(), s.d_pert, S, cudaMemcpyDeviceToHost));
+    }
+    if (h_scale && s.d_scale) {
+        h_scale->resize(S);
+        HSR_CK(cudaMemcpy(h_scale->data(), s.d_scale, (size_t)S * 8, cudaMemcpyDeviceToHost));
+    }
+    if (h_norm) {
+        h_norm->resize(S);
+        HSR_CK(cudaMemcpy(h_norm->data(), s.d_colnorm, (size_t)S * 8, cudaMemcpyDeviceToHost));
+    }
+    if (h_tile_scales) {
+        // Per-tile factors of the last pass of each column (valid when one
+        // pass covered every column).
+        h_tile_scales->assign((size_t)T * S, 0.0);
+        if (S <= s.Scap) {
+            std::vector<double> tmp((size_t)T * Sp);
+            HSR_CK(cudaMemcpy(tmp.data(), w.beta.p, (size_t)T * Sp * 8, cudaMemcpyDeviceToHost));
+            for (int I = 0; I < T; ++I)
+                for (int k = 0; k < S; ++k) (*h_tile_scales)[(size_t)I * S + k] = tmp[(size_t)I * Sp + k];
+        }
+    }
+    return result;
+}
+
+int check_args(int n, int ldH, int nrhs, int tlsz, int ldvr, const void *H, const void *wr, const void *vr) {
+    if (n <= 0 || ldH < n || nrhs < 0 || tlsz <= 0 || (tlsz % 4) != 0 || ldvr < n || !H) return HSR_ERR_ARG;
+    if (nrhs > 0 && (!wr || !vr)) return HSR_ERR_ARG;
+    return HSR_OK;
+}
+
+int host_call(int n, const double *H, int ldH, int nrhs, double *wr, int tlsz, int rhs_tlsz, double *vr,
+              int ldvr, const hsr_options *opt, hsr_column_info *info) {
+    g_launches = 0;
+    int rc = check_args(n, ldH, nrhs, tlsz, ldvr, H, wr, vr);
+    if (rc) return rc;
+    if (rhs_tlsz <= 0) return HSR_ERR_ARG;
+    if (nrhs == 0) return HSR_OK;
+    Workspace &w = ws();
+    if (!w.stream) HSR_CK(cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking));
+    cudaStream_t st = w.stream;
+    const long long ldh = round_up(n, 32);
+    const long long ldx = round_up(n, 32);
+    HSR_CK(w.H.ensure((size_t)ldh * n * 8));
+    HSR_CK(w.X.ensure((size_t)ldx * nrhs * 8));
+    HSR_CK(w.wr.ensure((size_t)nrhs * 8));
+    HSR_CK(cudaMemcpy2DAsync(w.H.p, ldh * 8, H, (size_t)ldH * 8, (size_t)n * 8, n, cudaMemcpyHostToDevice, st));
+    HSR_CK(cudaMemcpyAsync(w.wr.p, wr, (size_t)nrhs * 8, cudaMemcpyHostToDevice, st));
+    hsr_options o{};
+    if (opt) o = *opt;
+    if (o.user_rhs)
+        HSR_CK(cudaMemcpy2DAsync(w.X.p, ldx * 8, vr, (size_t)ldvr * 8, (size_t)n * 8, nrhs,
+                                 cudaMemcpyHostToDevice, st));
+    std::vector<int> hs;
+    std::vector<unsigned char> hp;
+    std::vector<double> hsc, hn, hts;
+    const bool want = info != nullptr;
+    rc = solve_device(n, w.H.as<double>(), ldh, nrhs, w.wr.as<double>(), tlsz, w.X.as<double>(), ldx, &o, st,
+                      nullptr, nullptr, want && info->status ? &hs : nullptr,
+                      want && info->perturbed ? &hp : nullptr, want && info->scale ? &hsc : nullptr,
+                      want && info->norm ? &hn : nullptr, want && info->tile_scales ? &hts : nullptr);
+    if (rc < 0) return rc;
+    HSR_CK(cudaMemcpy2DAsync(vr, (size_t)ldvr * 8, w.X.p, ldx * 8, (size_t)n * 8, nrhs, cudaMemcpyDeviceToHost, st));
+    HSR_CK(cudaMemcpyAsync(wr, w.wr.p, (size_t)nrhs * 8, cudaMemcpyDeviceToHost, st));
+    HSR_CK(cudaStreamSynchronize(st));
+    if (want) {
+        if (info->status) memcpy(info->status, hs.data(), (size_t)nrhs * sizeof(int));
+        if (info->perturbed) memcpy(info->perturbed, hp.data(), (size_t)nrhs);
+        if (info->scale) memcpy(info->scale, hsc.data(), (size_t)nrhs * 8);
+        if (info->norm) memcpy(info->norm, hn.data(), (size_t)nrhs * 8);
+        if (info->tile_scales) memcpy(info->tile_scales, hts.data(), hts.size() * 8);
+    }
+    return rc;
+}
+
+}  // namespace
+}  // namespace hsr
+
+using namespace hsr;
+
+extern "C" {
+
+int hsr_last_status(void) { return g_last_status; }
+
+const char *hsr_status_string(int status) {
+    switch (status) {
+    case HSR_OK: return "ok";
+    case HSR_ERR_ARG: return "invalid argument";
+    case HSR_ERR_NOMEM: return "out of memory";
+    case HSR_ERR_CUDA: return cudaGetErrorString(last_cuda_error());
+    case HSR_ERR_DEVICE: return "device kernel reported an internal error";
+    case HSR_ERR_NOT_CONVERGED: return "some columns did not converge";
+    default: return "unknown status";
+    }
+}
+
+void tiled_inverse_iteration(int n, const double *H, int ldH, int nrhs, double *wr, int tlsz, int rhs_tlsz,
+                             double *vr, int ldvr) {
+    g_last_status = host_call(n, H, ldH, nrhs, wr, tlsz, rhs_tlsz, vr, ldvr, nullptr, nullptr);
+}
+
+int hsr_inverse_iteration_ex(int n, const double *H, int ldH, int nrhs, double *wr, int tlsz, int rhs_tlsz,
+                             double *vr, int ldvr, const hsr_options *opt, hsr_column_info *info) {
+    g_last_status = host_call(n, H, ldH, nrhs, wr, tlsz, rhs_tlsz, vr, ldvr, opt, info);
+    return g_last_status;
+}
+
+int hsr_inverse_iteration_device(int n, const double *dH, int lddH, int nrhs, double *dwr, int tlsz, double *dvr,
+                                 int lddvr, const hsr_options *opt, void *stream, int *d_status, double *d_scale) {
+    g_launches = 0;
+    int rc = check_args(n, lddH, nrhs, tlsz, lddvr, dH, dwr, dvr);
+    if (rc) return g_last_status = rc;
+    if (nrhs == 0) return g_last_status = HSR_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const double *Huse = dH;
+    long long ldh = lddH;
+    if ((lddH & 1) || (reinterpret_cast<uintptr_t>(dH) & 15)) {
+        // TMA needs an even pitch and a 16-byte aligned base: use a padded copy.
+        Workspace &w = ws();
+        ldh = round_up(n, 32);
+        cudaError_t e = w.H.ensure((size_t)ldh * n * 8);
+        if (e == cudaSuccess)
+            e = cudaMemcpy2DAsync(w.H.p, ldh * 8, dH, (size_t)lddH * 8, (size_t)n * 8, n, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) {
+            last_cuda_error() = e;
+            return g_last_status = HSR_ERR_CUDA;
+        }
+        Huse = w.H.as<double>();
+    }
+    rc = solve_device(n, Huse, ldh, nrhs, dwr, tlsz, dvr, lddvr, opt, st, d_scale, d_status, nullptr, nullptr,
+                      nullptr, nullptr, nullptr);
+    return g_last_status = rc;
+}
+
+long hsr_last_launch_count(void) { return g_launches; }
+
+void hsr_release_workspace(void) { ws().release(); }
+
+int hsr_probe_fp64_peak(double ms_target, double *dfma_gflops, double *dmma_gflops) {
+    Workspace &w = ws();
+    if (w.probe.ensure(64) != cudaSuccess) return HSR_ERR_CUDA;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = sms * 4;
+    auto measure = [&](bool dmma, double *out) -> int {
+        int iters = 1024;
+        float ms = 0.f;
+        for (int rep = 0; rep < 8; ++rep) {
+            cudaEventRecord(e0, 0);
+            cudaError_t e = dmma ? launch_probe_dmma(w.probe.as<double>(), blocks, iters, 0)
+                                 : launch_probe_dfma(w.probe.as<double>(), blocks, iters, 0);
+            cudaEventRecord(e1, 0);
+            if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) return HSR_ERR_CUDA;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms >= ms_target || iters > (1 << 24)) break;
+            iters = (int)std::min<double>((double)iters * std::max(2.0, 1.2 * ms_target / std::max(ms, 0.01f)),
+                                          (double)(1 << 24));
+        }
+        const double warps = (double)blocks * 8;
+        const double flops = dmma ? warps * iters * 4.0 * 2.0 * 256 : warps * 32 * iters * 8.0 * 2.0;
+        *out = flops / (ms * 1e-3) / 1e9;
+        return HSR_OK;
+    };
+    int rc = HSR_OK;
+    if (dfma_gflops) rc |= measure(false, dfma_gflops);
+    if (dmma_gflops) rc |= measure(true, dmma_gflops);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc ? HSR_ERR_CUDA : HSR_OK;
+}
+
+const char *hsr_version(void) { return "hsrq3in_gb300 0.1 (sm_103a, FP64 DFMA)"; }
+
+}  // extern "C"

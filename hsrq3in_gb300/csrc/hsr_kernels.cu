@@ -1,0 +1,821 @@
+// hsr_kernels.cu -- sm_103a kernels of the robust level-3 inverse iteration.
+//
+// One solve sweeps the row tiles J = T-1 .. 0 (tile 0 is the short one,
+// partition.c:7-17).  For every J >= 1 three kernels run:
+//   k_diag   lane-per-shift: Givens generation of the diagonal tile fused with
+//            the robust back-substitution (reduce.c:27-68 + solve-task.c:19-119),
+//            then the stage operands W (crossover coefficients) and Zs (rotated
+//            solved tile, update-task.c:170-198).
+//   k_part1  warp-per-(tile, shift): scale consistency and the rank-1 update
+//            with the column left of tile J (update-task.c:68-174), and the
+//            Part-2 overflow decision (update-task.c:206-226).
+//   k_gemm   TMA-fed DFMA GEMM over H(0:fr[J], fr[J]-1 : fr[J+1]-1) against
+//            [W | Zs]; the epilogue advances the crossover columns
+//            (reduceOffdiagBlocked, reduce.c:73-143, in prefix-product form)
+//            and applies the tile update with its rank-1 crossover term
+//            (update-task.c:233-248), folding the new ||Y||_oo bounds.
+// Tile 0 runs k_diag in its factor_and_solve_R11 form (solve-task.c:123-225),
+// then k_finalize reconciles the scaling factors and back-transforms
+// (shifted_Hessenberg_solve.c:153-260) and k_normalize divides by the norm.
+//
+// FP64 on this part issues at ~2 lane-FMA per clock per SM whether or not a
+// lane is active, so sequential per-shift work runs one shift per lane, and
+// magnitude maxima run on the integer pipe over |x| bit patterns.
+#include "hsr_device.cuh"
+#include "hsr_kernels.h"
+
+#include <cfloat>
+
+namespace hsr {
+
+// --------------------------------------------------------------- norms
+// Row sums of |H| accumulated column by column in order, as LAPACK dlange
+// 'I' does (utils.c:155-174): per (row, tile J >= tile(row)) for the tile
+// norms, and over all columns for ||H||_oo.
+__global__ void k_tile_rowsums(DevProblem P, unsigned long long *Hn_bits,
+                               unsigned long long *hn_bits, int *nan_flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y;
+    if (i >= P.n) return;
+    const int T = P.T;
+    int I = T - 1 - (P.n - 1 - i) / P.tlsz;
+    if (I < 0) I = 0;
+    if (J < I) return;
+    const int c0 = P.fr[J], c1 = P.fr[J + 1];
+    double sum = 0.0;
+    const double *row = P.H + i;
+    for (int c = c0; c < c1; ++c) sum += fabs(row[(size_t)c * P.ldh]);
+    if (sum != sum) atomicOr(nan_flag, 1 << 1);
+    atomicMax(&Hn_bits[I + (size_t)J * T], (unsigned long long)__double_as_longlong(sum));
+    if (J > I) {
+        // hnrm: |H(i, fr[J]-1)| for the Part-1 column (update-task.c:124)
+        atomicMax(&hn_bits[I + (size_t)J * T], abs_bits(row[(size_t)(c0 - 1) * P.ldh]));
+    }
+}
+
+__global__ void k_full_rowsums(DevProblem P, unsigned long long *hinf_bits, int *nan_flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    double sum = 0.0;
+    const double *row = P.H + i;
+    for (int c = 0; c < P.n; ++c) sum += fabs(row[(size_t)c * P.ldh]);
+    if (sum != sum) atomicOr(nan_flag, 1);
+    atomicMax(hinf_bits, (unsigned long long)__double_as_longlong(sum));
+}
+
+cudaError_t launch_norms(const DevProblem &P, unsigned long long *Hn_bits,
+                         unsigned long long *hn_bits, unsigned long long *hinf_bits,
+                         int *nan_flag, cudaStream_t st) {
+    dim3 g((P.n + 127) / 128, P.T);
+    k_tile_rowsums<<<g, 128, 0, st>>>(P, Hn_bits, hn_bits, nan_flag);
+    k_full_rowsums<<<(P.n + 127) / 128, 128, 0, st>>>(P, hinf_bits, nan_flag);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- init
+// Start vectors (inverse_iteration.c:19-34 and the dlaein-style restart
+// vector :36-57), bounds, unit scaling factors, and the initial crossover
+// columns H(:, n-1) with the shift in the last row (reduce.c:276-308).
+__global__ void k_init(DevProblem P, int mode, const double *eps3_dev, int its) {
+    const int k = blockIdx.y;
+    if (k >= P.S) return;
+    const double eps3 = *eps3_dev;
+    const int n = P.n;
+    const double sq = sqrt((double)n);
+    const double tmp = eps3 / (sq + 1.0);
+    double *x = P.X + (size_t)k * P.ldx;
+    double *r = P.R + (size_t)k * P.ldr;
+    const double *hl = P.H + (size_t)(n - 1) * P.ldh;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double h = hl[i];
+        if (i == n - 1) h = h - P.wr[k];
+        r[i] = h;
+        if (mode == 0) {
+            x[i] = eps3;
+        } else if (mode == 1) {
+            double v = (i == 0) ? eps3 : tmp;
+            if (i == n - 1 - its) v -= eps3 * sq;
+            x[i] = v;
+        }
+    }
+    if (blockIdx.x == 0) {
+        const double ub = fmax(fmax(eps3, tmp), fabs(tmp - eps3 / sq));
+        for (int I = threadIdx.x; I < P.T; I += blockDim.x) {
+            P.beta[(size_t)I * P.Spad + k] = sc_one(P.is);
+            if (mode == 0) P.ynorm[(size_t)I * P.Spad + k] = eps3;
+            else if (mode == 1) P.ynorm[(size_t)I * P.Spad + k] = ub;
+        }
+        if (threadIdx.x == 0) P.pert[k] = 0;
+    }
+}
+
+// Bounds of caller right-hand sides: ||X(I, k)||_oo (mode 2).
+__global__ void k_rhs_bounds(DevProblem P) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int k = blockIdx.x * (blockDim.x >> 5) + warp;
+    const int I = blockIdx.y;
+    if (k >= P.S) return;
+    const int r0 = P.fr[I], m = P.fr[I + 1] - r0;
+    const double *x = P.X + r0 + (size_t)k * P.ldx;
+    unsigned long long mx = 0;
+    for (int i = lane; i < m; i += 32) mx = umax64(mx, abs_bits(x[i]));
+    for (int o = 16; o; o >>= 1) mx = umax64(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) P.ynorm[(size_t)I * P.Spad + k] = from_bits(mx);
+}
+
+cudaError_t launch_init(const DevProblem &P, int mode, const double *eps3_dev, int its,
+                        cudaStream_t st) {
+    int bx = (P.n + 255) / 256;
+    if (bx > 64) bx = 64;
+    dim3 g(bx, P.S);
+    k_init<<<g, 256, 0, st>>>(P, mode, eps3_dev, its);
+    if (mode == 2) {
+        dim3 g2((P.S + 7) / 8, P.T);
+        k_rhs_bounds<<<g2, 256, 0, st>>>(P);
+    }
+    return cudaGetLastError();
+}
+
+// -------------------------------------------------------------- diagonal
+// One lane per shift.  v (running column) and y (solution tile) live in
+// shared memory as [row][lane] so that every access is conflict-free; the
+// column of H needed by step j is staged one step ahead with cp.async and
+// read as a broadcast.  When 2*32*b doubles do not fit, v/y live in a global
+// scratch region instead (same code through generic pointers).
+size_t diag_smem_bytes(int b) {
+    const size_t full = (size_t)(64 * b + 2 * (b + 1)) * sizeof(double);
+    return full <= 200 * 1024 ? full : (size_t)(2 * (b + 1)) * sizeof(double);
+}
+
+__global__ void __launch_bounds__(32) k_diag(DevProblem P, int J, double *gscratch) {
+    extern __shared__ double sm[];
+    const int lane = threadIdx.x;
+    const int k0 = blockIdx.x * 32;
+    const int k = k0 + lane;
+    const bool act = k < P.S;
+    const int l = P.fr[J], b = P.fr[J + 1] - l;
+    const bool is = P.is != 0;
+    const size_t Spad = (size_t)P.Spad;
+
+    double *hc = sm;                                   // [2][b+1]
+    double *v, *y;
+    if (gscratch) {
+        v = gscratch + (size_t)blockIdx.x * 64 * b;
+        y = v + (size_t)32 * b;
+    } else {
+        v = sm + 2 * (b + 1);
+        y = v + (size_t)32 * b;
+    }
+#define V(i) v[(size_t)(i) * 32 + lane]
+#define Y(i) y[(size_t)(i) * 32 + lane]
+
+    // Load the crossover column and the right-hand side tile, transposed.
+    for (int c = 0; c < 32; ++c) {
+        const int kc = k0 + c;
+        if (kc < P.S) {
+            const double *rc = P.R + l + (size_t)kc * P.ldr;
+            const double *xc = P.X + l + (size_t)kc * P.ldx;
+            for (int i = lane; i < b; i += 32) {
+                v[(size_t)i * 32 + c] = rc[i];
+                y[(size_t)i * 32 + c] = xc[i];
+            }
+        } else {
+            for (int i = lane; i < b; i += 32) {
+                v[(size_t)i * 32 + c] = 1.0;
+                y[(size_t)i * 32 + c] = 0.0;
+            }
+        }
+    }
+    __syncwarp();
+
+    const double mu = act ? P.wr[k] : 0.0;
+    const double smin = fmax(DBL_EPSILON / 2 * fabs(mu), P.smlnum);
+    const double Hnorm = P.Hn[J + (size_t)J * P.T];
+    double beta = act ? P.beta[(size_t)J * Spad + k] : sc_one(is);
+    int pert = 0;
+
+    // Running maxima of |y(0:j-2)| and |v(0:j-2)| for the next step.
+    unsigned long long ymax = 0, vmax = 0;
+    for (int i = 0; i < b - 2; ++i) {
+        ymax = umax64(ymax, abs_bits(Y(i)));
+        vmax = umax64(vmax, abs_bits(V(i)));
+    }
+
+    const double *Hd = P.H + l + (size_t)l * P.ldh;    // H(l, l)
+    auto stage_col = [&](int col, double *dst) {       // H(l : l+col+1, l+col)
+        int rows = col + 2;
+        if (rows > b) rows = b;
+        const double *src = Hd + (size_t)col * P.ldh;
+        for (int i = lane; i < rows; i += 32) cp_async8(dst + i, src + i);
+        cp_async_commit();
+    };
+    int buf = 0;
+    if (b >= 2) stage_col(b - 2, hc);
+
+    for (int j = b - 1; j >= 1; --j) {
+        cp_async_wait_all();
+        __syncwarp();
+        const double *hcol = hc + buf * (b + 1);       // column j-1 of the tile
+        if (j >= 2) stage_col(j - 2, hc + (buf ^ 1) * (b + 1));
+
+        const double hsub = hcol[j];
+        const double vj = V(j);
+        double c, s;
+        givens(vj, hsub, c, s);
+        if (act) {
+            P.Cr[(size_t)(l + j) * Spad + k] = c;
+            P.Sr[(size_t)(l + j) * Spad + k] = s;
+        }
+
+        // y(j) := y(j) / R(j,j) robustly (solve-task.c:76-81).
+        double yj = Y(j);
+        double phi = sc_one(is);
+        pert |= solve_1x1(smin, c * vj, s * hsub, yj, phi, is);
+        beta = sc_combine(beta, phi, is);
+        {
+            const double a = sc_value(phi, is);
+            if (a != 1.0) {
+                for (int i = 0; i < b; ++i)
+                    if (i != j) Y(i) = a * Y(i);
+                ymax = abs_bits(a * from_bits(ymax));
+            }
+        }
+
+        // y(j-1) (solve-task.c:84-90).
+        const double hdiag = hcol[j - 1] - mu;
+        const double vjm1 = V(j - 1);
+        double yjm1 = Y(j - 1);
+        phi = protect_double_update(fabs(vjm1), fabs(yj), fabs(hdiag), fabs(yj), fabs(yjm1), is);
+        {
+            const double a = sc_value(phi, is);
+            if (a != 1.0) {
+                for (int i = 0; i < b; ++i) Y(i) = a * Y(i);
+                yj = a * yj;
+                yjm1 = a * yjm1;
+                ymax = abs_bits(a * from_bits(ymax));
+            }
+        }
+        beta = sc_combine(beta, phi, is);
+        {
+            const double yc = yj * c, ys = yj * s;
+            yjm1 = fma(ys, hdiag, fma(-yc, vjm1, yjm1));
+        }
+        Y(j - 1) = yjm1;
+
+        // y(0:j-2) (solve-task.c:92-100).
+        phi = protect_double_update(from_bits(vmax), fabs(yj), Hnorm, fabs(yj), from_bits(ymax), is);
+        {
+            const double a = sc_value(phi, is);
+            if (a != 1.0) {
+                for (int i = 0; i < b; ++i) Y(i) = a * Y(i);
+                yj = a * yj;
+            }
+        }
+        beta = sc_combine(beta, phi, is);
+        const double yc = yj * c, ys = yj * s;
+        unsigned long long ymx = 0, vmx = 0;
+        const int lim = j - 1;
+#pragma unroll 4
+        for (int i = 0; i < lim; ++i) {
+            const double h = hcol[i];
+            double yi = Y(i), vi = V(i);
+            yi = fma(ys, h, fma(-yc, vi, yi));
+            vi = fma(c, h, s * vi);
+            Y(i) = yi;
+            V(i) = vi;
+            if (i < lim - 1) {
+                ymx = umax64(ymx, abs_bits(yi));
+                vmx = umax64(vmx, abs_bits(vi));
+            }
+        }
+        // Next annihilation column (solve-task.c:105-108).
+        V(j - 1) = fma(c, hdiag, s * vjm1);
+        Y(j) = yj;
+        ymax = ymx;
+        vmax = vmx;
+        buf ^= 1;
+    }
+    __syncwarp();
+
+    double c0 = 0.0, s0 = 0.0;
+    {
+        double v0 = V(0);
+        double hleft = 0.0;
+        if (J > 0) {
+            // Final rotation with H(l, l-1) (reduce.c:53-61, solve-task.c:111-118).
+            hleft = P.H[l + (size_t)(l - 1) * P.ldh];
+            if (hleft != 0) {
+                givens(v0, hleft, c0, s0);
+            } else {
+                c0 = 1.0;
+                s0 = 0.0;
+            }
+            if (act) {
+                P.Cr[(size_t)l * Spad + k] = c0;
+                P.Sr[(size_t)l * Spad + k] = s0;
+            }
+            v0 = fma(v0, c0, -(hleft * s0));
+        }
+        double y0 = Y(0);
+        double phi = sc_one(is);
+        pert |= solve_1x1(smin, v0, 0.0, y0, phi, is);
+        beta = sc_combine(beta, phi, is);
+        const double a = sc_value(phi, is);
+        if (a != 1.0)
+            for (int i = 1; i < b; ++i) Y(i) = a * Y(i);
+        Y(0) = y0;
+    }
+    __syncwarp();
+
+    // Store the solved tile, its scaling factor and the perturbation flag.
+    for (int c = 0; c < 32; ++c) {
+        const int kc = k0 + c;
+        if (kc < P.S) {
+            double *xc = P.X + l + (size_t)kc * P.ldx;
+            for (int i = lane; i < b; i += 32) xc[i] = y[(size_t)i * 32 + c];
+        }
+    }
+    if (act) {
+        P.beta[(size_t)J * Spad + k] = beta;
+        if (pert) P.pert[k] = 1;
+    }
+    if (J == 0 || !act) return;
+
+    // Stage operands for the tiles above.
+    // W(q) = c_q * prod_{p<q} s_p, pi = prod s (crossover propagation).
+    {
+        double pk = 1.0;
+        for (int q = 0; q < b; ++q) {
+            const double cq = P.Cr[(size_t)(l + q) * Spad + k];
+            const double sq = P.Sr[(size_t)(l + q) * Spad + k];
+            P.W[(size_t)q * Spad + k] = cq * pk;
+            pk = pk * sq;
+        }
+        P.pi[k] = pk;
+    }
+    // Ytilde2 = G_{b-1}^T ... G_1^T (c_0 x_0, x_1, ...) (update-task.c:193-220);
+    // Zs(q) = Ytilde2(q-1), Zs(0) = 0, zlast = Ytilde2(b-1).
+    {
+        unsigned long long zmx = 0;
+        double z = c0 * Y(0);
+        P.Zs[k] = 0.0;
+        for (int q = 1; q < b; ++q) {
+            const double cq = P.Cr[(size_t)(l + q) * Spad + k];
+            const double sq = P.Sr[(size_t)(l + q) * Spad + k];
+            const double t1 = z, t2 = Y(q);
+            const double zo = fma(cq, t1, -(sq * t2));
+            z = fma(sq, t1, cq * t2);
+            P.Zs[(size_t)q * Spad + k] = zo;
+            zmx = umax64(zmx, abs_bits(zo));
+        }
+        zmx = umax64(zmx, abs_bits(z));
+        P.zlast[k] = z;
+        P.z2n[k] = from_bits(zmx);
+        P.ytil[k] = -s0 * Y(0);
+    }
+#undef V
+#undef Y
+}
+
+cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st) {
+    const size_t smem = gscratch ? (size_t)(2 * (b + 1)) * sizeof(double) : diag_smem_bytes(b);
+    static size_t configured = 0;
+    if (smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    k_diag<<<(P.S + 31) / 32, 32, smem, st>>>(P, J, gscratch);
+    return cudaGetLastError();
+}
+
+// --------------------------------------------------------------- Part 1
+// One warp per (tile I < J, shift k): update-task.c:68-174 and the Part-2
+// decision of :206-226.  Columns that need a rescaled Ytilde2 (Y scale below
+// X scale, or a Part-2 factor != 1) get it written to Zslow and are flagged
+// for the protected path of the GEMM epilogue.
+__global__ void __launch_bounds__(256) k_part1(DevProblem P, int J) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int I = blockIdx.y;
+    const int k = blockIdx.x * 8 + warp;
+    if (k >= P.S) return;
+    const bool is = P.is != 0;
+    const size_t Spad = (size_t)P.Spad;
+    const int T = P.T;
+    const int r0 = P.fr[I], m = P.fr[I + 1] - r0;
+    const int l = P.fr[J], b = P.fr[J + 1] - l;
+    const bool applyShift = (I == J - 1);
+    double *y = P.X + r0 + (size_t)k * P.ldx;
+    const double *h = P.H + r0 + (size_t)(l - 1) * P.ldh;
+    const double mu = P.wr[k];
+    double Ys = P.beta[(size_t)I * Spad + k];
+    const double Xs = P.beta[(size_t)J * Spad + k];
+    double Yn = P.ynorm[(size_t)I * Spad + k];
+
+    // Part 0: consistent scaling.
+    if (Xs < Ys) {
+        const double a = sc_upscale(Xs, Ys, is);
+        for (int i = lane; i < m; i += 32) y[i] = a * y[i];
+        Yn = a * Yn;
+        Ys = Xs;
+    }
+    // Part 1: y -= (H(I, l-1) - mu e_last) * ytilde.
+    double ytilde;
+    const double x0 = P.X[l + (size_t)k * P.ldx];
+    const double s0 = P.Sr[(size_t)l * Spad + k];
+    if (Ys < Xs) {
+        const double a = sc_upscale(Ys, Xs, is);
+        ytilde = -s0 * (a * x0);
+    } else {
+        ytilde = -s0 * x0;
+    }
+    const double hnrm = P.hn[I + (size_t)J * T];
+    const double alpha = protect_update(fmax(hnrm, fabs(mu)), fabs(ytilde), Yn, is);
+    const double a = sc_value(alpha, is);
+    unsigned long long mx = 0;
+    if (a != 1.0) {
+        const double at = a * ytilde;
+        for (int i = lane; i < m; i += 32) {
+            double yi = fma(-h[i], at, a * y[i]);
+            if (applyShift && i == m - 1) yi = fma(mu, at, yi);
+            y[i] = yi;
+            mx = umax64(mx, abs_bits(yi));
+        }
+    } else {
+        for (int i = lane; i < m; i += 32) {
+            double yi = fma(-h[i], ytilde, y[i]);
+            if (applyShift && i == m - 1) yi = fma(mu, ytilde, yi);
+            y[i] = yi;
+            mx = umax64(mx, abs_bits(yi));
+        }
+    }
+    Ys = sc_combine(Ys, alpha, is);
+    for (int o = 16; o; o >>= 1) mx = umax64(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    Yn = from_bits(mx);
+
+    // Part 2 decision.  Fast path: Ytilde2 from the unscaled solved tile.
+    bool slow = false;
+    double z2 = P.z2n[k];
+    double *zs = P.Zslow + (size_t)I * P.tlsz * Spad + k;   // zs[q*Spad]
+    if (Ys < Xs) {
+        // X scaled to the Y scale before rotation (update-task.c:196-203).
+        slow = true;
+        const double a2 = sc_upscale(Ys, Xs, is);
+        const double *x = P.X + l + (size_t)k * P.ldx;
+        unsigned long long zmx = 0;
+        double z = P.Cr[(size_t)l * Spad + k] * (a2 * x[0]);
+        for (int q = 1; q < b; ++q) {
+            const double cq = P.Cr[(size_t)(l + q) * Spad + k];
+            const double sq = P.Sr[(size_t)(l + q) * Spad + k];
+            const double t1 = z, t2 = a2 * x[q];
+            const double zo = fma(cq, t1, -(sq * t2));
+            z = fma(sq, t1, cq * t2);
+            if (lane == 0) zs[(size_t)(q - 1) * Spad] = zo;
+            zmx = umax64(zmx, abs_bits(zo));
+        }
+        zmx = umax64(zmx, abs_bits(z));
+        if (lane == 0) zs[(size_t)(b - 1) * Spad] = z;
+        z2 = from_bits(zmx);
+    }
+    const double tsc = protect_update(P.Hn[I + (size_t)J * T], z2, Yn, is);
+    const double ta = sc_value(tsc, is);
+    if (ta != 1.0) {
+        if (!slow) {
+            // Materialise Ytilde2 from the fast-path operand.
+            for (int q = lane; q < b - 1; q += 32) zs[(size_t)q * Spad] = P.Zs[(size_t)(q + 1) * Spad + k];
+            if (lane == 0) zs[(size_t)(b - 1) * Spad] = P.zlast[k];
+            __syncwarp();
+        }
+        slow = true;
+        __syncwarp();
+        for (int q = lane; q < b; q += 32) zs[(size_t)q * Spad] = ta * zs[(size_t)q * Spad];
+        for (int i = lane; i < m; i += 32) y[i] = ta * y[i];
+        Ys = sc_combine(Ys, tsc, is);
+    }
+    __syncwarp();
+    if (lane == 0) {
+        P.beta[(size_t)I * Spad + k] = Ys;
+        P.ynorm[(size_t)I * Spad + k] = 0.0;   // the GEMM epilogue folds the new bound
+        P.slow[(size_t)I * Spad + k] = slow ? 1 : 0;
+    }
+}
+
+cudaError_t launch_part1(const DevProblem &P, int J, cudaStream_t st) {
+    dim3 g((P.S + 7) / 8, J);
+    k_part1<<<g, 256, 0, st>>>(P, J);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ GEMM
+// CTA tile: 64 rows x 64 shifts, both operand halves; 256 threads, each with
+// a 4x4 block of both accumulators.  A = H(rows, l-1 .. l+b-2) and the two
+// B tiles arrive by TMA in 16-column chunks through a 3-stage mbarrier ring.
+// Each accumulator sums k = 0 .. b-1 in order with fma, the same order as
+// the oracle's dot products.
+struct GemmSmem {
+    double A[kGemmStages][kGemmKC][kGemmBM];
+    double W[kGemmStages][kGemmKC][kGemmBN];
+    double Z[kGemmStages][kGemmKC][kGemmBN];
+    uint64_t full[kGemmStages];
+};
+
+size_t gemm_smem_bytes() { return sizeof(GemmSmem) + 128; }
+
+__global__ void __launch_bounds__(256, 2)
+k_gemm(DevProblem P, int J, const __grid_constant__ CUtensorMap tmH,
+       const __grid_constant__ CUtensorMap tmW, const __grid_constant__ CUtensorMap tmZ) {
+    extern __shared__ unsigned char smraw[];
+    GemmSmem &sm = *reinterpret_cast<GemmSmem *>(
+        (reinterpret_cast<uintptr_t>(smraw) + 127) & ~uintptr_t(127));
+    const int tid = threadIdx.x;
+    const int row0 = blockIdx.x * kGemmBM;
+    const int col0 = blockIdx.y * kGemmBN;
+    const int l = P.fr[J], b = P.fr[J + 1] - l;
+    const int nk = (b + kGemmKC - 1) / kGemmKC;
+    const uint32_t bytes = (uint32_t)((kGemmBM + 2 * kGemmBN) * kGemmKC * sizeof(double));
+
+    if (tid == 0) {
+        for (int s = 0; s < kGemmStages; ++s) mbar_init(&sm.full[s], 1);
+        mbar_fence_init();
+        prefetch_tensormap(&tmH);
+        prefetch_tensormap(&tmW);
+        prefetch_tensormap(&tmZ);
+    }
+    __syncthreads();
+    auto issue = [&](int s, int kc) {
+        mbar_expect_tx(&sm.full[s], bytes);
+        tma_load_2d(&sm.A[s][0][0], &tmH, &sm.full[s], row0, l - 1 + kc * kGemmKC);
+        tma_load_2d(&sm.W[s][0][0], &tmW, &sm.full[s], col0, kc * kGemmKC);
+        tma_load_2d(&sm.Z[s][0][0], &tmZ, &sm.full[s], col0, kc * kGemmKC);
+    };
+    if (tid == 0)
+        for (int s = 0; s < kGemmStages && s < nk; ++s) issue(s, s);
+
+    const int tr = tid & 15, tc = tid >> 4;
+    double aw[4][4], az[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) aw[r][c] = az[r][c] = 0.0;
+
+    int issued = nk < kGemmStages ? nk : kGemmStages;
+    bool ok = true;
+    for (int kc = 0; kc < nk; ++kc) {
+        const int s = kc % kGemmStages;
+        const uint32_t par = (uint32_t)((kc / kGemmStages) & 1);
+        const bool got = mbar_wait(&sm.full[s], par, P.err);
+        if (!__syncthreads_and(got)) { ok = false; break; }
+        const int kmax = min(kGemmKC, b - kc * kGemmKC);
+        for (int kk = 0; kk < kmax; ++kk) {
+            const double2 a01 = *reinterpret_cast<const double2 *>(&sm.A[s][kk][4 * tr]);
+            const double2 a23 = *reinterpret_cast<const double2 *>(&sm.A[s][kk][4 * tr + 2]);
+            const double2 w01 = *reinterpret_cast<const double2 *>(&sm.W[s][kk][4 * tc]);
+            const double2 w23 = *reinterpret_cast<const double2 *>(&sm.W[s][kk][4 * tc + 2]);
+            const double2 z01 = *reinterpret_cast<const double2 *>(&sm.Z[s][kk][4 * tc]);
+            const double2 z23 = *reinterpret_cast<const double2 *>(&sm.Z[s][kk][4 * tc + 2]);
+            const double a[4] = {a01.x, a01.y, a23.x, a23.y};
+            const double w[4] = {w01.x, w01.y, w23.x, w23.y};
+            const double z[4] = {z01.x, z01.y, z23.x, z23.y};
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    aw[r][c] = fma(a[r], w[c], aw[r][c]);
+                    az[r][c] = fma(a[r], z[c], az[r][c]);
+                }
+        }
+        __syncthreads();
+        if (tid == 0 && kc + kGemmStages < nk) {
+            issue(s, kc + kGemmStages);
+            ++issued;
+        }
+    }
+    if (!ok) {
+        // Drain the copies still in flight (bounded) before the CTA exits.
+        if (tid == 0)
+            for (int kc = 0; kc < issued; ++kc)
+                mbar_wait(&sm.full[kc % kGemmStages], (uint32_t)((kc / kGemmStages) & 1), P.err, 1L << 20);
+        return;
+    }
+
+    // Epilogue.
+    const int M = l;
+    const size_t Spad = (size_t)P.Spad;
+    unsigned long long *ynb = reinterpret_cast<unsigned long long *>(P.ynorm);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const int col = col0 + 4 * tc + c;
+        if (col >= P.S) continue;
+        const double pik = P.pi[col], w0 = P.W[col], zl = P.zlast[col], mu = P.wr[col];
+        int curI = -1;
+        unsigned long long mx = 0;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int row = row0 + 4 * tr + r;
+            if (row >= M) continue;
+            const size_t ir = row + (size_t)col * P.ldr;
+            const size_t ix = row + (size_t)col * P.ldx;
+            const double rold = P.R[ir];
+            double rnew = fma(pik, rold, aw[r][c]);
+            if (row == l - 1) rnew = fma(-mu, w0, rnew);
+            P.R[ir] = rnew;
+            int I = P.T - 1 - (P.n - 1 - row) / P.tlsz;
+            if (I < 0) I = 0;
+            double yv = P.X[ix];
+            if (P.slow[(size_t)I * Spad + col]) {
+                // Protected path: rescaled Ytilde2 of this (tile, shift).
+                const double *zs = P.Zslow + (size_t)I * P.tlsz * Spad + col;
+                const double *hr = P.H + row + (size_t)l * P.ldh;
+                double acc = 0.0;
+                for (int q = 0; q < b - 1; ++q) acc = fma(hr[(size_t)q * P.ldh], zs[(size_t)q * Spad], acc);
+                yv = yv - acc;
+                yv = fma(-rold, zs[(size_t)(b - 1) * Spad], yv);
+            } else {
+                yv = yv - az[r][c];
+                yv = fma(-rold, zl, yv);
+            }
+            P.X[ix] = yv;
+            if (I != curI) {
+                if (curI >= 0) atomicMax(&ynb[(size_t)curI * Spad + col], mx);
+                curI = I;
+                mx = 0;
+            }
+            mx = umax64(mx, abs_bits(yv));
+        }
+        if (curI >= 0) atomicMax(&ynb[(size_t)curI * Spad + col], mx);
+    }
+}
+
+cudaError_t launch_gemm(const DevProblem &P, int J, int rows, const CUtensorMap &tmH,
+                        const CUtensorMap &tmW, const CUtensorMap &tmZ, cudaStream_t st) {
+    static bool configured = false;
+    const size_t smem = gemm_smem_bytes();
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    if (rows <= 0) return cudaSuccess;
+    dim3 g((rows + kGemmBM - 1) / kGemmBM, (P.S + kGemmBN - 1) / kGemmBN);
+    k_gemm<<<g, 256, smem, st>>>(P, J, tmH, tmW, tmZ);
+    return cudaGetLastError();
+}
+
+// -------------------------------------------------------------- finalize
+// Lane per shift: smin = min_I beta(I,k) (robust.c:58-82), back-transform
+// y <- Q^T y with the tile upscalings (shifted_Hessenberg_solve.c:153-215),
+// three-accumulator 2-norm and the convergence test ||y|| > 0.1/sqrt(n)
+// (:33-40, :229-273).  Rows move through shared memory 32 at a time so that
+// the column-major block is read and written coalesced.
+__global__ void __launch_bounds__(32) k_finalize(DevProblem P, double *colnorm, int *status,
+                                                 double *scale_out) {
+    __shared__ double buf[32][33];
+    const int lane = threadIdx.x;
+    const int k0 = blockIdx.x * 32;
+    const int k = k0 + lane;
+    const bool act = k < P.S;
+    const bool is = P.is != 0;
+    const size_t Spad = (size_t)P.Spad;
+    const int n = P.n;
+
+    double smin = act ? P.beta[k] : sc_one(is);
+    for (int I = 1; I < P.T; ++I)
+        if (act) smin = sc_min(smin, P.beta[(size_t)I * Spad + k], is);
+
+    Nrm3 acc;
+    acc.init();
+    double tau1 = 0.0;
+    int I = 0;
+    double alpha = act ? sc_upscale(smin, P.beta[k], is) : 1.0;
+    for (int r0 = 0; r0 < n; r0 += 32) {
+        const int rows = min(32, n - r0);
+        __syncwarp();
+        for (int c = 0; c < 32; ++c) {
+            const int kc = k0 + c;
+            if (kc < P.S && lane < rows) buf[lane][c] = P.X[r0 + lane + (size_t)kc * P.ldx];
+        }
+        __syncwarp();
+        for (int t = 0; t < rows; ++t) {
+            const int i = r0 + t;
+            if (i == P.fr[I + 1]) {
+                ++I;
+                alpha = act ? sc_upscale(smin, P.beta[(size_t)I * Spad + k], is) : 1.0;
+            }
+            if (i == 0) {
+                tau1 = alpha * buf[0][lane];
+                continue;
+            }
+            const double tau2 = alpha * buf[t][lane];
+            const double c = act ? P.Cr[(size_t)i * Spad + k] : 0.0;
+            const double s = act ? P.Sr[(size_t)i * Spad + k] : 0.0;
+            const double out = fma(c, tau1, -(s * tau2));
+            tau1 = fma(c, tau2, s * tau1);
+            acc.add(out);
+            if (t == 0) {
+                if (act) P.X[(i - 1) + (size_t)k * P.ldx] = out;
+            } else {
+                buf[t - 1][lane] = out;
+            }
+        }
+        __syncwarp();
+        // rows r0 .. r0+rows-2 hold outputs; row r0-1 was written directly.
+        for (int c = 0; c < 32; ++c) {
+            const int kc = k0 + c;
+            if (kc < P.S && lane < rows - 1) P.X[r0 + lane + (size_t)kc * P.ldx] = buf[lane][c];
+        }
+    }
+    if (act) {
+        P.X[(n - 1) + (size_t)k * P.ldx] = tau1;
+        acc.add(tau1);
+        const double ynrm = acc.finish();
+        colnorm[k] = ynrm;
+        status[k] = (ynrm > 0.1 / sqrt((double)n)) ? 1 : 0;
+        if (scale_out) scale_out[k] = smin;
+    }
+}
+
+cudaError_t launch_finalize(const DevProblem &P, double *colnorm, int *status, double *scale_out,
+                            cudaStream_t st) {
+    k_finalize<<<(P.S + 31) / 32, 32, 0, st>>>(P, colnorm, status, scale_out);
+    return cudaGetLastError();
+}
+
+__global__ void k_normalize(DevProblem P, const double *colnorm, const int *status) {
+    const int k = blockIdx.y;
+    if (k >= P.S || !status[k]) return;
+    const double nrm = colnorm[k];
+    double *x = P.X + (size_t)k * P.ldx;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n; i += gridDim.x * blockDim.x)
+        x[i] = x[i] / nrm;
+}
+
+cudaError_t launch_normalize(const DevProblem &P, const double *colnorm, const int *status,
+                             cudaStream_t st) {
+    int bx = (P.n + 255) / 256;
+    if (bx > 64) bx = 64;
+    dim3 g(bx, P.S);
+    k_normalize<<<g, 256, 0, st>>>(P, colnorm, status);
+    return cudaGetLastError();
+}
+
+__global__ void k_gather_cols(double *dst, long long ldd, const double *src, long long lds, int n,
+                              const int *perm) {
+    const int j = blockIdx.y;
+    const double *s = src + (size_t)perm[j] * lds;
+    double *d = dst + (size_t)j * ldd;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) d[i] = s[i];
+}
+
+cudaError_t launch_gather_cols(double *dst, long long ldd, const double *src, long long lds, int n,
+                               const int *perm, int cnt, cudaStream_t st) {
+    if (cnt <= 0) return cudaSuccess;
+    int bx = (n + 255) / 256;
+    if (bx > 64) bx = 64;
+    dim3 g(bx, cnt);
+    k_gather_cols<<<g, 256, 0, st>>>(dst, ldd, src, lds, n, perm);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------- FP64 peak probe
+__global__ void k_probe_dfma(double *out, int iters) {
+    double x[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) x[q] = threadIdx.x * 1e-3 + q;
+    const double a = 0.999999, b = 1e-7;
+    for (int it = 0; it < iters; ++it)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) x[q] = fma(x[q], a, b);
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s += x[q];
+    if (s == 123456.789) out[0] = s;
+}
+
+__global__ void k_probe_dmma(double *out, int iters) {
+    const double a = threadIdx.x * 1e-3, bb = 1.0 - threadIdx.x * 1e-4;
+    double c[4][2];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) c[t][0] = c[t][1] = 0.0;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+            asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                         : "+d"(c[t][0]), "+d"(c[t][1])
+                         : "d"(a), "d"(bb));
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) s += c[t][0] + c[t][1];
+    if (s == 123456.789) out[0] = s;
+}
+
+cudaError_t launch_probe_dfma(double *out, int blocks, int iters, cudaStream_t st) {
+    k_probe_dfma<<<blocks, 256, 0, st>>>(out, iters);
+    return cudaGetLastError();
+}
+cudaError_t launch_probe_dmma(double *out, int blocks, int iters, cudaStream_t st) {
+    k_probe_dmma<<<blocks, 256, 0, st>>>(out, iters);
+    return cudaGetLastError();
+}
+
+}  // namespace hsr

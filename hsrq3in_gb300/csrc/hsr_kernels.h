@@ -1,0 +1,73 @@
+// hsr_kernels.h -- kernel argument block and launch wrappers shared by the
+// host orchestration (hsr_host.cu) and the kernels (hsr_kernels.cu).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+namespace hsr {
+
+// Device-resident state of one solve over S shifts.  Layouts:
+//   H   n x n column-major (ldh even, 16-byte aligned base: TMA source)
+//   X   n x S column-major, the eigenvector block (ldx)
+//   R   n x S column-major, running crossover columns (ldr)
+//   Cr, Sr  Givens rotations, row-major [n][Spad]: Cr[i*Spad + k]
+//   beta, ynorm  per-(tile, shift) scaling factor and bound, [T][Spad]
+//   W, Zs  stage operands [tlsz][Spad]: crossover coefficients and the
+//          rotated solved tile (row 0 of Zs is zero)
+//   Zslow  rescaled copies of Ytilde2 for columns needing overflow
+//          protection, [(T*tlsz)][Spad] indexed by (I*tlsz + q)
+struct DevProblem {
+    int n, T, S, Spad, tlsz;
+    const int *fr;             // first row of each tile, [T+1]
+    const double *H;
+    long long ldh;
+    const double *wr;          // shifts [S]
+    double *X;
+    long long ldx;
+    double *R;
+    long long ldr;
+    double *Cr, *Sr;
+    double *beta, *ynorm;
+    const double *Hn;          // ||H(I,J)||_oo, [T*T], Hn[I + J*T]
+    const double *hn;          // ||H(I, fr[J]-1)||_oo, [T*T]
+    double *W, *Zs;
+    double *pi, *ytil, *z2n, *zlast;   // per-shift stage scalars [Spad]
+    double *Zslow;
+    unsigned char *slow;       // [T][Spad], column needs the protected path
+    unsigned char *pert;       // [Spad], 1x1 solve perturbed
+    double smlnum;
+    int is;                    // integer (base-2 exponent) scaling factors
+    int *err;                  // device error word
+};
+
+// Setup: tile norms, eps3 = ||H||_oo * eps/2.  hnbits/Hnbits/hnorm_bits are
+// zeroed by the caller.
+cudaError_t launch_norms(const DevProblem &P, unsigned long long *Hn_bits,
+                         unsigned long long *hn_bits, unsigned long long *hinf_bits,
+                         int *nan_flag, cudaStream_t st);
+// Initial state.  mode 0: start vector eps3; 1: restart vector (its);
+// 2: caller right-hand sides already in X.
+cudaError_t launch_init(const DevProblem &P, int mode, const double *eps3_dev,
+                        int its, cudaStream_t st);
+cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st);
+size_t diag_smem_bytes(int b);
+cudaError_t launch_part1(const DevProblem &P, int J, cudaStream_t st);
+cudaError_t launch_gemm(const DevProblem &P, int J, int rows, const CUtensorMap &tmH,
+                        const CUtensorMap &tmW, const CUtensorMap &tmZ, cudaStream_t st);
+size_t gemm_smem_bytes();
+cudaError_t launch_finalize(const DevProblem &P, double *colnorm, int *status,
+                            double *scale_out, cudaStream_t st);
+cudaError_t launch_normalize(const DevProblem &P, const double *colnorm,
+                             const int *status, cudaStream_t st);
+// Column gather: dst(:, j) = src(:, perm[j]) for j < cnt.
+cudaError_t launch_gather_cols(double *dst, long long ldd, const double *src,
+                               long long lds, int n, const int *perm, int cnt,
+                               cudaStream_t st);
+// FP64 throughput probe kernels.
+cudaError_t launch_probe_dfma(double *out, int blocks, int iters, cudaStream_t st);
+cudaError_t launch_probe_dmma(double *out, int blocks, int iters, cudaStream_t st);
+
+constexpr int kGemmBM = 64, kGemmBN = 64, kGemmKC = 16, kGemmStages = 3;
+
+}  // namespace hsr

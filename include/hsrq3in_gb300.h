@@ -1,0 +1,113 @@
+/*
+ * hsrq3in_gb300.h -- C ABI of the GB300 (sm_103a) robust level-3 inverse
+ * iteration library (libhsrq3in_gb300.so).
+ *
+ * All entry points use plain C types: pointers, sizes and status codes.
+ * Matrices are column-major, FP64.  Citations name the interface of the
+ * reference (hsrq3in) that each entry point replaces or extends.
+ */
+#ifndef HSRQ3IN_GB300_H
+#define HSRQ3IN_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+    HSR_OK = 0,
+    HSR_ERR_ARG = -1,          /* invalid argument (n, ld, tlsz, ...)            */
+    HSR_ERR_NOMEM = -2,        /* device or host allocation failed               */
+    HSR_ERR_CUDA = -3,         /* a CUDA runtime call failed                     */
+    HSR_ERR_DEVICE = -4,       /* a kernel reported an internal error            */
+    HSR_ERR_NOT_CONVERGED = 1  /* finished; some columns did not converge        */
+};
+
+/* Status of the last call made on this host thread (0 = success). */
+int hsr_last_status(void);
+/* Human-readable text for a status code. */
+const char *hsr_status_string(int status);
+
+/* ---------------------------------------------------------- drop-in call */
+/* Replaces tiled_inverse_iteration (inverse_iteration.h:19-22, implemented at
+ * inverse_iteration.c:128-335).  Same arguments, layout and semantics:
+ *   n       order of the upper-Hessenberg matrix H, n > 0
+ *   H       n x n, column-major, leading dimension ldH >= n (read only)
+ *   nrhs    number of real shifts
+ *   wr      [nrhs] shifts; reordered (converged columns first) only when some
+ *           columns needed a restart, as inverse_iteration.h:10 allows
+ *   tlsz    row tile size, a positive multiple of 4; the first tile is the
+ *           short one (partition.c:7-17)
+ *   rhs_tlsz  column tile size (> 0); accepted for compatibility -- the
+ *           device path computes every column independently
+ *   vr      n x nrhs output, leading dimension ldvr >= n; column k is the
+ *           unit-2-norm eigenvector for wr[k]
+ * Runs on the current CUDA device.  Returns nothing, like the reference;
+ * hsr_last_status() reports errors and non-convergence. */
+void tiled_inverse_iteration(int n, const double *H, int ldH, int nrhs,
+                             double *wr, int tlsz, int rhs_tlsz, double *vr,
+                             int ldvr);
+
+/* ---------------------------------------------------- extended host call */
+typedef struct hsr_options {
+    int intscale;      /* 0: double scaling factors (reference default build);
+                          1: base-2 exponents (reference -DINTSCALING build)   */
+    int user_rhs;      /* 0: eps3 start vectors (inverse_iteration.c:19-34);
+                          1: vr holds caller right-hand sides on entry, one
+                             solve, no restart (shifted_Hessenberg_solve.h:26) */
+    int max_restarts;  /* < 0: up to n rounds as inverse_iteration.c:229       */
+    double hbm_budget_bytes; /* workspace cap for shift batching; 0 = auto    */
+} hsr_options;
+
+/* Per-column outputs (each pointer optional, arrays of length nrhs, in the
+ * final column order). */
+typedef struct hsr_column_info {
+    int *status;            /* 1 converged, 0 not (vrnorms(k,0), shifted_Hessenberg_solve.c:263-273) */
+    unsigned char *perturbed; /* 1 if a 1x1 solve was lifted to smin (robust.c:432-435) */
+    double *scale;          /* reconciled scaling factor smin (robust.c:58-82) */
+    double *tile_scales;    /* optional [num_tiles x nrhs] per-tile scaling factors
+                               before reconciliation (shifted_Hessenberg_solve.c:105-123) */
+    double *norm;           /* 2-norm before normalisation (shifted_Hessenberg_solve.c:229-260) */
+} hsr_column_info;
+
+/* Extended twin of tiled_inverse_iteration with options, per-column outputs
+ * (the scaling factors the reference keeps internal) and a status code. */
+int hsr_inverse_iteration_ex(int n, const double *H, int ldH, int nrhs,
+                             double *wr, int tlsz, int rhs_tlsz, double *vr,
+                             int ldvr, const hsr_options *opt,
+                             hsr_column_info *info);
+
+/* ------------------------------------------------ device-resident call */
+/* Same computation on device pointers (inputs already in HBM), enqueued on
+ * `stream` (a cudaStream_t, NULL = legacy default stream).  dH needs lddH
+ * even and a 16-byte aligned base (TMA); otherwise HSR_ERR_ARG.  Synchronises
+ * the stream once at the end to read convergence status.  Device arrays
+ * d_status/d_scale may be NULL.  Replaces solve_Hessenberg_system_real_shift
+ * (shifted_Hessenberg_solve.h:26-30) plus the driver loop. */
+int hsr_inverse_iteration_device(int n, const double *dH, int lddH, int nrhs,
+                                 double *dwr, int tlsz, double *dvr, int lddvr,
+                                 const hsr_options *opt, void *stream,
+                                 int *d_status, double *d_scale);
+
+/* Number of kernel launches the last call on this thread enqueued. */
+long hsr_last_launch_count(void);
+
+/* Release cached device workspaces of this thread. */
+void hsr_release_workspace(void);
+
+/* ----------------------------------------------------------- diagnostics */
+/* Measured FP64 throughput of this GPU (GFLOP/s): a DFMA stream and a DMMA
+ * (mma.sync m8n8k4 f64) stream, each timed with CUDA events over `ms_target`
+ * milliseconds.  Used as the roofline denominator; no reference counterpart. */
+int hsr_probe_fp64_peak(double ms_target, double *dfma_gflops,
+                        double *dmma_gflops);
+
+/* Library version string. */
+const char *hsr_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1090 @@
+/*
+ * hsro.c -- CPU oracle for hsrq3in's robust level-3 inverse iteration.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA library and the timed
+ * CPU port in the benchmark.  The product never links or calls this file.
+ *
+ * A plain-C restatement of the reference algorithm, written from its
+ * behaviour; each routine names the reference file:line it follows.  The
+ * reference's task DAG (reduce.c:239-394, shifted_Hessenberg_solve.c:126-343)
+ * is replaced by a per-shift-tile sweep over tile columns J = T-1 .. 0 that
+ * interleaves, for each J, the diagonal reduction, the diagonal solve, the
+ * tile updates (which need the crossover column R_I *before* tile J's
+ * rotations are applied to it) and the crossover propagation.  Every
+ * floating-point operation of the reference is executed with the same
+ * operands in the same order; only independent tasks are reordered, which
+ * cannot change a result.  Shift tiles run in parallel (OpenMP).
+ *
+ * Divergences from the reference, all in branches that never execute on
+ * unreduced Hessenberg inputs (the reference's own behaviour there is
+ * undefined or aborts):
+ *   1. update-task.c:218,223 index tmp_scales[k] (k = tile height) instead of
+ *      tmp_scales[rhs]; restated with [rhs].
+ *   2. update-task.c:173-186 decide the X rescale per call (rescale_X): a
+ *      column whose Y scale drops below its X scale only through the Part-1
+ *      factor is copied unscaled when no other column set the flag, and
+ *      columns not below their X scale are left uninitialised when one did;
+ *      restated per column: X is scaled by Yscale/Xscale exactly when the Y
+ *      scale is below the X scale, else copied.
+ *   3. update-task.c:111 uses Yscales/Xscales instead of compute_upscaling
+ *      (wrong for integer scaling); restated with compute_upscaling.
+ *   4. update-task.c:127 scales Y(m-1) by the Part-1 factor twice when the
+ *      shift is applied; restated with a single scaling.
+ *   5. inverse_iteration.c:75-125,176-205 invert "converged" and re-solve the
+ *      converged columns on restart; restated as the intended restart: the
+ *      converged columns move to the front (stable order), the rest get the
+ *      dlaein-style start vector of inverse_iteration.c:36-57 and are
+ *      re-solved, up to n rounds.
+ *   6. reduce.c:265-289 reads H(0,-1) when there is a single tile; that
+ *      reduction's output is unused, so it is skipped here.
+ */
+#include "hsro.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#ifdef HSRO_FMA
+#define HSRO_MODE 1
+#else
+#define HSRO_MODE 0
+#endif
+
+/* dgemm: the same BLAS the reference links (scipy's OpenBLAS, renamed
+ * symbols), else a plain triple loop.                                       */
+#ifdef HSRO_DGEMM
+extern void HSRO_DGEMM(const char *ta, const char *tb, const int *m,
+                       const int *n, const int *k, const double *alpha,
+                       const double *a, const int *lda, const double *b,
+                       const int *ldb, const double *beta, double *c,
+                       const int *ldc);
+#endif
+#ifdef HSRO_BLAS_THREADS
+extern void HSRO_BLAS_THREADS(int);
+#endif
+
+/* Overflow threshold Omega and its reciprocal (robust.c:14-15). */
+static const double g_omega = 1.e+300;
+static const double g_omega_inv = 1.e-300;
+
+int hsro_mode(void) { return HSRO_MODE; }
+
+void hsro_set_threads(int nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* Scaling-factor algebra (robust.c:24-121).  A scaling factor is a double  */
+/* holding either the factor itself (default build) or a base-2 exponent    */
+/* (-DINTSCALING build); `is` selects the representation at run time.      */
+/* ------------------------------------------------------------------------ */
+static inline double sc_one(int is) { return is ? 0.0 : 1.0; }          /* robust.c:24-33 */
+static inline double sc_value(double a, int is)                          /* robust.c:112-121 */
+{ return is ? ldexp(1.0, (int)a) : a; }
+static inline double sc_combine(double g, double phi, int is)            /* robust.c:86-93 */
+{ return is ? phi + g : phi * g; }
+static inline double sc_upscale(double amin, double a, int is)           /* robust.c:96-109 */
+{ return is ? ldexp(1.0, (int)(amin - a)) : amin / a; }
+static inline double sc_min(double a, double b, int is)                  /* robust.c:58-82 */
+{ return is ? (a < b ? a : b) : fmin(a, b); }
+
+/* scale(): x := beta * x unless the factor is 1 (robust.c:38-53). */
+static inline void sc_scale(int n, double *x, double beta, int is)
+{
+    const double alpha = sc_value(beta, is);
+    if (alpha != 1.0)
+        for (int i = 0; i < n; i++) x[i] = alpha * x[i];
+}
+/* scale_except(): all entries but x[skip] (utils.c:83-104). */
+static inline void sc_scale_except(int n, int skip, double *x, double beta, int is)
+{
+    const double alpha = sc_value(beta, is);
+    if (alpha != 1.0)
+        for (int i = 0; i < n; i++)
+            if (i != skip) x[i] = alpha * x[i];
+}
+
+/* vector_infnorm (utils.h:75-85): NaN never replaces the running max. */
+static inline double infnorm(int n, const double *x)
+{
+    double nrm = 0.0;
+    for (int i = 0; i < n; i++) {
+        const double a = fabs(x[i]);
+        if (a > nrm) nrm = a;
+    }
+    return nrm;
+}
+
+/* dlange('I') (utils.c:155-174 -> LAPACK): row sums accumulated column by
+ * column, then the max (a NaN row sum wins, as in LAPACK's DISNAN test).   */
+double hsro_dlange_inf(int m, int n, const double *A, int ldA)
+{
+    if (m <= 0 || n <= 0) return 0.0;
+    double *work = (double *)calloc((size_t)m, sizeof(double));
+    if (!work) return NAN;
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++)
+            work[i] += fabs(A[i + (size_t)j * ldA]);
+    double value = 0.0;
+    for (int i = 0; i < m; i++) {
+        const double t = work[i];
+        if (value < t || t != t) value = t;
+    }
+    free(work);
+    return value;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Robust scalar kernels, real subset (robust.c:144-479).                   */
+/* ------------------------------------------------------------------------ */
+
+/* protect_real_division (robust.c:144-166). */
+static double protect_real_division(double b, double t)
+{
+    double scale = 1.0;
+    if (fabs(t) < g_omega_inv) {
+        if (fabs(b) > fabs(t) * g_omega) scale = (fabs(t) * g_omega) / fabs(b);
+    } else {
+        if (1.0 > fabs(t) && fabs(b) > fabs(t) * g_omega) scale = 1.0 / fabs(b);
+    }
+    return scale;
+}
+
+/* protect_sum (robust.c:175-185). */
+static double protect_sum(double x, double y)
+{
+    double scale = 1.0;
+    if ((x > 0 && y > 0) || (x < 0 && y < 0))
+        if (fabs(x) > g_omega - fabs(y)) scale = 0.5;
+    return scale;
+}
+
+/* protect_update (robust.c:220-262): factor alpha such that
+ * (alpha*y) - t*(alpha*x) cannot overflow; an exponent under INTSCALING.   */
+double hsro_protect_update(double tnorm, double xnorm, double ynorm, int is)
+{
+    double scale = 1.0;
+    if (xnorm <= 1.0) {
+        if (tnorm * xnorm > g_omega - ynorm) scale = 0.5;
+    } else {
+        if (tnorm > (g_omega - ynorm) / xnorm) scale = 0.5 / xnorm;
+    }
+    return is ? (double)ilogb(scale) : scale;
+}
+
+/* protect_double_update (robust.c:270-285). */
+static double protect_double_update(double t1, double x1, double t2, double x2,
+                                    double y, int is)
+{
+    const double a1 = hsro_protect_update(t1, x1, y, is);
+    const double a2 = hsro_protect_update(t2, x2, y, is);
+    return is ? (a1 < a2 ? a1 : a2) : fmin(a1, a2);
+}
+
+/* solve_1x1_real_system (robust.c:422-479): x := (scale*x)/(t-lambda) with
+ * |t-lambda| lifted to smin when smaller; returns 1 if lifted.             */
+int hsro_solve_1x1(double smin, double t, double lambda, double *x,
+                   double *scale, int is)
+{
+    int info = 0;
+    const double s = protect_sum(t, -lambda);
+    double csr = (s * t) - (s * lambda);
+    if (fabs(csr) < smin) {
+        csr = smin;
+        info = 1;
+    }
+    const double alpha = protect_real_division(x[0], csr);
+    x[0] = (alpha * x[0]) / csr;
+    scale[0] = is ? (double)ilogb(alpha / s) : alpha / s;
+    return info;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Givens rotations: LAPACK >= 3.10 dlartg (E. Anderson, "Algorithm 978:     */
+/* Safe scaling in the Level 1 BLAS", ACM TOMS 44(1), 2017), restated from   */
+/* the published algorithm; reduce.c:14-24 wraps it and negates s.           */
+/* ------------------------------------------------------------------------ */
+void hsro_dlartg(double f, double g, double *c, double *s, double *r)
+{
+    const double safmin = DBL_MIN;          /* 2^-1022 */
+    const double safmax = 1.0 / DBL_MIN;    /* 2^1022  */
+    const double rtmin = sqrt(safmin);
+    const double rtmax = sqrt(safmax / 2);
+    const double f1 = fabs(f), g1 = fabs(g);
+    if (g == 0.0) {
+        *c = 1.0; *s = 0.0; *r = f;
+    } else if (f == 0.0) {
+        *c = 0.0; *s = copysign(1.0, g); *r = g1;
+    } else if (f1 > rtmin && f1 < rtmax && g1 > rtmin && g1 < rtmax) {
+        const double d = sqrt(f * f + g * g);
+        *c = f1 / d;
+        *r = copysign(d, f);
+        *s = g / *r;
+    } else {
+        const double u = fmin(safmax, fmax(safmin, fmax(f1, g1)));
+        const double fs = f / u, gs = g / u;
+        const double d = sqrt(fs * fs + gs * gs);
+        *c = fabs(fs) / d;
+        const double rr = copysign(d, f);
+        *s = gs / rr;
+        *r = rr * u;
+    }
+}
+
+void hsro_givens(double f, double g, double *c, double *s)
+{
+    double r;
+    hsro_dlartg(f, g, c, s, &r);
+    *s = (-1.0) * (*s);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Expression shapes.  REF: the reference's C expressions, evaluated left   */
+/* to right with no contraction.  FMA: the CUDA kernels' fused forms.        */
+/* ------------------------------------------------------------------------ */
+/* c*a + s*b   (reduce.c:48,51; solve-task.c:96-100,205-208) */
+static inline double rot_comb(double c, double a, double s, double b)
+{
+#if HSRO_MODE
+    return fma(c, a, s * b);
+#else
+    return (c * a) + (s * b);
+#endif
+}
+/* y - yc*v + ys*h   (solve-task.c:90,99,198,200) with yc = y_j*c_j, ys = y_j*s_j */
+static inline double bsub(double y, double yc, double v, double ys, double h)
+{
+#if HSRO_MODE
+    return fma(ys, h, fma(-yc, v, y));
+#else
+    return (y - (yc * v)) + (ys * h);
+#endif
+}
+/* c*t1 - s*t2   (update-task.c:195; shifted_Hessenberg_solve.c:167) */
+static inline double rot_diff(double c, double t1, double s, double t2)
+{
+#if HSRO_MODE
+    return fma(c, t1, -(s * t2));
+#else
+    return (c * t1) - (s * t2);
+#endif
+}
+/* y - h*t   (update-task.c:136,139; the rank-1 term update-task.c:241) */
+static inline double axmy(double y, double h, double t)
+{
+#if HSRO_MODE
+    return fma(-h, t, y);
+#else
+    return y - (h * t);
+#endif
+}
+/* y + m*t   (update-task.c:141) */
+static inline double axpy(double y, double m, double t)
+{
+#if HSRO_MODE
+    return fma(m, t, y);
+#else
+    return y + (m * t);
+#endif
+}
+/* (a*y) - h*(a*t)   (update-task.c:130) */
+static inline double scaled_axmy(double a, double y, double h, double at)
+{
+#if HSRO_MODE
+    return fma(-h, at, a * y);
+#else
+    return (a * y) - (h * at);
+#endif
+}
+/* acc += t*t   (dnrm2 accumulators, shifted_Hessenberg_solve.c:173-178) */
+static inline double sq_acc(double acc, double t)
+{
+#if HSRO_MODE
+    return fma(t, t, acc);
+#else
+    return acc + (t * t);
+#endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* Problem layout.                                                           */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    int n, T;
+    const int *fr;           /* first_row[T+1]; the first tile is the short one */
+    const double *H; int ldH;
+    const double *Hn;        /* Hn[I + J*T] = ||H(I,J)||_oo for I <= J          */
+    double smlnum;
+    int is;                  /* integer scaling */
+} prob_t;
+
+#define HH(i, j) (P->H[(size_t)(i) + (size_t)(j) * (size_t)P->ldH])
+
+/* partition (partition.c:7-17): tiles of tlsz, the first takes the rest. */
+static void partition(int n, int num_tiles, int tlsz, int *p)
+{
+    for (int i = 1; i < num_tiles; i++) p[i] = n - (num_tiles - i) * tlsz;
+    p[0] = 0;
+    p[num_tiles] = n;
+}
+
+typedef struct {
+    long pert, divr, solr, p1r, p2r, p0r;
+} cnt_t;
+
+/* ------------------------------------------------------------------------ */
+/* Diagonal tile: Givens generation fused with the robust back-substitution. */
+/* J > 0: reduceDiag (reduce.c:27-68) + solve (solve-task.c:19-119).         */
+/* J = 0: factor_and_solve_R11 (solve-task.c:123-225).                       */
+/* v: the crossover column of tile J on entry (b entries); y: X(J,k).        */
+/* ------------------------------------------------------------------------ */
+static int diag_tile(const prob_t *P, int J, double mu, double *v, double *y,
+                     double *beta, double *c, double *s, cnt_t *cn)
+{
+    const int is = P->is;
+    const int l = P->fr[J];
+    const int b = P->fr[J + 1] - l;
+    const double Hnorm = P->Hn[J + (size_t)J * P->T];
+    const double smin = fmax(DBL_EPSILON / 2 * fabs(mu), P->smlnum);
+    int info = 0;
+    double phi;
+
+    for (int j = b - 1; j >= 1; j--) {
+        const double hsub = HH(l + j, l + j - 1);
+        hsro_givens(v[j], hsub, &c[j], &s[j]);
+
+        /* y(j) := y(j) / R(j,j), R(j,j) = c(j)*v(j) - s(j)*H(j,j-1). */
+        phi = sc_one(is);
+        const int pj = hsro_solve_1x1(smin, c[j] * v[j], s[j] * hsub, &y[j], &phi, is);
+        info |= pj;
+        cn->pert += pj;
+        if (sc_value(phi, is) != 1.0) cn->divr++;
+        *beta = sc_combine(*beta, phi, is);
+        sc_scale_except(b, j, y, phi, is);
+
+        /* y(j-1) update, protected (solve-task.c:86-90). */
+        const double hdiag = HH(l + j - 1, l + j - 1) - mu;
+        phi = protect_double_update(fabs(v[j - 1]), fabs(y[j]), fabs(hdiag),
+                                    fabs(y[j]), fabs(y[j - 1]), is);
+        if (sc_value(phi, is) != 1.0) cn->solr++;
+        sc_scale(b, y, phi, is);
+        *beta = sc_combine(*beta, phi, is);
+        {
+            const double yc = y[j] * c[j], ys = y[j] * s[j];
+            y[j - 1] = bsub(y[j - 1], yc, v[j - 1], ys, hdiag);
+        }
+
+        /* y(0:j-2) update, protected by the tile norm (solve-task.c:93-100). */
+        const double ynorm = infnorm(j - 1, y);
+        const double vnorm = infnorm(j - 1, v);
+        phi = protect_double_update(vnorm, fabs(y[j]), Hnorm, fabs(y[j]), ynorm, is);
+        if (sc_value(phi, is) != 1.0) cn->solr++;
+        sc_scale(b, y, phi, is);
+        *beta = sc_combine(*beta, phi, is);
+        {
+            const double yc = y[j] * c[j], ys = y[j] * s[j];
+            for (int i = 0; i < j - 1; i++)
+                y[i] = bsub(y[i], yc, v[i], ys, HH(l + i, l + j - 1));
+        }
+
+        /* Next annihilation column (solve-task.c:105-108). */
+        v[j - 1] = rot_comb(c[j], hdiag, s[j], v[j - 1]);
+        for (int i = 0; i < j - 1; i++)
+            v[i] = rot_comb(c[j], HH(l + i, l + j - 1), s[j], v[i]);
+    }
+
+    if (J > 0) {
+        /* Final rotation with the entry left of the tile (reduce.c:53-61,
+         * solve-task.c:111-118). */
+        const double hleft = HH(l, l - 1);
+        if (hleft != 0) {
+            hsro_givens(v[0], hleft, &c[0], &s[0]);
+        } else {
+            c[0] = 1.0;
+            s[0] = 0.0;
+        }
+#if HSRO_MODE
+        v[0] = fma(v[0], c[0], -(hleft * s[0]));
+#else
+        v[0] = v[0] * c[0] - hleft * s[0];
+#endif
+    }
+    phi = sc_one(is);
+    {
+        const int p0 = hsro_solve_1x1(smin, v[0], 0.0, &y[0], &phi, is);
+        info |= p0;
+        cn->pert += p0;
+    }
+    if (sc_value(phi, is) != 1.0) cn->divr++;
+    *beta = sc_combine(*beta, phi, is);
+    sc_scale(b - 1, &y[1], phi, is);
+    return info;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Crossover-column propagation of tile J's rotations into tile I < J.       */
+/* REF: reduceOffdiagBlocked (reduce.c:73-143), 4 rotations per sweep.       */
+/* FMA: the device form R := H(I,J^-) * w + pi * R with prefix-product       */
+/*      coefficients w_k = c_k * prod_{l<k} s_l, summed k = 0 .. b-1.       */
+/* ------------------------------------------------------------------------ */
+static void offdiag_reduce(const prob_t *P, int I, int J, double mu,
+                           const double *c, const double *s, double *r)
+{
+    const int m = P->fr[I + 1] - P->fr[I];
+    const int nc = P->fr[J + 1] - P->fr[J];          /* multiple of 4 */
+    const int r0 = P->fr[I], c0 = P->fr[J] - 1;        /* H(I, J^-) */
+    const int applyShift = (I == J - 1);
+#define HIJ(i, k) HH(r0 + (i), c0 + (k))
+#if HSRO_MODE
+    double w[nc];
+    double pk = 1.0;
+    for (int k = 0; k < nc; k++) {
+        w[k] = c[k] * pk;
+        pk = pk * s[k];
+    }
+    for (int i = 0; i < m; i++) {
+        double acc = 0.0;
+        for (int k = 0; k < nc; k++) acc = fma(HIJ(i, k), w[k], acc);
+        r[i] = fma(pk, r[i], acc);
+    }
+    if (applyShift) r[m - 1] = fma(-mu, w[0], r[m - 1]);
+#else
+    for (int k = nc - 1; k >= 4; k -= 4) {
+        const double c3 = c[k - 3], c2 = c[k - 2], c1 = c[k - 1], c0k = c[k];
+        const double s3 = s[k - 3], s2 = s[k - 2], s1 = s[k - 1], s0k = s[k];
+        for (int i = 0; i < m; i++) {
+            r[i] = c3 * HIJ(i, k - 3)
+                 + s3 * c2 * HIJ(i, k - 2)
+                 + s3 * s2 * c1 * HIJ(i, k - 1)
+                 + s3 * s2 * s1 * c0k * HIJ(i, k)
+                 + s3 * s2 * s1 * s0k * r[i];
+        }
+    }
+    {
+        for (int i = 0; i < m - 1; i++) {
+            r[i] = c[0] * HIJ(i, 0)
+                 + s[0] * c[1] * HIJ(i, 1)
+                 + s[0] * s[1] * c[2] * HIJ(i, 2)
+                 + s[0] * s[1] * s[2] * c[3] * HIJ(i, 3)
+                 + s[0] * s[1] * s[2] * s[3] * r[i];
+        }
+        const int i = m - 1;
+        r[i] = c[0] * (HIJ(i, 0) - applyShift * mu)
+             + s[0] * c[1] * HIJ(i, 1)
+             + s[0] * s[1] * c[2] * HIJ(i, 2)
+             + s[0] * s[1] * s[2] * c[3] * HIJ(i, 3)
+             + s[0] * s[1] * s[2] * s[3] * r[i];
+    }
+#endif
+#undef HIJ
+}
+
+/* ------------------------------------------------------------------------ */
+/* Robust tile update Y(I) -= H(I,J)*(Q_J^T X(J))  (update-task.c:16-262),   */
+/* for the `ns` columns of one shift tile.                                   */
+/*   Y: X(I,:) (ldY), Yn: upper bounds [ns], Ys: scales [ns]                 */
+/*   X: X(J,:) (ldX), Xs: scales [ns]; c, s: tile J's rotations (ld = kb)    */
+/*   Rt: crossover columns of tile I *before* tile J's rotations (ld = m)    */
+/* ------------------------------------------------------------------------ */
+static void tile_update(const prob_t *P, int I, int J, int ns, const double *wr,
+                        double *Y, int ldY, double *Yn, double *Ys,
+                        const double *X, int ldX, const double *Xs,
+                        const double *c, const double *s, const double *Rt,
+                        double *work /* kb*ns */, double *tmp /* 2*ns */,
+                        cnt_t *cn)
+{
+    const int is = P->is;
+    const int m = P->fr[I + 1] - P->fr[I];
+    const int kb = P->fr[J + 1] - P->fr[J];
+    const int r0 = P->fr[I];
+    const int applyShift = (I == J - 1);
+    const double Hnorm = P->Hn[I + (size_t)J * P->T];
+    const double *h = &HH(r0, P->fr[J] - 1);
+    double *tscale = tmp, *z2n = tmp + ns;
+
+    /* Part 0: consistent scaling (update-task.c:68-88). */
+    for (int k = 0; k < ns; k++) {
+        if (Xs[k] < Ys[k]) {
+            const double a = sc_upscale(Xs[k], Ys[k], is);
+            double *y = Y + (size_t)k * ldY;
+            for (int i = 0; i < m; i++) y[i] = a * y[i];
+            Yn[k] = a * Yn[k];
+            Ys[k] = Xs[k];
+            cn->p0r++;
+        }
+    }
+
+    /* Part 1: the column left of tile J (update-task.c:103-151). */
+    const double hnrm = infnorm(m, h);
+    for (int k = 0; k < ns; k++) {
+        const double mu = wr[k];
+        const double x0 = X[(size_t)k * ldX];
+        double ytilde;
+        if (Ys[k] < Xs[k]) {
+            const double a = sc_upscale(Ys[k], Xs[k], is);
+            ytilde = -s[(size_t)k * kb] * (a * x0);
+        } else {
+            ytilde = -s[(size_t)k * kb] * x0;
+        }
+        const double alpha = hsro_protect_update(fmax(hnrm, fabs(mu)), fabs(ytilde), Yn[k], is);
+        const double a = sc_value(alpha, is);
+        double *y = Y + (size_t)k * ldY;
+        if (a != 1.0) {
+            cn->p1r++;
+            const double at = a * ytilde;
+            for (int i = 0; i < m; i++) y[i] = scaled_axmy(a, y[i], h[i], at);
+            if (applyShift) y[m - 1] = axpy(y[m - 1], mu, at);
+        } else {
+            for (int i = 0; i < m; i++) y[i] = axmy(y[i], h[i], ytilde);
+            if (applyShift) y[m - 1] = axpy(y[m - 1], mu, ytilde);
+        }
+        Ys[k] = sc_combine(Ys[k], alpha, is);
+        Yn[k] = infnorm(m, y);
+    }
+
+    /* Part 2: rotate X(J) into Ytilde2 (update-task.c:170-198). */
+    for (int k = 0; k < ns; k++) {
+        double *z = work + (size_t)k * kb;
+        const double *x = X + (size_t)k * ldX;
+        const double *ck = c + (size_t)k * kb, *sk = s + (size_t)k * kb;
+        if (Ys[k] < Xs[k]) {
+            const double a = sc_upscale(Ys[k], Xs[k], is);
+            for (int i = 0; i < kb; i++) z[i] = a * x[i];
+        } else {
+            memcpy(z, x, (size_t)kb * sizeof(double));
+        }
+        z[0] = ck[0] * z[0];
+        for (int j = 1; j < kb; j++) {
+            const double t1 = z[j - 1], t2 = z[j];
+            z[j - 1] = rot_diff(ck[j], t1, sk[j], t2);
+#if HSRO_MODE
+            z[j] = fma(sk[j], t1, ck[j] * t2);
+#else
+            z[j] = (sk[j] * t1) + (ck[j] * t2);
+#endif
+        }
+        z2n[k] = infnorm(kb, z);
+    }
+
+    /* Bounds (update-task.c:206-226). */
+    int status = 0;
+    for (int k = 0; k < ns; k++) {
+        tscale[k] = hsro_protect_update(Hnorm, z2n[k], Yn[k], is);
+        if (sc_value(tscale[k], is) != 1.0) status = 1;
+    }
+    if (status) {
+        for (int k = 0; k < ns; k++) {
+            if (sc_value(tscale[k], is) != 1.0) cn->p2r++;
+            sc_scale(kb, work + (size_t)k * kb, tscale[k], is);
+            sc_scale(m, Y + (size_t)k * ldY, tscale[k], is);
+            Ys[k] = sc_combine(Ys[k], tscale[k], is);
+        }
+    }
+
+    /* Y -= H(I, J .. J+kb-2) * Ytilde2(0:kb-2) (update-task.c:233). */
+    const double *Hs = &HH(r0, P->fr[J]);
+#if HSRO_MODE
+    for (int k = 0; k < ns; k++) {
+        const double *z = work + (size_t)k * kb;
+        double *y = Y + (size_t)k * ldY;
+        for (int i = 0; i < m; i++) {
+            double acc = 0.0;
+            for (int q = 0; q < kb - 1; q++)
+                acc = fma(Hs[(size_t)i + (size_t)q * P->ldH], z[q], acc);
+            y[i] = y[i] - acc;
+        }
+    }
+#else
+    {
+        const int mm = m, nn = ns, kk = kb - 1;
+        if (kk > 0) {
+#ifdef HSRO_DGEMM
+            const double mone = -1.0, one = 1.0;
+            const char nt = 'N';
+            HSRO_DGEMM(&nt, &nt, &mm, &nn, &kk, &mone, Hs, &P->ldH, work, &kb,
+                       &one, Y, &ldY);
+#else
+            for (int k = 0; k < nn; k++) {
+                const double *z = work + (size_t)k * kb;
+                double *y = Y + (size_t)k * ldY;
+                for (int i = 0; i < mm; i++) {
+                    double acc = 0.0;
+                    for (int q = 0; q < kk; q++)
+                        acc += Hs[(size_t)i + (size_t)q * P->ldH] * z[q];
+                    y[i] = y[i] + (-1.0) * acc;
+                }
+            }
+#endif
+        }
+    }
+#endif
+
+    /* Rank-1 term with the crossover column (update-task.c:239-243). */
+    for (int k = 0; k < ns; k++) {
+        const double zl = work[(size_t)k * kb + kb - 1];
+        const double *rt = Rt + (size_t)k * m;
+        double *y = Y + (size_t)k * ldY;
+        for (int i = 0; i < m; i++) y[i] = axmy(y[i], rt[i], zl);
+        Yn[k] = infnorm(m, y);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* 2-norm with three accumulators (LAPACK 3.10 dnrm2; shifted_Hessenberg_    */
+/* solve.c:135-229).  Blue's thresholds for IEEE double (Anderson 2017):     */
+/* tsml = 2^ceil((emin-1)/2), tbig = 2^floor((emax-p+1)/2),                  */
+/* ssml = 2^-floor((emin-p)/2), sbig = 2^-ceil((emax+p-1)/2), emin = -1021,  */
+/* emax = 1024, p = 53.                                                      */
+/* ------------------------------------------------------------------------ */
+#define NRM_TSML 0x1p-511
+#define NRM_TBIG 0x1p+486
+#define NRM_SSML 0x1p+537
+#define NRM_SBIG 0x1p-538
+
+typedef struct { double asml, amed, abig; } nrm3_t;
+
+static inline void nrm3_add(nrm3_t *a, double x)
+{
+    const double ax = fabs(x);
+    if (ax > NRM_TBIG) a->abig = sq_acc(a->abig, ax * NRM_SBIG);
+    else if (ax < NRM_TSML) a->asml = sq_acc(a->asml, ax * NRM_SSML);
+    else a->amed = sq_acc(a->amed, ax);
+}
+
+static inline double nrm3_finish(nrm3_t a)
+{
+    double ynrm, scale = 1.0;
+    if (a.abig > 0.0) {
+        ynrm = a.abig + (a.amed * NRM_SBIG) * NRM_SBIG;
+        scale = 1.0 / NRM_SBIG;
+    } else if (a.asml > 0.0) {
+        if (a.amed > 0.0) {
+            const double amed = sqrt(a.amed);
+            const double asml = sqrt(a.asml) / NRM_SSML;
+            double ymin, ymax;
+            if (asml > amed) { ymin = amed; ymax = asml; }
+            else { ymin = asml; ymax = amed; }
+            ynrm = ymax * ymax * (1.0 + (ymin / ymax) * (ymin / ymax));
+        } else {
+            scale = 1.0 / NRM_SSML;
+            ynrm = a.asml;
+        }
+    } else {
+        ynrm = a.amed;
+    }
+    return scale * sqrt(ynrm);
+}
+
+/* ------------------------------------------------------------------------ */
+/* One shift tile through the whole sweep (solve_Hessenberg_system_real_     */
+/* shift, shifted_Hessenberg_solve.c:334-394, with robustTiledSolve :43-331  */
+/* and tiledReduce reduce.c:201-356).                                        */
+/*   vr: n x ns (ldvr); vrn: vrnorms [T][ns] in/out, column 0 gets the       */
+/*   convergence flag; sc_out: reconciled scale per column (or NULL).        */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    double *R;      /* n*ns crossover columns, tile-major: tile I at fr[I]*ns */
+    double *C, *S;  /* rotations, tile-major, ld = tile height              */
+    double *scales; /* T*ns */
+    double *work;   /* bmax*ns */
+    double *tmp;    /* 2*ns */
+    double *v;      /* bmax */
+} ws_t;
+
+static int shift_tile(const prob_t *P, int ns, const double *wr, double *vr,
+                      int ldvr, double *vrn, double *sc_out,
+                      unsigned char *pert, ws_t *w, cnt_t *cn)
+{
+    const int n = P->n, T = P->T, is = P->is;
+    const int *fr = P->fr;
+#define RT(I) (w->R + (size_t)fr[I] * ns)
+#define CT(I) (w->C + (size_t)fr[I] * ns)
+#define ST(I) (w->S + (size_t)fr[I] * ns)
+#define SC(I) (w->scales + (size_t)(I) * ns)
+#define VRN(I) (vrn + (size_t)(I) * ns)
+#define Y(I, k) (vr + (size_t)fr[I] + (size_t)(k) * ldvr)
+
+    for (int i = 0; i < T * ns; i++) w->scales[i] = sc_one(is);
+    memset(w->C, 0, (size_t)n * ns * sizeof(double));
+    memset(w->S, 0, (size_t)n * ns * sizeof(double));
+
+    /* Initial crossover columns: H(I, n-1), shifted in the last tile
+     * (reduce.c:276-284, 301-308). */
+    for (int I = 0; I < T; I++) {
+        const int m = fr[I + 1] - fr[I];
+        for (int k = 0; k < ns; k++) {
+            double *r = RT(I) + (size_t)k * m;
+            for (int i = 0; i < m; i++) r[i] = HH(fr[I] + i, n - 1);
+            if (I == T - 1) r[m - 1] -= wr[k];
+        }
+    }
+
+    for (int J = T - 1; J >= 0; J--) {
+        const int b = fr[J + 1] - fr[J];
+        /* Diagonal tile, one shift at a time. */
+        for (int k = 0; k < ns; k++) {
+            double *v = w->v;
+            memcpy(v, RT(J) + (size_t)k * b, (size_t)b * sizeof(double));
+            const int pk = diag_tile(P, J, wr[k], v, Y(J, k), SC(J) + k,
+                                     CT(J) + (size_t)k * b, ST(J) + (size_t)k * b, cn);
+            if (pert && pk) pert[k] = 1;
+        }
+        if (J == 0) break;
+        /* Updates of the tiles above (shifted_Hessenberg_solve.c:274-311). */
+        for (int I = J - 1; I >= 0; I--) {
+            tile_update(P, I, J, ns, wr, Y(I, 0), ldvr, VRN(I), SC(I),
+                        Y(J, 0), ldvr, SC(J), CT(J), ST(J), RT(I),
+                        w->work, w->tmp, cn);
+        }
+        /* Crossover propagation (reduce.c:354-387). */
+        for (int I = J - 1; I >= 0; I--) {
+            const int m = fr[I + 1] - fr[I];
+            for (int k = 0; k < ns; k++)
+                offdiag_reduce(P, I, J, wr[k], CT(J) + (size_t)k * b,
+                               ST(J) + (size_t)k * b, RT(I) + (size_t)k * m);
+        }
+    }
+
+    /* Reconciliation, back-transform, norm, convergence, normalisation
+     * (shifted_Hessenberg_solve.c:153-242). */
+    for (int k = 0; k < ns; k++) {
+        double smin = SC(0)[k];
+        for (int I = 1; I < T; I++) smin = sc_min(smin, SC(I)[k], is);
+        if (sc_out) sc_out[k] = smin;
+        nrm3_t acc = {0.0, 0.0, 0.0};
+        double tau1 = 0.0, tau2;
+        for (int I = 0; I < T; I++) {
+            const int m = fr[I + 1] - fr[I];
+            double *y = Y(I, k);
+            const double *ck = CT(I) + (size_t)k * m, *sk = ST(I) + (size_t)k * m;
+            const double alpha = sc_upscale(smin, SC(I)[k], is);
+            int start = 0;
+            if (I == 0) {
+                start = 1;
+                tau1 = alpha * y[0];
+            }
+            for (int i = start; i < m; i++) {
+                tau2 = alpha * y[i];
+                y[i - 1] = rot_diff(ck[i], tau1, sk[i], tau2);
+                tau1 = rot_comb(ck[i], tau2, sk[i], tau1);
+                nrm3_add(&acc, y[i - 1]);
+            }
+        }
+        vr[(size_t)(n - 1) + (size_t)k * ldvr] = tau1;
+        nrm3_add(&acc, tau1);
+        const double ynrm = nrm3_finish(acc);
+        if (!(ynrm > 0.1 / sqrt(n))) {
+            VRN(0)[k] = 0.0;
+        } else {
+            double *y = vr + (size_t)k * ldvr;
+            for (int i = 0; i < n; i++) y[i] /= ynrm;
+            VRN(0)[k] = 1.0;
+        }
+    }
+    return 0;
+#undef RT
+#undef CT
+#undef ST
+#undef SC
+#undef VRN
+#undef Y
+}
+
+/* ------------------------------------------------------------------------ */
+/* One solve of all columns [0, nrhs) with the reference's batching          */
+/* (inverse_iteration.c:140-146, 209-252) and shift tiles of rhs_tlsz.       */
+/* vrnorms on entry: per-(column, tile) bounds [T][nrhs]; on exit column 0  */
+/* holds the convergence flag.                                               */
+/* ------------------------------------------------------------------------ */
+static int solve_all(const prob_t *P, int nrhs, const double *wr, double *vr,
+                     int ldvr, double *vrnorms, int rhs_tlsz,
+                     unsigned char *pert, double *colscale, cnt_t *total)
+{
+    const int n = P->n, T = P->T;
+    const int max_num_elems = 44000 * 44000;
+    int batch_size = rhs_tlsz > max_num_elems / (n * 2 * T) ? rhs_tlsz
+                                                             : max_num_elems / (n * 2 * T);
+    if (batch_size % 2 == 1) batch_size--;
+    if (batch_size < 1) batch_size = 1;
+
+    /* Enumerate shift tiles over all batches. */
+    int ntiles = 0;
+    for (int r = 0; r < nrhs; r += batch_size) {
+        const int b = nrhs - r < batch_size ? nrhs - r : batch_size;
+        ntiles += (b + rhs_tlsz - 1) / rhs_tlsz;
+    }
+    int *t0 = (int *)malloc(sizeof(int) * (size_t)(ntiles + 1));
+    int *tn = (int *)malloc(sizeof(int) * (size_t)(ntiles + 1));
+    if (!t0 || !tn) { free(t0); free(tn); return -2; }
+    {
+        int q = 0;
+        for (int r = 0; r < nrhs; r += batch_size) {
+            const int b = nrhs - r < batch_size ? nrhs - r : batch_size;
+            const int nt = (b + rhs_tlsz - 1) / rhs_tlsz;
+            int *fc = (int *)malloc(sizeof(int) * (size_t)(nt + 1));
+            partition(b, nt, rhs_tlsz, fc);
+            for (int t = 0; t < nt; t++) {
+                t0[q] = r + fc[t];
+                tn[q] = fc[t + 1] - fc[t];
+                q++;
+            }
+            free(fc);
+        }
+    }
+    int bmax = 0;
+    for (int I = 0; I < T; I++)
+        if (P->fr[I + 1] - P->fr[I] > bmax) bmax = P->fr[I + 1] - P->fr[I];
+    int err = 0;
+
+#pragma omp parallel
+    {
+        cnt_t cn = {0, 0, 0, 0, 0, 0};
+        ws_t w;
+        const int smax = rhs_tlsz;
+        w.R = (double *)malloc(sizeof(double) * (size_t)n * smax);
+        w.C = (double *)malloc(sizeof(double) * (size_t)n * smax);
+        w.S = (double *)malloc(sizeof(double) * (size_t)n * smax);
+        w.scales = (double *)malloc(sizeof(double) * (size_t)T * smax);
+        w.work = (double *)malloc(sizeof(double) * (size_t)bmax * smax);
+        w.tmp = (double *)malloc(sizeof(double) * 2 * (size_t)smax);
+        w.v = (double *)malloc(sizeof(double) * (size_t)bmax);
+        double *vrn = (double *)malloc(sizeof(double) * (size_t)T * smax);
+        const int ok = w.R && w.C && w.S && w.scales && w.work && w.tmp && w.v && vrn;
+        if (!ok) {
+#pragma omp atomic write
+            err = -2;
+        }
+#pragma omp for schedule(dynamic, 1)
+        for (int q = 0; q < ntiles; q++) {
+            if (!ok) continue;
+            const int k0 = t0[q], ns = tn[q];
+            for (int I = 0; I < T; I++)
+                for (int k = 0; k < ns; k++)
+                    vrn[(size_t)I * ns + k] = vrnorms[(size_t)(k0 + k) + (size_t)I * nrhs];
+            shift_tile(P, ns, wr + k0, vr + (size_t)k0 * ldvr, ldvr, vrn,
+                       colscale ? colscale + k0 : NULL, pert ? pert + k0 : NULL,
+                       &w, &cn);
+            for (int I = 0; I < T; I++)
+                for (int k = 0; k < ns; k++)
+                    vrnorms[(size_t)(k0 + k) + (size_t)I * nrhs] = vrn[(size_t)I * ns + k];
+        }
+        free(w.R); free(w.C); free(w.S); free(w.scales); free(w.work);
+        free(w.tmp); free(w.v); free(vrn);
+#pragma omp critical
+        {
+            total->pert += cn.pert; total->divr += cn.divr; total->solr += cn.solr;
+            total->p1r += cn.p1r; total->p2r += cn.p2r; total->p0r += cn.p0r;
+        }
+    }
+    free(t0);
+    free(tn);
+    return err;
+}
+
+/* Norm bounds of the tiles of H (Hnorms, inverse_iteration.c:172-175 with
+ * the lazy dlange calls of solve-task.c:30-34 and update-task.c:81-85).    */
+static double *tile_norms(const prob_t *P)
+{
+    const int T = P->T;
+    double *Hn = (double *)malloc(sizeof(double) * (size_t)T * T);
+    if (!Hn) return NULL;
+    for (int i = 0; i < T * T; i++) Hn[i] = -1.0;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int J = 0; J < T; J++) {
+        for (int I = 0; I <= J; I++) {
+            const int m = P->fr[I + 1] - P->fr[I];
+            const int k = P->fr[J + 1] - P->fr[J];
+            Hn[I + (size_t)J * T] = hsro_dlange_inf(m, k, &P->H[(size_t)P->fr[I] + (size_t)P->fr[J] * P->ldH], P->ldH);
+        }
+    }
+    return Hn;
+}
+
+static int setup(prob_t *P, int n, const double *H, int ldH, int tlsz, int is,
+                 int **fr_out)
+{
+    const int T = (n + tlsz - 1) / tlsz;
+    int *fr = (int *)malloc(sizeof(int) * (size_t)(T + 1));
+    if (!fr) return -2;
+    partition(n, T, tlsz, fr);
+    P->n = n; P->T = T; P->fr = fr; P->H = H; P->ldH = ldH; P->is = is;
+    {
+        const double eps = DBL_EPSILON / 2;
+        P->smlnum = fmax(2 * DBL_MIN, DBL_MIN * ((double)n / eps));   /* shifted_Hessenberg_solve.c:71 */
+    }
+    P->Hn = tile_norms(P);
+    if (!P->Hn) { free(fr); return -2; }
+    *fr_out = fr;
+    return 0;
+}
+
+static void stats_out(hsro_stats *st, const cnt_t *c)
+{
+    if (!st) return;
+    st->perturbations = c->pert;
+    st->div_rescales = c->divr;
+    st->solve_rescales = c->solr;
+    st->part1_rescales = c->p1r;
+    st->part2_rescales = c->p2r;
+    st->consistency_rescales = c->p0r;
+}
+
+/* Intended restart (inverse_iteration.c:36-125,176-205): stable partition,
+ * converged columns first.  Returns the number of converged columns.        */
+static int separate(int n, int nrhs, const int *conv, double *wr, double *vr,
+                    int ldvr, unsigned char *pert, double *colscale)
+{
+    int nc = 0;
+    for (int k = 0; k < nrhs; k++) nc += conv[k] != 0;
+    double *swr = (double *)malloc(sizeof(double) * (size_t)nrhs);
+    double *svr = (double *)malloc(sizeof(double) * (size_t)n * nrhs);
+    unsigned char *sp = (unsigned char *)malloc((size_t)nrhs);
+    double *scs = (double *)malloc(sizeof(double) * (size_t)nrhs);
+    int pc = 0, pn = nc;
+    for (int k = 0; k < nrhs; k++) {
+        const int pos = conv[k] ? pc++ : pn++;
+        swr[pos] = wr[k];
+        memcpy(svr + (size_t)pos * n, vr + (size_t)k * ldvr, sizeof(double) * (size_t)n);
+        sp[pos] = pert ? pert[k] : 0;
+        scs[pos] = colscale ? colscale[k] : 0.0;
+    }
+    memcpy(wr, swr, sizeof(double) * (size_t)nrhs);
+    for (int k = 0; k < nrhs; k++)
+        memcpy(vr + (size_t)k * ldvr, svr + (size_t)k * n, sizeof(double) * (size_t)n);
+    if (pert) memcpy(pert, sp, (size_t)nrhs);
+    if (colscale) memcpy(colscale, scs, sizeof(double) * (size_t)nrhs);
+    free(swr); free(svr); free(sp); free(scs);
+    return nc;
+}
+
+int hsro_inverse_iteration(int n, const double *H, int ldH, int nrhs,
+                           double *wr, int tlsz, int rhs_tlsz, double *vr,
+                           int ldvr, int intscale, unsigned char *perturbed,
+                           double *colscale, int *status, hsro_stats *stats)
+{
+    if (n <= 0 || ldH < n || nrhs < 0 || tlsz <= 0 || tlsz % 4 != 0 ||
+        rhs_tlsz <= 0 || ldvr < n || !H || (!wr && nrhs) || (!vr && nrhs))
+        return -1;
+    if (stats) memset(stats, 0, sizeof(*stats));
+    if (nrhs == 0) return 0;
+#ifdef HSRO_BLAS_THREADS
+    HSRO_BLAS_THREADS(1);
+#endif
+    prob_t P;
+    int *fr = NULL;
+    if (setup(&P, n, H, ldH, tlsz, intscale, &fr) != 0) return -2;
+    const int T = P.T;
+    cnt_t total = {0, 0, 0, 0, 0, 0};
+
+    /* Starting vector eps3 = ||H||_oo * eps/2 (inverse_iteration.c:154-158). */
+    const double eps3 = hsro_dlange_inf(n, n, H, ldH) * (DBL_EPSILON / 2);
+    double *vrnorms = (double *)malloc(sizeof(double) * (size_t)T * nrhs);
+    int *conv = (int *)malloc(sizeof(int) * (size_t)nrhs);
+    if (!vrnorms || !conv) { free(vrnorms); free(conv); free(fr); free((void *)P.Hn); return -2; }
+    if (perturbed) memset(perturbed, 0, (size_t)nrhs);
+
+    /* init_real_eigenvectors (inverse_iteration.c:19-34). */
+    for (int k = 0; k < nrhs; k++)
+        for (int i = 0; i < n; i++) vr[(size_t)i + (size_t)k * ldvr] = eps3;
+    for (int i = 0; i < T * nrhs; i++) vrnorms[i] = eps3;
+
+    int rc = solve_all(&P, nrhs, wr, vr, ldvr, vrnorms, rhs_tlsz, perturbed, colscale, &total);
+    int nconv_front = 0;   /* columns [0, nconv_front) are final */
+    int its = 0;
+    long restarts = 0;
+    while (rc == 0) {
+        const int m = nrhs - nconv_front;
+        int all = 1;
+        for (int k = 0; k < m; k++) {
+            conv[k] = vrnorms[k] != 0.0;
+            if (!conv[k]) all = 0;
+        }
+        if (all || its >= n) break;
+        const int nc = separate(n, m, conv, wr + nconv_front, vr + (size_t)nconv_front * ldvr, ldvr,
+                                perturbed ? perturbed + nconv_front : NULL,
+                                colscale ? colscale + nconv_front : NULL);
+        nconv_front += nc;
+        const int mm = nrhs - nconv_front;
+        /* new_real_starting_vector (inverse_iteration.c:36-57). */
+        const double tmp = eps3 / (sqrt(n) + 1.0);
+        double *v0 = vr + (size_t)nconv_front * ldvr;
+        for (int k = 0; k < mm; k++) {
+            double *v = v0 + (size_t)k * ldvr;
+            v[0] = eps3;
+            for (int i = 1; i < n; i++) v[i] = tmp;
+            v[n - 1 - its] -= eps3 * sqrt(n);
+        }
+        const double ub = fmax(fmax(eps3, tmp), fabs(tmp - eps3 / sqrt(n)));
+        for (int i = 0; i < T * mm; i++) vrnorms[i] = ub;
+        if (perturbed) memset(perturbed + nconv_front, 0, (size_t)mm);
+        rc = solve_all(&P, mm, wr + nconv_front, v0, ldvr, vrnorms, rhs_tlsz,
+                       perturbed ? perturbed + nconv_front : NULL,
+                       colscale ? colscale + nconv_front : NULL, &total);
+        its++;
+        restarts++;
+    }
+    int nonconv = 0;
+    {
+        const int m = nrhs - nconv_front;
+        for (int k = 0; k < nrhs; k++) {
+            int ok = 1;
+            if (k >= nconv_front) ok = vrnorms[k - nconv_front] != 0.0;
+            if (status) status[k] = ok;
+            nonconv += !ok;
+        }
+        (void)m;
+    }
+    stats_out(stats, &total);
+    if (stats) { stats->restarts = restarts; stats->nonconverged = nonconv; }
+    free(vrnorms); free(conv); free(fr); free((void *)P.Hn);
+    return rc;
+}
+
+int hsro_solve_rhs(int n, const double *H, int ldH, int nrhs, const double *wr,
+                   int tlsz, int rhs_tlsz, double *vr, int ldvr, int intscale,
+                   unsigned char *perturbed, double *colscale, int *status,
+                   hsro_stats *stats)
+{
+    if (n <= 0 || ldH < n || nrhs < 0 || tlsz <= 0 || tlsz % 4 != 0 ||
+        rhs_tlsz <= 0 || ldvr < n || !H || (!wr && nrhs) || (!vr && nrhs))
+        return -1;
+    if (stats) memset(stats, 0, sizeof(*stats));
+    if (nrhs == 0) return 0;
+#ifdef HSRO_BLAS_THREADS
+    HSRO_BLAS_THREADS(1);
+#endif
+    prob_t P;
+    int *fr = NULL;
+    if (setup(&P, n, H, ldH, tlsz, intscale, &fr) != 0) return -2;
+    const int T = P.T;
+    cnt_t total = {0, 0, 0, 0, 0, 0};
+    double *vrnorms = (double *)malloc(sizeof(double) * (size_t)T * nrhs);
+    if (!vrnorms) { free(fr); free((void *)P.Hn); return -2; }
+    if (perturbed) memset(perturbed, 0, (size_t)nrhs);
+    for (int I = 0; I < T; I++)
+        for (int k = 0; k < nrhs; k++)
+            vrnorms[(size_t)k + (size_t)I * nrhs] =
+                infnorm(fr[I + 1] - fr[I], vr + (size_t)fr[I] + (size_t)k * ldvr);
+    const int rc = solve_all(&P, nrhs, wr, vr, ldvr, vrnorms, rhs_tlsz, perturbed,
+                             colscale, &total);
+    int nonconv = 0;
+    for (int k = 0; k < nrhs; k++) {
+        const int ok = vrnorms[k] != 0.0;
+        if (status) status[k] = ok;
+        nonconv += !ok;
+    }
+    stats_out(stats, &total);
+    if (stats) stats->nonconverged = nonconv;
+    free(vrnorms); free(fr); free((void *)P.Hn);
+    return rc;
+}
