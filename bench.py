@@ -1,0 +1,351 @@
+#!/usr/bin/env python3
+"""Benchmark: FP64 eigenvectors/s of the robust level-3 inverse iteration.
+
+Workload (the plain large configuration): one real upper-Hessenberg H of
+order n = 10000 from the seeded real-spectrum generator, all 10000 eigenvalues
+as shifts with relative 1e-12 noise, tlsz = 200.  One step = one complete
+solve (tile sweep, reconciliation, back-transform, normalisation, convergence
+check) of all shifts.
+
+* value: eigenvectors/s with H, the shifts and the output block resident in
+  HBM (hsr_inverse_iteration_device), timed with CUDA events on the launching
+  stream.  H (800 MB) is larger than L2, so no flush is needed between steps.
+* e2e: the same metric through the drop-in C entry point
+  tiled_inverse_iteration with pinned host buffers: H and the shifts copied
+  in, the eigenvectors and shifts copied out, every step.
+* roofline: the dominant kernel (the crossover/update GEMM) against the FP64
+  DFMA peak measured in the same run; traffic from the committed ncu capture.
+* cpu_baseline: the C restatement of the reference (oracle port, OpenMP over
+  shift tiles, OpenBLAS dgemm) on all host cores over a bounded sample of the
+  shifts.
+``--impl reference`` times that CPU implementation alone on the same config.
+Under torchrun every rank solves its own replica (weak scaling, no collective
+on the data path); rank 0 prints one JSON line with the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "FP64 eigenvectors/s at n=10k"
+UNIT = "eigenvectors/s"
+# DRAM bytes per GEMM launch, averaged over the launches of the n=4096,
+# S=4096, tlsz=200 capture in profiles/k_gemm_n4096.md, scaled to this
+# workload by the algorithmic FMAs per launch (traffic grows with them).
+GEMM_DRAM_BYTES_PER_FMA = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=10000)
+    ap.add_argument("--nrhs", type=int, default=0, help="0 = all n eigenvalues")
+    ap.add_argument("--tlsz", type=int, default=200)
+    ap.add_argument("--rhs-tlsz", type=int, default=64)
+    ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--cpu-sample", type=int, default=0, help="shifts in the CPU sample (0 = 64 per core)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ inputs
+def workload(n: int, seed: int):
+    """(H, shifts), generated once per host and cached in the temp dir."""
+    from hsrq3in_gb300 import generators as G
+    d = os.path.join(tempfile.gettempdir(), "hsrq3in_bench")
+    os.makedirs(d, exist_ok=True)
+    f = os.path.join(d, "real_n%d_s%d_v1.npz" % (n, seed))
+    if os.path.exists(f):
+        z = np.load(f)
+        return np.asfortranarray(z["H"]), z["wr"]
+    H, lam = G.real_spectrum(n, seed)
+    wr = G.perturbed_shifts(lam, seed + 1)
+    tmp = f + ".%d.tmp.npz" % os.getpid()
+    np.savez(tmp, H=H, wr=wr)
+    os.replace(tmp, f)
+    return H, wr
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons every 200 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unsampled"]}
+        load = [x for x in sm if mx and x > 0.5 * mx] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------- CPU (port)
+def cpu_sample(H, wr, tlsz, rhs_tlsz, sample, steps, warmup):
+    """Time the oracle port (reference arithmetic, -O3) on `sample` shifts."""
+    from oracle import pyoracle as O
+    cores = os.cpu_count() or 1
+    O.set_threads(cores, variant="ref_fast")
+    w = np.ascontiguousarray(wr[:sample])
+    times = []
+    for it in range(warmup + steps):
+        t0 = time.perf_counter()
+        O.oracle_inverse_iteration(H, w, tlsz, rhs_tlsz, variant="ref_fast")
+        dt = time.perf_counter() - t0
+        if it >= warmup:
+            times.append(dt)
+    t = statistics.mean(times)
+    return sample / t, t, cores
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu(args, H, wr, rank, world):
+    import torch
+    import hsrq3in_gb300 as hsr
+    from hsrq3in_gb300 import _lib
+    lib = hsr.load(build_if_missing=True)
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    n, S = H.shape[0], wr.shape[0]
+    ldh = n + (n & 1)
+    dHt = torch.zeros((n, ldh), dtype=torch.float64, device=dev)   # row j = column j of H
+    dHt[:, :n] = torch.from_numpy(np.ascontiguousarray(H.T)).to(dev)
+    dwr0 = torch.from_numpy(np.ascontiguousarray(wr)).to(dev)
+    dwr = dwr0.clone()
+    dX = torch.empty((S, ldh), dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    opt = _lib.Options(0, 0, -1, 0.0)
+
+    def step():
+        dwr.copy_(dwr0)
+        rc = lib.hsr_inverse_iteration_device(n, dHt.data_ptr(), ldh, S, dwr.data_ptr(), args.tlsz,
+                                              dX.data_ptr(), ldh, C.byref(opt), C.c_void_p(stream.cuda_stream),
+                                              None, None)
+        if rc < 0:
+            raise RuntimeError("device call failed: %d" % rc)
+        return rc
+
+    dfma, dmma = hsr.fp64_peak(100.0)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    torch.cuda.synchronize()
+    lib.hsr_set_kernel_timing(1)
+    kms = np.zeros(6)
+    kl = np.zeros(6, dtype=np.int64)
+    gemm_fma = 0.0
+    launches = 0
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            rcs = []
+            for _ in range(args.steps):
+                rcs.append(step())
+                ms = (C.c_double * 6)()
+                ln = (C.c_long * 6)()
+                fm = C.c_double()
+                lib.hsr_last_kernel_times(ms, ln, C.byref(fm))
+                kms += np.array(ms[:])
+                kl += np.array(ln[:])
+                gemm_fma += fm.value
+                launches += lib.hsr_last_launch_count()
+            ev1.record(stream)
+        torch.cuda.synchronize()
+    lib.hsr_set_kernel_timing(0)
+    t_ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    ms_per_step = t_ms / args.steps
+    value = world * S / (ms_per_step / 1e3)
+
+    # result sanity (residual on a sample of columns; full matrix on host)
+    X = dX[:, :n].cpu().numpy().T
+    from oracle import pyoracle as O
+    cols = np.linspace(0, S - 1, 64).astype(int)
+    res = O.residuals(H, dwr.cpu().numpy()[cols], X[:, cols])
+    finite = bool(np.isfinite(X).all())
+
+    gemm_ms = kms[3]
+    achieved = 2.0 * gemm_fma / (gemm_ms * 1e-3) / 1e12 if gemm_ms > 0 else None
+    peak = dfma / 1e3
+    roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": (achieved / peak) if achieved else None,
+            "traffic": (GEMM_DRAM_BYTES_PER_FMA * gemm_fma / max(kl[3], 1)) if GEMM_DRAM_BYTES_PER_FMA else None,
+            "kernel": "k_gemm (crossover propagation + tile update, DFMA)",
+            "peak_source": "FP64 DFMA stream measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
+            "algorithmic_flops_per_launch": 2.0 * gemm_fma / max(kl[3], 1),
+            "avg_launch_ms": gemm_ms / max(kl[3], 1)}
+    whole = 2.0 * n * n * S / (ms_per_step * 1e-3) / 1e12
+    out = dict(value=value, ms_per_step=ms_per_step, roofline=roof, clocks=clk.summary(),
+               gpu_launches=int(launches), fp64_peak_gflops={"dfma": dfma, "dmma": dmma},
+               kernel_ms_per_step={k: float(v) / args.steps for k, v in zip(_lib.KERNEL_CLASSES, kms)},
+               whole_solve_tflops_2n2S=whole, whole_solve_frac=whole / peak,
+               check={"max_residual_64cols": float(np.max(res)), "finite": finite,
+                      "rc": rcs[-1] if rcs else None})
+
+    # e2e through the drop-in C entry point with pinned host buffers
+    if not args.no_e2e:
+        Hp = torch.from_numpy(np.asfortranarray(H).ravel(order="F")).pin_memory()
+        Xp = torch.empty(n * S, dtype=torch.float64).pin_memory()
+        w0 = np.ascontiguousarray(wr)
+        wp = torch.empty(S, dtype=torch.float64).pin_memory()
+        lib.tiled_inverse_iteration.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                                C.c_int, C.c_int, C.c_void_p, C.c_int]
+
+        def e2e_step():
+            wp.numpy()[:] = w0
+            lib.tiled_inverse_iteration(n, Hp.data_ptr(), n, S, wp.data_ptr(), args.tlsz, args.rhs_tlsz,
+                                        Xp.data_ptr(), n)
+            if lib.hsr_last_status() < 0:
+                raise RuntimeError("drop-in call failed")
+        e2e_step()
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        te = (time.perf_counter() - t0) / args.steps
+        if world > 1:
+            import torch.distributed as dist
+            tt = torch.tensor([te], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            te = float(tt.item())
+        out["e2e"] = {"value": world * S / te, "unit": UNIT, "h2d_bytes_per_step": 8 * (n * n + S),
+                      "d2h_bytes_per_step": 8 * (n * S + S), "ms_per_step": te * 1e3,
+                      "api": "tiled_inverse_iteration (C ABI, pinned host buffers)"}
+    return out
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if (args.impl == "gb300" and torch.cuda.is_available()) else "gloo"
+        dist.init_process_group(backend=backend)
+    n = args.n
+    S = args.nrhs or n
+    cores = os.cpu_count() or 1
+    sample = args.cpu_sample or min(S, 64 * cores)
+    config = {"workload": "plain large: n=%d, %d real shifts (eigenvalues, rel. 1e-12 noise), tlsz=%d"
+                          % (n, S, args.tlsz),
+              "n": n, "nrhs": S, "tlsz": args.tlsz, "rhs_tlsz": args.rhs_tlsz, "seed": args.seed,
+              "generator": "T upper triangular, diag jittered-uniform in [-1,1] (gap>=1e-4), strictly-upper "
+                           "N(0,1); H = hess(Q T Q^T), Q^T e1 uniform on the sphere",
+              "l2": "inputs larger than L2 (H is %.0f MB); no flush" % (8 * n * n / 1e6),
+              "parallelism": "replicas" if args.gpus > 1 else "1 gpu"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        H, wr = workload(n, args.seed)
+        v, t, c = cpu_sample(H, wr[:S], args.tlsz, args.rhs_tlsz, sample, args.steps, args.warmup)
+        line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)", "config": config,
+                "impl": "reference",
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": c, "kind": "port",
+                                 "sample": "n=%d, first %d of %d shifts per step, tlsz=%d, rhs_tlsz=%d; the C "
+                                           "restatement of the reference (reference sources are not on this "
+                                           "host)" % (n, sample, S, args.tlsz, args.rhs_tlsz)},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    H, wr = workload(n, args.seed)
+    wr = wr[:S]
+    g = run_gpu(args, H, wr, rank, world)
+    line = {"metric": METRIC, "value": g["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": g["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+            "config": config}
+    for k in ("e2e", "roofline", "clocks", "gpu_launches", "fp64_peak_gflops", "kernel_ms_per_step",
+              "whole_solve_tflops_2n2S", "whole_solve_frac", "check"):
+        if k in g:
+            line[k] = g[k]
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, t, c = cpu_sample(H, wr, args.tlsz, args.rhs_tlsz, sample, 1, 0)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": c, "kind": "port",
+                                "sample": "n=%d, first %d of %d shifts, one solve (%.1f s), tlsz=%d, rhs_tlsz=%d"
+                                          % (n, sample, S, t, args.tlsz, args.rhs_tlsz)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -22,9 +22,10 @@ HSR_ERR_NOT_CONVERGED = 1
 EXPORTS = [
     "hsr_last_status", "hsr_status_string", "tiled_inverse_iteration",
     "hsr_inverse_iteration_ex", "hsr_inverse_iteration_device",
-    "hsr_last_launch_count", "hsr_release_workspace", "hsr_probe_fp64_peak",
-    "hsr_version",
+    "hsr_last_launch_count", "hsr_set_kernel_timing", "hsr_last_kernel_times",
+    "hsr_release_workspace", "hsr_probe_fp64_peak", "hsr_version",
 ]
+KERNEL_CLASSES = ["setup", "diag", "part1", "gemm", "finalize", "other"]
 
 
 class Options(C.Structure):
@@ -73,6 +74,10 @@ def load(build_if_missing: bool = False) -> C.CDLL:
                                                  C.c_int, C.c_void_p, C.c_int, C.POINTER(Options),
                                                  C.c_void_p, C.c_void_p, C.c_void_p]
     lib.hsr_last_launch_count.restype = C.c_long
+    lib.hsr_set_kernel_timing.restype = None
+    lib.hsr_set_kernel_timing.argtypes = [C.c_int]
+    lib.hsr_last_kernel_times.restype = C.c_int
+    lib.hsr_last_kernel_times.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     lib.hsr_release_workspace.restype = None
     lib.hsr_probe_fp64_peak.restype = C.c_int
     lib.hsr_probe_fp64_peak.argtypes = [C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]

@@ -21,6 +21,55 @@ namespace {
 thread_local int g_last_status = HSR_OK;
 thread_local long g_launches = 0;
 
+// Optional per-kernel-class device timing: an event pair around every launch
+// on the launching stream, resolved after the call's final synchronisation.
+enum KernelClass { kcSetup = 0, kcDiag, kcPart1, kcGemm, kcFinal, kcOther, kcCount };
+struct Timing {
+    bool enabled = false;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    std::vector<int> cls;
+    double ms[kcCount] = {0};
+    long launches[kcCount] = {0};
+    double gemm_fma[1] = {0};   // algorithmic FMAs of the timed GEMM launches
+    void reset() {
+        used = 0;
+        cls.clear();
+        for (int i = 0; i < kcCount; ++i) ms[i] = 0.0, launches[i] = 0;
+        gemm_fma[0] = 0.0;
+    }
+    cudaEvent_t next() {
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            pool.push_back(e);
+        }
+        return pool[used++];
+    }
+    void begin(int c, cudaStream_t st) {
+        if (!enabled) return;
+        cls.push_back(c);
+        cudaEventRecord(next(), st);
+    }
+    void end(cudaStream_t st) {
+        if (!enabled) return;
+        cudaEventRecord(next(), st);
+    }
+    void resolve() {
+        if (!enabled) return;
+        for (size_t i = 0; i < cls.size(); ++i) {
+            float t = 0.f;
+            if (2 * i + 1 < used && cudaEventElapsedTime(&t, pool[2 * i], pool[2 * i + 1]) == cudaSuccess) {
+                ms[cls[i]] += t;
+                launches[cls[i]] += 1;
+            }
+        }
+        used = 0;
+        cls.clear();
+    }
+};
+thread_local Timing g_timing;
+
 #define HSR_CK(x)                                  \
     do {                                           \
         cudaError_t e_ = (x);                      \
@@ -29,10 +78,13 @@ thread_local long g_launches = 0;
             return HSR_ERR_CUDA;                   \
         }                                          \
     } while (0)
-#define HSR_LAUNCH(x)                              \
+#define HSR_LAUNCH_C(c, stream, x)                 \
     do {                                           \
         ++g_launches;                              \
-        HSR_CK(x);                                 \
+        g_timing.begin((c), (stream));             \
+        cudaError_t le_ = (x);                     \
+        g_timing.end((stream));                    \
+        HSR_CK(le_);                               \
     } while (0)
 
 cudaError_t &last_cuda_error() {
@@ -190,21 +242,22 @@ int run_pass(Solver &s, int mode, int its, int off, int cnt) {
     for (int c0 = 0; c0 < cnt; c0 += s.Scap) {
         const int cc = std::min(s.Scap, cnt - c0);
         DevProblem P = problem_for(s, off + c0, cc);
-        HSR_LAUNCH(launch_init(P, mode, s.eps3_dev, its, s.st));
+        HSR_LAUNCH_C(kcSetup, s.st, launch_init(P, mode, s.eps3_dev, its, s.st));
         if (mode == 2) ++g_launches;
         const int b = s.tlsz;
         const bool big = (size_t)(64 * b + 2 * (b + 1)) * sizeof(double) > 200 * 1024;
         double *gs = big ? s.w->gscratch.as<double>() : nullptr;
         for (int J = s.T - 1; J >= 0; --J) {
             const int bj = s.fr[J + 1] - s.fr[J];
-            HSR_LAUNCH(launch_diag(P, J, bj, big ? gs : nullptr, s.st));
+            HSR_LAUNCH_C(kcDiag, s.st, launch_diag(P, J, bj, big ? gs : nullptr, s.st));
             if (J == 0) break;
-            HSR_LAUNCH(launch_part1(P, J, s.st));
-            HSR_LAUNCH(launch_gemm(P, J, s.fr[J], s.tmH, s.tmW, s.tmZ, s.st));
+            HSR_LAUNCH_C(kcPart1, s.st, launch_part1(P, J, s.st));
+            HSR_LAUNCH_C(kcGemm, s.st, launch_gemm(P, J, s.fr[J], s.tmH, s.tmW, s.tmZ, s.st));
+            if (g_timing.enabled) g_timing.gemm_fma[0] += (double)s.fr[J] * (2.0 * bj - 1.0) * cc;
         }
-        HSR_LAUNCH(launch_finalize(P, s.d_colnorm + off + c0, s.d_status + off + c0,
-                                   s.d_scale ? s.d_scale + off + c0 : nullptr, s.st));
-        HSR_LAUNCH(launch_normalize(P, s.d_colnorm + off + c0, s.d_status + off + c0, s.st));
+        HSR_LAUNCH_C(kcFinal, s.st, launch_finalize(P, s.d_colnorm + off + c0, s.d_status + off + c0,
+                                                     s.d_scale ? s.d_scale + off + c0 : nullptr, s.st));
+        HSR_LAUNCH_C(kcFinal, s.st, launch_normalize(P, s.d_colnorm + off + c0, s.d_status + off + c0, s.st));
     }
     return HSR_OK;
 }
@@ -297,8 +350,8 @@ int solve_device(int n, const double *dH, long long ldh, int S, double *dwr, int
     HSR_CK(cudaMemsetAsync(bits, 0, (2 * (size_t)T * T + 2) * 8, st));
     {
         DevProblem P0 = problem_for(s, 0, std::min(S, s.Scap));
-        HSR_LAUNCH(launch_norms(P0, bits, bits + (size_t)T * T, bits + 2 * (size_t)T * T,
-                                w.err.as<int>() + 1, st));
+        HSR_LAUNCH_C(kcSetup, st, launch_norms(P0, bits, bits + (size_t)T * T, bits + 2 * (size_t)T * T,
+                                               w.err.as<int>() + 1, st));
         ++g_launches;
     }
     double hinf = 0.0;
@@ -343,8 +396,8 @@ int solve_device(int n, const double *dH, long long ldh, int S, double *dwr, int
         HSR_CK(w.tmpX.ensure((size_t)n * m * 8));
         HSR_CK(w.perm.ensure((size_t)m * sizeof(int)));
         HSR_CK(cudaMemcpyAsync(w.perm.p, perm.data(), m * sizeof(int), cudaMemcpyHostToDevice, st));
-        HSR_LAUNCH(launch_gather_cols(w.tmpX.as<double>(), n, dX + (size_t)front * ldx, ldx, n,
-                                      w.perm.as<int>(), m, st));
+        HSR_LAUNCH_C(kcOther, st, launch_gather_cols(w.tmpX.as<double>(), n, dX + (size_t)front * ldx, ldx, n,
+                                                     w.perm.as<int>(), m, st));
         HSR_CK(cudaMemcpy2DAsync(dX + (size_t)front * ldx, ldx * 8, w.tmpX.p, (size_t)n * 8, (size_t)n * 8, m,
                                  cudaMemcpyDeviceToDevice, st));
         // Permute the small per-column arrays on the host.
@@ -379,6 +432,7 @@ int solve_device(int n, const double *dH, long long ldh, int S, double *dwr, int
     int errw = 0;
     HSR_CK(cudaMemcpyAsync(&errw, w.err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     HSR_CK(cudaStreamSynchronize(st));
+    g_timing.resolve();
     if (errw) return HSR_ERR_DEVICE;
     if (h_status) *h_status = st_h;
     if (h_pert) {
@@ -416,6 +470,7 @@ int check_args(int n, int ldH, int nrhs, int tlsz, int ldvr, const void *H, cons
 int host_call(int n, const double *H, int ldH, int nrhs, double *wr, int tlsz, int rhs_tlsz, double *vr,
               int ldvr, const hsr_options *opt, hsr_column_info *info) {
     g_launches = 0;
+    g_timing.reset();
     int rc = check_args(n, ldH, nrhs, tlsz, ldvr, H, wr, vr);
     if (rc) return rc;
     if (rhs_tlsz <= 0) return HSR_ERR_ARG;
@@ -492,6 +547,7 @@ int hsr_inverse_iteration_ex(int n, const double *H, int ldH, int nrhs, double *
 int hsr_inverse_iteration_device(int n, const double *dH, int lddH, int nrhs, double *dwr, int tlsz, double *dvr,
                                  int lddvr, const hsr_options *opt, void *stream, int *d_status, double *d_scale) {
     g_launches = 0;
+    g_timing.reset();
     int rc = check_args(n, lddH, nrhs, tlsz, lddvr, dH, dwr, dvr);
     if (rc) return g_last_status = rc;
     if (nrhs == 0) return g_last_status = HSR_OK;
@@ -517,6 +573,17 @@ int hsr_inverse_iteration_device(int n, const double *dH, int lddH, int nrhs, do
 }
 
 long hsr_last_launch_count(void) { return g_launches; }
+
+void hsr_set_kernel_timing(int enable) { g_timing.enabled = enable != 0; }
+
+int hsr_last_kernel_times(double *ms, long *launches, double *gemm_fma) {
+    for (int i = 0; i < kcCount; ++i) {
+        if (ms) ms[i] = g_timing.ms[i];
+        if (launches) launches[i] = g_timing.launches[i];
+    }
+    if (gemm_fma) *gemm_fma = g_timing.gemm_fma[0];
+    return kcCount;
+}
 
 void hsr_release_workspace(void) { ws().release(); }
 

@@ -81,8 +81,9 @@ int hsr_inverse_iteration_ex(int n, const double *H, int ldH, int nrhs,
 
 /* ------------------------------------------------ device-resident call */
 /* Same computation on device pointers (inputs already in HBM), enqueued on
- * `stream` (a cudaStream_t, NULL = legacy default stream).  dH needs lddH
- * even and a 16-byte aligned base (TMA); otherwise HSR_ERR_ARG.  Synchronises
+ * `stream` (a cudaStream_t, NULL = legacy default stream).  The GEMM reads
+ * dH through TMA, which needs an even lddH and a 16-byte aligned base; other
+ * inputs are first copied to a padded device buffer.  Synchronises
  * the stream once at the end to read convergence status.  Device arrays
  * d_status/d_scale may be NULL.  Replaces solve_Hessenberg_system_real_shift
  * (shifted_Hessenberg_solve.h:26-30) plus the driver loop. */
@@ -93,6 +94,14 @@ int hsr_inverse_iteration_device(int n, const double *dH, int lddH, int nrhs,
 
 /* Number of kernel launches the last call on this thread enqueued. */
 long hsr_last_launch_count(void);
+
+/* Per-kernel-class device timing (CUDA events on the launching stream
+ * around every launch), off by default.  hsr_last_kernel_times fills
+ * ms[6] and launches[6] for the classes {setup, diagonal, part1, gemm,
+ * finalize, other} of the last call, and the algorithmic FMA count of its
+ * GEMM launches; returns the number of classes.  No reference counterpart. */
+void hsr_set_kernel_timing(int enable);
+int hsr_last_kernel_times(double *ms, long *launches, double *gemm_fma);
 
 /* Release cached device workspaces of this thread. */
 void hsr_release_workspace(void);
