@@ -153,6 +153,19 @@ struct DevBuf {
 struct Workspace {
     int device = -1;
     cudaStream_t stream = nullptr;
+    // Look-ahead: the diagonal kernel of the next tile runs on a
+    // high-priority side stream while the current stage's GEMM finishes.
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_top = nullptr, ev_diag = nullptr;
+    cudaError_t ensure_side() {
+        if (side) return cudaSuccess;
+        int lo = 0, hi = 0;
+        cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+        if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_top, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_diag, cudaEventDisableTiming);
+        return e;
+    }
     DevBuf H, X, wr, R, Cr, Sr, beta, ynorm, W, Zs, vecs, Zslow, slow, pert, fr, bits, err, colnorm,
         status, scale, tmpX, perm, gscratch, probe;
     ~Workspace() { release(); }
@@ -161,7 +174,11 @@ struct Workspace {
                          &fr, &bits, &err, &colnorm, &status, &scale, &tmpX, &perm, &gscratch, &probe};
         for (DevBuf *b : all) b->release();
         if (stream) cudaStreamDestroy(stream);
-        stream = nullptr;
+        if (side) cudaStreamDestroy(side);
+        if (ev_top) cudaEventDestroy(ev_top);
+        if (ev_diag) cudaEventDestroy(ev_diag);
+        stream = side = nullptr;
+        ev_top = ev_diag = nullptr;
     }
 };
 
@@ -191,7 +208,7 @@ struct Solver {
     double smlnum;
     cudaStream_t st;
     Workspace *w;
-    CUtensorMap tmH, tmW, tmZ;
+    CUtensorMap tmH, tmW[2], tmZ[2];
     double *eps3_dev;
     int *d_status;     // [S] per final column
     double *d_colnorm; // [S]
@@ -199,7 +216,10 @@ struct Solver {
     unsigned char *d_pert;  // [S]
 };
 
-DevProblem problem_for(const Solver &s, int off, int cnt) {
+// Stage operands (W, Zs and the per-shift scalars) are double-buffered by
+// tile parity so that the diagonal kernel of tile J-1 can write its operands
+// while the GEMM of stage J still reads those of tile J.
+DevProblem problem_for(const Solver &s, int off, int cnt, int parity = 0) {
     Workspace &w = *s.w;
     DevProblem P{};
     P.n = s.n;
@@ -221,9 +241,10 @@ DevProblem problem_for(const Solver &s, int off, int cnt) {
     P.ynorm = w.ynorm.as<double>();
     P.Hn = w.bits.as<double>();
     P.hn = w.bits.as<double>() + (size_t)s.T * s.T;
-    P.W = w.W.as<double>();
-    P.Zs = w.Zs.as<double>();
-    double *v = w.vecs.as<double>();
+    const size_t stage = (size_t)s.tlsz * s.Spad;
+    P.W = w.W.as<double>() + parity * stage;
+    P.Zs = w.Zs.as<double>() + parity * stage;
+    double *v = w.vecs.as<double>() + parity * 4 * (size_t)s.Spad;
     P.pi = v;
     P.ytil = v + s.Spad;
     P.z2n = v + 2 * (size_t)s.Spad;
@@ -238,26 +259,48 @@ DevProblem problem_for(const Solver &s, int off, int cnt) {
 }
 
 // Runs columns [off, off+cnt) through one pass; mode as launch_init.
+// Per stage J (main stream M, side stream D):
+//   M: part1(J) -> gemm(J) on the rows of tile J-1 -> [ev_top] -> gemm(J) on
+//      rows above tile J-1 -> wait ev_diag
+//   D: wait ev_top -> diag(J-1) -> [ev_diag]
+// so diag(J-1), a latency-bound sequential kernel, overlaps the bulk of the
+// FP64-bound GEMM of stage J.  Stage operands alternate buffers by parity.
 int run_pass(Solver &s, int mode, int its, int off, int cnt) {
+    Workspace &w = *s.w;
+    HSR_CK(w.ensure_side());
+    cudaStream_t M = s.st, D = w.side;
     for (int c0 = 0; c0 < cnt; c0 += s.Scap) {
         const int cc = std::min(s.Scap, cnt - c0);
-        DevProblem P = problem_for(s, off + c0, cc);
-        HSR_LAUNCH_C(kcSetup, s.st, launch_init(P, mode, s.eps3_dev, its, s.st));
+        DevProblem P0 = problem_for(s, off + c0, cc, 0);
+        HSR_LAUNCH_C(kcSetup, M, launch_init(P0, mode, s.eps3_dev, its, M));
         if (mode == 2) ++g_launches;
         const int b = s.tlsz;
-        const bool big = (size_t)(64 * b + 2 * (b + 1)) * sizeof(double) > 200 * 1024;
-        double *gs = big ? s.w->gscratch.as<double>() : nullptr;
-        for (int J = s.T - 1; J >= 0; --J) {
+        const bool big = diag_smem_bytes(b) < (size_t)64 * b * sizeof(double);
+        double *gs = big ? w.gscratch.as<double>() : nullptr;
+        {
+            const int J = s.T - 1;
+            DevProblem P = problem_for(s, off + c0, cc, J & 1);
+            HSR_LAUNCH_C(kcDiag, M, launch_diag(P, J, s.fr[J + 1] - s.fr[J], gs, M));
+        }
+        for (int J = s.T - 1; J >= 1; --J) {
             const int bj = s.fr[J + 1] - s.fr[J];
-            HSR_LAUNCH_C(kcDiag, s.st, launch_diag(P, J, bj, big ? gs : nullptr, s.st));
-            if (J == 0) break;
-            HSR_LAUNCH_C(kcPart1, s.st, launch_part1(P, J, s.st));
-            HSR_LAUNCH_C(kcGemm, s.st, launch_gemm(P, J, s.fr[J], s.tmH, s.tmW, s.tmZ, s.st));
+            DevProblem P = problem_for(s, off + c0, cc, J & 1);
+            DevProblem Pn = problem_for(s, off + c0, cc, (J - 1) & 1);
+            HSR_LAUNCH_C(kcPart1, M, launch_part1(P, J, M));
+            HSR_LAUNCH_C(kcGemm, M, launch_gemm(P, J, s.fr[J - 1], s.fr[J], s.tmH, s.tmW[J & 1], s.tmZ[J & 1], M));
+            HSR_CK(cudaEventRecord(w.ev_top, M));
+            HSR_CK(cudaStreamWaitEvent(D, w.ev_top, 0));
+            HSR_LAUNCH_C(kcDiag, D, launch_diag(Pn, J - 1, s.fr[J] - s.fr[J - 1], gs, D));
+            HSR_CK(cudaEventRecord(w.ev_diag, D));
+            if (s.fr[J - 1] > 0)
+                HSR_LAUNCH_C(kcGemm, M, launch_gemm(P, J, 0, s.fr[J - 1], s.tmH, s.tmW[J & 1], s.tmZ[J & 1], M));
+            HSR_CK(cudaStreamWaitEvent(M, w.ev_diag, 0));
             if (g_timing.enabled) g_timing.gemm_fma[0] += (double)s.fr[J] * (2.0 * bj - 1.0) * cc;
         }
-        HSR_LAUNCH_C(kcFinal, s.st, launch_finalize(P, s.d_colnorm + off + c0, s.d_status + off + c0,
-                                                     s.d_scale ? s.d_scale + off + c0 : nullptr, s.st));
-        HSR_LAUNCH_C(kcFinal, s.st, launch_normalize(P, s.d_colnorm + off + c0, s.d_status + off + c0, s.st));
+        DevProblem P = problem_for(s, off + c0, cc, 0);
+        HSR_LAUNCH_C(kcFinal, M, launch_finalize(P, s.d_colnorm + off + c0, s.d_status + off + c0,
+                                                 s.d_scale ? s.d_scale + off + c0 : nullptr, M));
+        HSR_LAUNCH_C(kcFinal, M, launch_normalize(P, s.d_colnorm + off + c0, s.d_status + off + c0, M));
     }
     return HSR_OK;
 }
@@ -302,7 +345,7 @@ int solve_device(int n, const double *dH, long long ldh, int S, double *dwr, int
         size_t free_b = 0, total_b = 0;
         cudaMemGetInfo(&free_b, &total_b);
         double budget = o.hbm_budget_bytes > 0 ? o.hbm_budget_bytes : 0.6 * (double)free_b;
-        const double per_col = 8.0 * (4.0 * round_up(n, 4) + 2.0 * tlsz + 2.0 * T + 8) + T;
+        const double per_col = 8.0 * (4.0 * round_up(n, 4) + 4.0 * tlsz + 2.0 * T + 16) + T;
         long long cap = (long long)(budget / per_col);
         cap = std::max<long long>(32, std::min<long long>(cap, S));
         cap = std::min<long long>(cap, 65535);  // grid.y extent of the per-column kernels
@@ -316,9 +359,9 @@ int solve_device(int n, const double *dH, long long ldh, int S, double *dwr, int
     HSR_CK(w.Sr.ensure((size_t)n * Sp * 8));
     HSR_CK(w.beta.ensure((size_t)T * Sp * 8));
     HSR_CK(w.ynorm.ensure((size_t)T * Sp * 8));
-    HSR_CK(w.W.ensure((size_t)tlsz * Sp * 8));
-    HSR_CK(w.Zs.ensure((size_t)tlsz * Sp * 8));
-    HSR_CK(w.vecs.ensure(4 * Sp * 8));
+    HSR_CK(w.W.ensure(2 * (size_t)tlsz * Sp * 8));
+    HSR_CK(w.Zs.ensure(2 * (size_t)tlsz * Sp * 8));
+    HSR_CK(w.vecs.ensure(2 * 4 * Sp * 8));
     HSR_CK(w.Zslow.ensure((size_t)T * tlsz * Sp * 8));
     HSR_CK(w.slow.ensure((size_t)T * Sp));
     HSR_CK(w.fr.ensure((size_t)(T + 1) * sizeof(int)));
@@ -328,10 +371,10 @@ int solve_device(int n, const double *dH, long long ldh, int S, double *dwr, int
     HSR_CK(w.status.ensure((size_t)S * sizeof(int)));
     HSR_CK(w.pert.ensure((size_t)S));
     if (!d_scale_user && (h_scale || h_tile_scales)) HSR_CK(w.scale.ensure((size_t)S * 8));
-    if ((size_t)(64 * tlsz + 2 * (tlsz + 1)) * sizeof(double) > 200 * 1024)
+    if (diag_smem_bytes(tlsz) < (size_t)64 * tlsz * sizeof(double))
         HSR_CK(w.gscratch.ensure((size_t)((Sp + 31) / 32) * 64 * tlsz * 8));
-    HSR_CK(cudaMemsetAsync(w.W.p, 0, (size_t)tlsz * Sp * 8, st));
-    HSR_CK(cudaMemsetAsync(w.Zs.p, 0, (size_t)tlsz * Sp * 8, st));
+    HSR_CK(cudaMemsetAsync(w.W.p, 0, 2 * (size_t)tlsz * Sp * 8, st));
+    HSR_CK(cudaMemsetAsync(w.Zs.p, 0, 2 * (size_t)tlsz * Sp * 8, st));
     HSR_CK(cudaMemsetAsync(w.err.p, 0, 16, st));
     HSR_CK(cudaMemcpyAsync(w.fr.p, s.fr.data(), (T + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
     s.d_status = d_status_user ? d_status_user : w.status.as<int>();
@@ -341,8 +384,12 @@ int solve_device(int n, const double *dH, long long ldh, int S, double *dwr, int
 
     if (!make_map(&s.tmH, dH, (unsigned long long)n, (unsigned long long)n, (unsigned long long)ldh, kGemmBM,
                   kGemmKC) ||
-        !make_map(&s.tmW, w.W.as<double>(), Sp, (unsigned long long)tlsz, Sp, kGemmBN, kGemmKC) ||
-        !make_map(&s.tmZ, w.Zs.as<double>(), Sp, (unsigned long long)tlsz, Sp, kGemmBN, kGemmKC))
+        !make_map(&s.tmW[0], w.W.as<double>(), Sp, (unsigned long long)tlsz, Sp, kGemmBN, kGemmKC) ||
+        !make_map(&s.tmW[1], w.W.as<double>() + (size_t)tlsz * Sp, Sp, (unsigned long long)tlsz, Sp, kGemmBN,
+                  kGemmKC) ||
+        !make_map(&s.tmZ[0], w.Zs.as<double>(), Sp, (unsigned long long)tlsz, Sp, kGemmBN, kGemmKC) ||
+        !make_map(&s.tmZ[1], w.Zs.as<double>() + (size_t)tlsz * Sp, Sp, (unsigned long long)tlsz, Sp, kGemmBN,
+                  kGemmKC))
         return HSR_ERR_CUDA;
 
     // Norms and eps3.

@@ -137,19 +137,28 @@ cudaError_t launch_init(const DevProblem &P, int mode, const double *eps3_dev, i
 }
 
 // -------------------------------------------------------------- diagonal
-// One lane per shift.  v (running column) and y (solution tile) live in
-// shared memory as [row][lane] so that every access is conflict-free; the
-// column of H needed by step j is staged one step ahead with cp.async and
-// read as a broadcast.  When 2*32*b doubles do not fit, v/y live in a global
-// scratch region instead (same code through generic pointers).
+// 32 shifts per CTA, one per lane, and four warps per CTA: the FP64 unit is
+// per SM sub-partition, so the vector part of each step (the updates of
+// y(0:j-2) and of the running column) is split over the four warps by row
+// (i mod 4), while every warp evaluates the short scalar chain of the step
+// (Givens, 1x1 solve, overflow decisions) itself -- identical arithmetic, no
+// broadcast.  v (running column) and y (solution tile) live in shared memory
+// as [row][lane]; the column of H needed by step j is staged one step ahead
+// with cp.async and read as a broadcast.  Per-warp maxima of |y| and |v|
+// meet in shared memory once per step.  When 2*32*b doubles do not fit, v/y
+// live in a global scratch region instead (same code, generic pointers).
+constexpr int kDiagWarps = 4;
+
 size_t diag_smem_bytes(int b) {
-    const size_t full = (size_t)(64 * b + 2 * (b + 1)) * sizeof(double);
-    return full <= 200 * 1024 ? full : (size_t)(2 * (b + 1)) * sizeof(double);
+    const size_t small = (size_t)(2 * (b + 1)) * sizeof(double) + (size_t)2 * kDiagWarps * 2 * 32 * 8;
+    const size_t full = small + (size_t)64 * b * sizeof(double);
+    return full <= 200 * 1024 ? full : small;
 }
 
-__global__ void __launch_bounds__(32) k_diag(DevProblem P, int J, double *gscratch) {
+__global__ void __launch_bounds__(32 * kDiagWarps) k_diag(DevProblem P, int J, double *gscratch) {
     extern __shared__ double sm[];
-    const int lane = threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
     const int k0 = blockIdx.x * 32;
     const int k = k0 + lane;
     const bool act = k < P.S;
@@ -157,20 +166,23 @@ __global__ void __launch_bounds__(32) k_diag(DevProblem P, int J, double *gscrat
     const bool is = P.is != 0;
     const size_t Spad = (size_t)P.Spad;
 
-    double *hc = sm;                                   // [2][b+1]
+    double *hc = sm;                                          // [2][b+1]
+    // Per-warp partial maxima, double-buffered by step parity: [2][W][2][32].
+    unsigned long long *pmax = reinterpret_cast<unsigned long long *>(sm + 2 * (b + 1));
     double *v, *y;
     if (gscratch) {
         v = gscratch + (size_t)blockIdx.x * 64 * b;
         y = v + (size_t)32 * b;
     } else {
-        v = sm + 2 * (b + 1);
+        v = sm + 2 * (b + 1) + 2 * kDiagWarps * 2 * 32;
         y = v + (size_t)32 * b;
     }
 #define V(i) v[(size_t)(i) * 32 + lane]
 #define Y(i) y[(size_t)(i) * 32 + lane]
+#define PMAX(par, w, which) pmax[(((par) * kDiagWarps + (w)) * 2 + (which)) * 32 + lane]
 
     // Load the crossover column and the right-hand side tile, transposed.
-    for (int c = 0; c < 32; ++c) {
+    for (int c = wid; c < 32; c += kDiagWarps) {
         const int kc = k0 + c;
         if (kc < P.S) {
             const double *rc = P.R + l + (size_t)kc * P.ldr;
@@ -186,7 +198,6 @@ __global__ void __launch_bounds__(32) k_diag(DevProblem P, int J, double *gscrat
             }
         }
     }
-    __syncwarp();
 
     const double mu = act ? P.wr[k] : 0.0;
     const double smin = fmax(DBL_EPSILON / 2 * fabs(mu), P.smlnum);
@@ -194,91 +205,141 @@ __global__ void __launch_bounds__(32) k_diag(DevProblem P, int J, double *gscrat
     double beta = act ? P.beta[(size_t)J * Spad + k] : sc_one(is);
     int pert = 0;
 
-    // Running maxima of |y(0:j-2)| and |v(0:j-2)| for the next step.
-    unsigned long long ymax = 0, vmax = 0;
-    for (int i = 0; i < b - 2; ++i) {
-        ymax = umax64(ymax, abs_bits(Y(i)));
-        vmax = umax64(vmax, abs_bits(V(i)));
-    }
-
-    const double *Hd = P.H + l + (size_t)l * P.ldh;    // H(l, l)
-    auto stage_col = [&](int col, double *dst) {       // H(l : l+col+1, l+col)
+    const double *Hd = P.H + l + (size_t)l * P.ldh;          // H(l, l)
+    auto stage_col = [&](int col, double *dst) {              // H(l : l+col+1, l+col), warp 0
         int rows = col + 2;
         if (rows > b) rows = b;
         const double *src = Hd + (size_t)col * P.ldh;
         for (int i = lane; i < rows; i += 32) cp_async8(dst + i, src + i);
         cp_async_commit();
     };
-    int buf = 0;
-    if (b >= 2) stage_col(b - 2, hc);
+    if (wid == 0 && b >= 2) stage_col(b - 2, hc);
+    __syncthreads();                                           // tiles loaded
 
+    // Per-warp maxima of |y(0:b-3)| and |v(0:b-3)| for the first step.
+    {
+        unsigned long long ym = 0, vm = 0;
+        for (int i = wid; i < b - 2; i += kDiagWarps) {
+            ym = umax64(ym, abs_bits(Y(i)));
+            vm = umax64(vm, abs_bits(V(i)));
+        }
+        PMAX(0, wid, 0) = ym;
+        PMAX(0, wid, 1) = vm;
+    }
+    // v(j) and y(j) of the current step are carried in registers: every warp
+    // computes them identically in the previous step.
+    double vcar = V(b - 1), ycar = Y(b - 1);
+
+    int buf = 0, par = 0;
     for (int j = b - 1; j >= 1; --j) {
-        cp_async_wait_all();
-        __syncwarp();
-        const double *hcol = hc + buf * (b + 1);       // column j-1 of the tile
-        if (j >= 2) stage_col(j - 2, hc + (buf ^ 1) * (b + 1));
-
+        if (wid == 0) cp_async_wait_all();
+        __syncthreads();                                       // previous step's rows and column j-1 visible
+        const double *hcol = hc + buf * (b + 1);              // column j-1 of the tile
+        if (wid == 0 && j >= 2) stage_col(j - 2, hc + (buf ^ 1) * (b + 1));
+        unsigned long long ymax = 0, vmax = 0;
+#pragma unroll
+        for (int w = 0; w < kDiagWarps; ++w) {
+            ymax = umax64(ymax, PMAX(par, w, 0));
+            vmax = umax64(vmax, PMAX(par, w, 1));
+        }
         const double hsub = hcol[j];
-        const double vj = V(j);
+        const double hdiag = hcol[j - 1] - mu;
+        const double vj = vcar, vjm1 = V(j - 1);
+        double yj = ycar, yjm1 = Y(j - 1);
+
         double c, s;
         givens(vj, hsub, c, s);
-        if (act) {
+        if (act && wid == 0) {
             P.Cr[(size_t)(l + j) * Spad + k] = c;
             P.Sr[(size_t)(l + j) * Spad + k] = s;
         }
-
         // y(j) := y(j) / R(j,j) robustly (solve-task.c:76-81).
-        double yj = Y(j);
         double phi = sc_one(is);
         pert |= solve_1x1(smin, c * vj, s * hsub, yj, phi, is);
         beta = sc_combine(beta, phi, is);
-        {
-            const double a = sc_value(phi, is);
-            if (a != 1.0) {
-                for (int i = 0; i < b; ++i)
-                    if (i != j) Y(i) = a * Y(i);
-                ymax = abs_bits(a * from_bits(ymax));
-            }
+        const double a1 = sc_value(phi, is);
+        if (a1 != 1.0) {
+            yjm1 = a1 * yjm1;
+            ymax = abs_bits(a1 * from_bits(ymax));
         }
-
         // y(j-1) (solve-task.c:84-90).
-        const double hdiag = hcol[j - 1] - mu;
-        const double vjm1 = V(j - 1);
-        double yjm1 = Y(j - 1);
         phi = protect_double_update(fabs(vjm1), fabs(yj), fabs(hdiag), fabs(yj), fabs(yjm1), is);
-        {
-            const double a = sc_value(phi, is);
-            if (a != 1.0) {
-                for (int i = 0; i < b; ++i) Y(i) = a * Y(i);
-                yj = a * yj;
-                yjm1 = a * yjm1;
-                ymax = abs_bits(a * from_bits(ymax));
-            }
+        const double a2 = sc_value(phi, is);
+        if (a2 != 1.0) {
+            yj = a2 * yj;
+            yjm1 = a2 * yjm1;
+            ymax = abs_bits(a2 * from_bits(ymax));
         }
         beta = sc_combine(beta, phi, is);
         {
             const double yc = yj * c, ys = yj * s;
             yjm1 = fma(ys, hdiag, fma(-yc, vjm1, yjm1));
         }
-        Y(j - 1) = yjm1;
-
         // y(0:j-2) (solve-task.c:92-100).
         phi = protect_double_update(from_bits(vmax), fabs(yj), Hnorm, fabs(yj), from_bits(ymax), is);
-        {
-            const double a = sc_value(phi, is);
-            if (a != 1.0) {
-                for (int i = 0; i < b; ++i) Y(i) = a * Y(i);
-                yj = a * yj;
-            }
+        const double a3 = sc_value(phi, is);
+        if (a3 != 1.0) {
+            yj = a3 * yj;
+            yjm1 = a3 * yjm1;
         }
         beta = sc_combine(beta, phi, is);
+        const bool scaled = (a1 != 1.0) || (a2 != 1.0) || (a3 != 1.0);
+        if (scaled) {
+            // Rare: the whole-vector scale() also reaches the solved rows j+1 .. b-1.
+            for (int i = j + 1 + ((wid - (j + 1)) % kDiagWarps + kDiagWarps) % kDiagWarps; i < b; i += kDiagWarps) {
+                double t = Y(i);
+                if (a1 != 1.0) t = a1 * t;
+                if (a2 != 1.0) t = a2 * t;
+                if (a3 != 1.0) t = a3 * t;
+                Y(i) = t;
+            }
+        }
         const double yc = yj * c, ys = yj * s;
         unsigned long long ymx = 0, vmx = 0;
         const int lim = j - 1;
-#pragma unroll 4
-        for (int i = 0; i < lim; ++i) {
+        // Rows i = wid, wid+4, ... < j-1 in batches of 4: loads first, then
+        // the independent FMA chains, then the stores.
+        int i = wid;
+        for (; i + 3 * kDiagWarps < lim; i += 4 * kDiagWarps) {
+            double hh[4], yy[4], vv[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                hh[q] = hcol[i + q * kDiagWarps];
+                yy[q] = Y(i + q * kDiagWarps);
+                vv[q] = V(i + q * kDiagWarps);
+            }
+            if (scaled) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (a1 != 1.0) yy[q] = a1 * yy[q];
+                    if (a2 != 1.0) yy[q] = a2 * yy[q];
+                    if (a3 != 1.0) yy[q] = a3 * yy[q];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                yy[q] = fma(ys, hh[q], fma(-yc, vv[q], yy[q]));
+                vv[q] = fma(c, hh[q], s * vv[q]);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int r = i + q * kDiagWarps;
+                Y(r) = yy[q];
+                V(r) = vv[q];
+                if (r < lim - 1) {
+                    ymx = umax64(ymx, abs_bits(yy[q]));
+                    vmx = umax64(vmx, abs_bits(vv[q]));
+                }
+            }
+        }
+        for (; i < lim; i += kDiagWarps) {
             const double h = hcol[i];
             double yi = Y(i), vi = V(i);
+            if (scaled) {
+                if (a1 != 1.0) yi = a1 * yi;
+                if (a2 != 1.0) yi = a2 * yi;
+                if (a3 != 1.0) yi = a3 * yi;
+            }
             yi = fma(ys, h, fma(-yc, vi, yi));
             vi = fma(c, h, s * vi);
             Y(i) = yi;
@@ -288,18 +349,20 @@ __global__ void __launch_bounds__(32) k_diag(DevProblem P, int J, double *gscrat
                 vmx = umax64(vmx, abs_bits(vi));
             }
         }
-        // Next annihilation column (solve-task.c:105-108).
-        V(j - 1) = fma(c, hdiag, s * vjm1);
-        Y(j) = yj;
-        ymax = ymx;
-        vmax = vmx;
+        PMAX(par ^ 1, wid, 0) = ymx;
+        PMAX(par ^ 1, wid, 1) = vmx;
+        if (j % kDiagWarps == wid) Y(j) = yj;                 // solved entry, by its owner
+        // Next annihilation column entry (solve-task.c:105-108) and y(j-1).
+        vcar = fma(c, hdiag, s * vjm1);
+        ycar = yjm1;
         buf ^= 1;
+        par ^= 1;
     }
-    __syncwarp();
 
     double c0 = 0.0, s0 = 0.0;
     {
-        double v0 = V(0);
+        double v0 = b >= 2 ? vcar : V(0);
+        double y0 = b >= 2 ? ycar : Y(0);
         double hleft = 0.0;
         if (J > 0) {
             // Final rotation with H(l, l-1) (reduce.c:53-61, solve-task.c:111-118).
@@ -310,40 +373,40 @@ __global__ void __launch_bounds__(32) k_diag(DevProblem P, int J, double *gscrat
                 c0 = 1.0;
                 s0 = 0.0;
             }
-            if (act) {
+            if (act && wid == 0) {
                 P.Cr[(size_t)l * Spad + k] = c0;
                 P.Sr[(size_t)l * Spad + k] = s0;
             }
             v0 = fma(v0, c0, -(hleft * s0));
         }
-        double y0 = Y(0);
         double phi = sc_one(is);
         pert |= solve_1x1(smin, v0, 0.0, y0, phi, is);
         beta = sc_combine(beta, phi, is);
         const double a = sc_value(phi, is);
+        __syncthreads();                                       // last step's rows written
         if (a != 1.0)
-            for (int i = 1; i < b; ++i) Y(i) = a * Y(i);
-        Y(0) = y0;
+            for (int i = 1 + ((wid - 1) % kDiagWarps + kDiagWarps) % kDiagWarps; i < b; i += kDiagWarps)
+                Y(i) = a * Y(i);
+        if (wid == 0) Y(0) = y0;
     }
-    __syncwarp();
+    __syncthreads();
 
     // Store the solved tile, its scaling factor and the perturbation flag.
-    for (int c = 0; c < 32; ++c) {
+    for (int c = wid; c < 32; c += kDiagWarps) {
         const int kc = k0 + c;
         if (kc < P.S) {
             double *xc = P.X + l + (size_t)kc * P.ldx;
             for (int i = lane; i < b; i += 32) xc[i] = y[(size_t)i * 32 + c];
         }
     }
-    if (act) {
+    if (act && wid == 0) {
         P.beta[(size_t)J * Spad + k] = beta;
         if (pert) P.pert[k] = 1;
     }
     if (J == 0 || !act) return;
 
-    // Stage operands for the tiles above.
-    // W(q) = c_q * prod_{p<q} s_p, pi = prod s (crossover propagation).
-    {
+    if (wid == 0) {
+        // W(q) = c_q * prod_{p<q} s_p, pi = prod s (crossover propagation).
         double pk = 1.0;
         for (int q = 0; q < b; ++q) {
             const double cq = P.Cr[(size_t)(l + q) * Spad + k];
@@ -352,10 +415,9 @@ __global__ void __launch_bounds__(32) k_diag(DevProblem P, int J, double *gscrat
             pk = pk * sq;
         }
         P.pi[k] = pk;
-    }
-    // Ytilde2 = G_{b-1}^T ... G_1^T (c_0 x_0, x_1, ...) (update-task.c:193-220);
-    // Zs(q) = Ytilde2(q-1), Zs(0) = 0, zlast = Ytilde2(b-1).
-    {
+    } else if (wid == 1) {
+        // Ytilde2 = G_{b-1}^T ... G_1^T (c_0 x_0, x_1, ...) (update-task.c:193-220);
+        // Zs(q) = Ytilde2(q-1), Zs(0) = 0, zlast = Ytilde2(b-1).
         unsigned long long zmx = 0;
         double z = c0 * Y(0);
         P.Zs[k] = 0.0;
@@ -375,17 +437,19 @@ __global__ void __launch_bounds__(32) k_diag(DevProblem P, int J, double *gscrat
     }
 #undef V
 #undef Y
+#undef PMAX
 }
 
 cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st) {
-    const size_t smem = gscratch ? (size_t)(2 * (b + 1)) * sizeof(double) : diag_smem_bytes(b);
+    const size_t small = (size_t)(2 * (b + 1)) * sizeof(double) + (size_t)2 * kDiagWarps * 2 * 32 * 8;
+    const size_t smem = gscratch ? small : diag_smem_bytes(b);
     static size_t configured = 0;
     if (smem > configured) {
         cudaError_t e = cudaFuncSetAttribute(k_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    k_diag<<<(P.S + 31) / 32, 32, smem, st>>>(P, J, gscratch);
+    k_diag<<<(P.S + 31) / 32, 32 * kDiagWarps, smem, st>>>(P, J, gscratch);
     return cudaGetLastError();
 }
 
@@ -522,13 +586,15 @@ struct GemmSmem {
 size_t gemm_smem_bytes() { return sizeof(GemmSmem) + 128; }
 
 __global__ void __launch_bounds__(256, 2)
-k_gemm(DevProblem P, int J, const __grid_constant__ CUtensorMap tmH,
+k_gemm(DevProblem P, int J, int row_lo, int row_hi, const __grid_constant__ CUtensorMap tmH,
        const __grid_constant__ CUtensorMap tmW, const __grid_constant__ CUtensorMap tmZ) {
     extern __shared__ unsigned char smraw[];
     GemmSmem &sm = *reinterpret_cast<GemmSmem *>(
         (reinterpret_cast<uintptr_t>(smraw) + 127) & ~uintptr_t(127));
     const int tid = threadIdx.x;
-    const int row0 = blockIdx.x * kGemmBM;
+    // Row blocks start at row_lo rounded down to 8, so the TMA x coordinate
+    // is always 16-byte aligned; rows outside [row_lo, row_hi) are not stored.
+    const int row0 = (row_lo & ~7) + blockIdx.x * kGemmBM;
     const int col0 = blockIdx.y * kGemmBN;
     const int l = P.fr[J], b = P.fr[J + 1] - l;
     const int nk = (b + kGemmKC - 1) / kGemmKC;
@@ -599,7 +665,6 @@ k_gemm(DevProblem P, int J, const __grid_constant__ CUtensorMap tmH,
     }
 
     // Epilogue.
-    const int M = l;
     const size_t Spad = (size_t)P.Spad;
     unsigned long long *ynb = reinterpret_cast<unsigned long long *>(P.ynorm);
 #pragma unroll
@@ -612,7 +677,7 @@ k_gemm(DevProblem P, int J, const __grid_constant__ CUtensorMap tmH,
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
             const int row = row0 + 4 * tr + r;
-            if (row >= M) continue;
+            if (row < row_lo || row >= row_hi) continue;
             const size_t ir = row + (size_t)col * P.ldr;
             const size_t ix = row + (size_t)col * P.ldx;
             const double rold = P.R[ir];
@@ -646,7 +711,7 @@ k_gemm(DevProblem P, int J, const __grid_constant__ CUtensorMap tmH,
     }
 }
 
-cudaError_t launch_gemm(const DevProblem &P, int J, int rows, const CUtensorMap &tmH,
+cudaError_t launch_gemm(const DevProblem &P, int J, int row_lo, int row_hi, const CUtensorMap &tmH,
                         const CUtensorMap &tmW, const CUtensorMap &tmZ, cudaStream_t st) {
     static bool configured = false;
     const size_t smem = gemm_smem_bytes();
@@ -655,9 +720,10 @@ cudaError_t launch_gemm(const DevProblem &P, int J, int rows, const CUtensorMap 
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    if (rows <= 0) return cudaSuccess;
-    dim3 g((rows + kGemmBM - 1) / kGemmBM, (P.S + kGemmBN - 1) / kGemmBN);
-    k_gemm<<<g, 256, smem, st>>>(P, J, tmH, tmW, tmZ);
+    if (row_hi <= row_lo) return cudaSuccess;
+    const int span = row_hi - (row_lo & ~7);
+    dim3 g((span + kGemmBM - 1) / kGemmBM, (P.S + kGemmBN - 1) / kGemmBN);
+    k_gemm<<<g, 256, smem, st>>>(P, J, row_lo, row_hi, tmH, tmW, tmZ);
     return cudaGetLastError();
 }
 

@@ -53,7 +53,8 @@ cudaError_t launch_init(const DevProblem &P, int mode, const double *eps3_dev,
 cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st);
 size_t diag_smem_bytes(int b);
 cudaError_t launch_part1(const DevProblem &P, int J, cudaStream_t st);
-cudaError_t launch_gemm(const DevProblem &P, int J, int rows, const CUtensorMap &tmH,
+// Crossover/update GEMM of stage J over rows [row_lo, row_hi) (row_hi <= fr[J]).
+cudaError_t launch_gemm(const DevProblem &P, int J, int row_lo, int row_hi, const CUtensorMap &tmH,
                         const CUtensorMap &tmW, const CUtensorMap &tmZ, cudaStream_t st);
 size_t gemm_smem_bytes();
 cudaError_t launch_finalize(const DevProblem &P, double *colnorm, int *status,

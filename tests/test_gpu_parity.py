@@ -25,6 +25,7 @@ def _device(H, wr, tlsz, rhs_tlsz=16, **kw):
     (1, 4, 1), (2, 4, 2), (7, 8, 3), (60, 64, 4),          # one tile
     (64, 16, 5), (100, 40, 6), (203, 40, 7), (256, 64, 8),  # several tiles, ragged first tile
     (333, 12, 9),
+    (900, 440, 10),                                         # v/y in global scratch (tile too big for smem)
 ])
 def test_bitwise_vs_oracle(gpu_lib, n, tlsz, seed):
     H, lam = G.real_spectrum(n, seed)
