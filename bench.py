@@ -186,11 +186,11 @@ def run_gpu(args, H, wr, rank, world):
             raise RuntimeError("device call failed: %d" % rc)
         return rc
 
-    dfma, dmma = hsr.fp64_peak(100.0)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             step()
     torch.cuda.synchronize()
+    dfma, dmma = hsr.fp64_peak(200.0)          # after warm-up: clocks ramped
     lib.hsr_set_kernel_timing(1)
     kms = np.zeros(6)
     kl = np.zeros(6, dtype=np.int64)

@@ -38,19 +38,49 @@ __device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsig
     return a > b ? a : b;
 }
 
+// ------------------------------------------ exact integer-pipe shortcuts
+// FP64 issues at a fraction of the integer rate here, so comparisons against
+// fixed thresholds run on IEEE bit patterns (for non-negative finite values
+// the order of the patterns is the order of the numbers; NaN patterns sort
+// above +Inf and every shortcut below is written so that NaN fails it and
+// takes the exact path), and multiplications or divisions by a factor that
+// is exactly 1.0 are skipped (1*x == x bit for bit).  Each shortcut returns
+// exactly what the full expression returns.
+__device__ __forceinline__ unsigned long long ubits(double x) {
+    return (unsigned long long)__double_as_longlong(x);
+}
+__device__ __forceinline__ unsigned long long mag(double x) { return ubits(x) & 0x7fffffffffffffffULL; }
+constexpr unsigned long long kOneBits = 0x3ff0000000000000ULL;
+constexpr unsigned long long kInfBits = 0x7ff0000000000000ULL;
+__host__ __device__ constexpr unsigned long long pow2_bits(int e) { return (unsigned long long)(1023 + e) << 52; }
+__device__ __forceinline__ bool is_one(double a) { return ubits(a) == kOneBits; }
+__device__ __forceinline__ bool is_zero(double a) { return (ubits(a) << 1) == 0ULL; }
+__device__ __forceinline__ double neg(double a) { return __longlong_as_double((long long)(ubits(a) ^ 0x8000000000000000ULL)); }
+
 // ------------------------------------------------ scaling-factor algebra
 // robust.c:24-121.  `is` selects base-2 exponents (INTSCALING) at run time.
 __device__ __forceinline__ double sc_one(bool is) { return is ? 0.0 : 1.0; }
-__device__ __forceinline__ double sc_value(double a, bool is) { return is ? ldexp(1.0, (int)a) : a; }
-__device__ __forceinline__ double sc_combine(double g, double phi, bool is) { return is ? phi + g : phi * g; }
+__device__ __forceinline__ double sc_value(double a, bool is) {
+    if (is) return is_zero(a) ? 1.0 : ldexp(1.0, (int)a);
+    return a;
+}
+__device__ __forceinline__ double sc_combine(double g, double phi, bool is) {
+    if (is) return is_zero(phi) ? g : phi + g;
+    return is_one(phi) ? g : phi * g;
+}
 __device__ __forceinline__ double sc_upscale(double amin, double a, bool is) {
     return is ? ldexp(1.0, (int)(amin - a)) : amin / a;
 }
 __device__ __forceinline__ double sc_min(double a, double b, bool is) { return is ? (a < b ? a : b) : fmin(a, b); }
 
 // ------------------------------------------------- robust scalar kernels
-// protect_real_division (robust.c:144-166)
+// protect_real_division (robust.c:144-166).  Shortcut: with t normal and
+// exponent(b) <= exponent(t) + 989, |b| < 2^990 |t| <= fl(|t| Omega), so
+// neither branch rescales.
 __device__ __forceinline__ double protect_real_division(double b, double t) {
+    const unsigned long long mb = mag(b), mt = mag(t);
+    if (mt >= pow2_bits(-1022) && mt <= kInfBits && mb <= kInfBits && (mb >> 52) < (mt >> 52) + 990)
+        return 1.0;
     double scale = 1.0;
     const double at = fabs(t), ab = fabs(b);
     if (at < kOmegaInv) {
@@ -60,15 +90,20 @@ __device__ __forceinline__ double protect_real_division(double b, double t) {
     }
     return scale;
 }
-// protect_sum (robust.c:175-185)
+// protect_sum (robust.c:175-185).  Shortcut: |x|, |y| < 2^995 gives
+// Omega - |y| > 2^995 > |x|.
 __device__ __forceinline__ double protect_sum(double x, double y) {
+    if (mag(x) < pow2_bits(995) && mag(y) < pow2_bits(995)) return 1.0;
     double scale = 1.0;
     if ((x > 0 && y > 0) || (x < 0 && y < 0))
         if (fabs(x) > kOmega - fabs(y)) scale = 0.5;
     return scale;
 }
-// protect_update (robust.c:220-262)
+// protect_update (robust.c:220-262), for t, x, y >= 0.  Shortcut: t, x <
+// 2^497 and y < 2^995 give t*x < 2^994 < Omega - y and t < (Omega - y)/x.
 __device__ __forceinline__ double protect_update(double tnorm, double xnorm, double ynorm, bool is) {
+    if (mag(tnorm) < pow2_bits(497) && mag(xnorm) < pow2_bits(497) && mag(ynorm) < pow2_bits(995))
+        return sc_one(is);
     double scale = 1.0;
     if (xnorm <= 1.0) {
         if (tnorm * xnorm > kOmega - ynorm) scale = 0.5;
@@ -82,44 +117,49 @@ __device__ __forceinline__ double protect_double_update(double t1, double x1, do
                                                         double y, bool is) {
     const double a1 = protect_update(t1, x1, y, is);
     const double a2 = protect_update(t2, x2, y, is);
+    if (ubits(a1) == ubits(a2)) return a1;
     return is ? (a1 < a2 ? a1 : a2) : fmin(a1, a2);
 }
 // solve_1x1_real_system (robust.c:422-479); returns 1 if |t-lambda| < smin.
 __device__ __forceinline__ int solve_1x1(double smin, double t, double lambda, double &x,
                                          double &scale, bool is) {
     int info = 0;
-    const double s = protect_sum(t, -lambda);
-    double csr = (s * t) - (s * lambda);
-    if (fabs(csr) < smin) {
+    const double s = protect_sum(t, neg(lambda));
+    double csr = is_one(s) ? t - lambda : (s * t) - (s * lambda);
+    if (mag(csr) < ubits(smin)) {          // fabs(csr) < smin, smin > 0
         csr = smin;
         info = 1;
     }
     const double alpha = protect_real_division(x, csr);
-    x = (alpha * x) / csr;
-    scale = is ? (double)ilogb(alpha / s) : alpha / s;
+    x = is_one(alpha) ? x / csr : (alpha * x) / csr;
+    if (is_one(alpha) && is_one(s)) scale = sc_one(is);
+    else scale = is ? (double)ilogb(alpha / s) : alpha / s;
     return info;
 }
 
 // ------------------------------------------------------------- Givens
 // LAPACK >= 3.10 dlartg (E. Anderson, "Algorithm 978: Safe scaling in the
 // Level 1 BLAS", ACM TOMS 44(1), 2017), transposed as in reduce.c:14-24.
+// rtmin = sqrt(2^-1022) = 2^-511 and rtmax = sqrt(2^1021) = 2^510 * sqrt(2)
+// (correctly rounded), as bit patterns.
+constexpr unsigned long long kRtminBits = 0x2000000000000000ULL;
+constexpr unsigned long long kRtmaxBits = 0x5fd6a09e667f3bcdULL;
 __device__ __forceinline__ void givens(double f, double g, double &c, double &s) {
     const double safmin = 2.2250738585072014e-308;   // 2^-1022
     const double safmax = 1.0 / safmin;               // 2^1022
-    const double rtmin = sqrt(safmin);
-    const double rtmax = sqrt(safmax / 2);
-    const double f1 = fabs(f), g1 = fabs(g);
+    const unsigned long long mf = mag(f), mg = mag(g);
     double sv;
-    if (g == 0.0) {
+    if (is_zero(g)) {
         c = 1.0; sv = 0.0;
-    } else if (f == 0.0) {
+    } else if (is_zero(f)) {
         c = 0.0; sv = copysign(1.0, g);
-    } else if (f1 > rtmin && f1 < rtmax && g1 > rtmin && g1 < rtmax) {
+    } else if (mf > kRtminBits && mf < kRtmaxBits && mg > kRtminBits && mg < kRtmaxBits) {
         const double d = sqrt(f * f + g * g);
-        c = f1 / d;
+        c = fabs(f) / d;
         const double r = copysign(d, f);
         sv = g / r;
     } else {
+        const double f1 = fabs(f), g1 = fabs(g);
         const double u = fmin(safmax, fmax(safmin, fmax(f1, g1)));
         const double fs = f / u, gs = g / u;
         const double d = sqrt(fs * fs + gs * gs);
@@ -127,7 +167,7 @@ __device__ __forceinline__ void givens(double f, double g, double &c, double &s)
         const double r = copysign(d, f);
         sv = gs / r;
     }
-    s = (-1.0) * sv;
+    s = neg(sv);
 }
 
 // ------------------------------------------- 2-norm, three accumulators
@@ -143,8 +183,9 @@ struct Nrm3 {
     __device__ __forceinline__ void init() { asml = amed = abig = 0.0; }
     __device__ __forceinline__ void add(double x) {
         const double ax = fabs(x);
-        if (ax > kTbig) { const double t = ax * kSbig; abig = fma(t, t, abig); }
-        else if (ax < kTsml) { const double t = ax * kSsml; asml = fma(t, t, asml); }
+        const unsigned long long m = mag(x);
+        if (m > pow2_bits(486) && m <= kInfBits) { const double t = ax * kSbig; abig = fma(t, t, abig); }
+        else if (m < pow2_bits(-511)) { const double t = ax * kSsml; asml = fma(t, t, asml); }
         else amed = fma(ax, ax, amed);
     }
     __device__ __forceinline__ double finish() const {

@@ -644,22 +644,34 @@ int hsr_probe_fp64_peak(double ms_target, double *dfma_gflops, double *dmma_gflo
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     const int blocks = sms * 4;
+    // Size one launch to ~ms_target/4, warm up, then time four launches
+    // back to back (clocks ramped), and report the throughput.
     auto measure = [&](bool dmma, double *out) -> int {
-        int iters = 1024;
+        int iters = 512;
         float ms = 0.f;
-        for (int rep = 0; rep < 8; ++rep) {
+        auto launch = [&]() {
+            return dmma ? launch_probe_dmma(w.probe.as<double>(), blocks, iters, 0)
+                        : launch_probe_dfma(w.probe.as<double>(), blocks, iters, 0);
+        };
+        for (int rep = 0; rep < 12; ++rep) {
             cudaEventRecord(e0, 0);
-            cudaError_t e = dmma ? launch_probe_dmma(w.probe.as<double>(), blocks, iters, 0)
-                                 : launch_probe_dfma(w.probe.as<double>(), blocks, iters, 0);
+            cudaError_t e = launch();
             cudaEventRecord(e1, 0);
             if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) return HSR_ERR_CUDA;
             cudaEventElapsedTime(&ms, e0, e1);
-            if (ms >= ms_target || iters > (1 << 24)) break;
-            iters = (int)std::min<double>((double)iters * std::max(2.0, 1.2 * ms_target / std::max(ms, 0.01f)),
-                                          (double)(1 << 24));
+            if (ms >= 0.25 * ms_target || iters >= (1 << 24)) break;
+            iters = (int)std::min<double>((double)iters * 2.0, (double)(1 << 24));
         }
+        for (int rep = 0; rep < 2; ++rep)
+            if (launch() != cudaSuccess) return HSR_ERR_CUDA;
+        cudaEventRecord(e0, 0);
+        for (int rep = 0; rep < 4; ++rep)
+            if (launch() != cudaSuccess) return HSR_ERR_CUDA;
+        cudaEventRecord(e1, 0);
+        if (cudaEventSynchronize(e1) != cudaSuccess) return HSR_ERR_CUDA;
+        cudaEventElapsedTime(&ms, e0, e1);
         const double warps = (double)blocks * 8;
-        const double flops = dmma ? warps * iters * 4.0 * 2.0 * 256 : warps * 32 * iters * 8.0 * 2.0;
+        const double flops = 4.0 * (dmma ? warps * iters * 4.0 * 2.0 * 256 : warps * 32 * iters * 8.0 * 2.0);
         *out = flops / (ms * 1e-3) / 1e9;
         return HSR_OK;
     };

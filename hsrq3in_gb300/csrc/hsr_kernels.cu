@@ -258,43 +258,42 @@ __global__ void __launch_bounds__(32 * kDiagWarps) k_diag(DevProblem P, int J, d
         pert |= solve_1x1(smin, c * vj, s * hsub, yj, phi, is);
         beta = sc_combine(beta, phi, is);
         const double a1 = sc_value(phi, is);
-        if (a1 != 1.0) {
+        if (!is_one(a1)) {
             yjm1 = a1 * yjm1;
             ymax = abs_bits(a1 * from_bits(ymax));
         }
         // y(j-1) (solve-task.c:84-90).
         phi = protect_double_update(fabs(vjm1), fabs(yj), fabs(hdiag), fabs(yj), fabs(yjm1), is);
         const double a2 = sc_value(phi, is);
-        if (a2 != 1.0) {
+        if (!is_one(a2)) {
             yj = a2 * yj;
             yjm1 = a2 * yjm1;
             ymax = abs_bits(a2 * from_bits(ymax));
         }
         beta = sc_combine(beta, phi, is);
-        {
-            const double yc = yj * c, ys = yj * s;
-            yjm1 = fma(ys, hdiag, fma(-yc, vjm1, yjm1));
-        }
+        double yc = yj * c, ys = yj * s;
+        yjm1 = fma(ys, hdiag, fma(-yc, vjm1, yjm1));
         // y(0:j-2) (solve-task.c:92-100).
         phi = protect_double_update(from_bits(vmax), fabs(yj), Hnorm, fabs(yj), from_bits(ymax), is);
         const double a3 = sc_value(phi, is);
-        if (a3 != 1.0) {
+        if (!is_one(a3)) {
             yj = a3 * yj;
             yjm1 = a3 * yjm1;
+            yc = yj * c;
+            ys = yj * s;
         }
         beta = sc_combine(beta, phi, is);
-        const bool scaled = (a1 != 1.0) || (a2 != 1.0) || (a3 != 1.0);
+        const bool scaled = (!is_one(a1)) || (!is_one(a2)) || (!is_one(a3));
         if (scaled) {
             // Rare: the whole-vector scale() also reaches the solved rows j+1 .. b-1.
             for (int i = j + 1 + ((wid - (j + 1)) % kDiagWarps + kDiagWarps) % kDiagWarps; i < b; i += kDiagWarps) {
                 double t = Y(i);
-                if (a1 != 1.0) t = a1 * t;
-                if (a2 != 1.0) t = a2 * t;
-                if (a3 != 1.0) t = a3 * t;
+                if (!is_one(a1)) t = a1 * t;
+                if (!is_one(a2)) t = a2 * t;
+                if (!is_one(a3)) t = a3 * t;
                 Y(i) = t;
             }
         }
-        const double yc = yj * c, ys = yj * s;
         unsigned long long ymx = 0, vmx = 0;
         const int lim = j - 1;
         // Rows i = wid, wid+4, ... < j-1 in batches of 4: loads first, then
@@ -311,9 +310,9 @@ __global__ void __launch_bounds__(32 * kDiagWarps) k_diag(DevProblem P, int J, d
             if (scaled) {
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    if (a1 != 1.0) yy[q] = a1 * yy[q];
-                    if (a2 != 1.0) yy[q] = a2 * yy[q];
-                    if (a3 != 1.0) yy[q] = a3 * yy[q];
+                    if (!is_one(a1)) yy[q] = a1 * yy[q];
+                    if (!is_one(a2)) yy[q] = a2 * yy[q];
+                    if (!is_one(a3)) yy[q] = a3 * yy[q];
                 }
             }
 #pragma unroll
@@ -336,9 +335,9 @@ __global__ void __launch_bounds__(32 * kDiagWarps) k_diag(DevProblem P, int J, d
             const double h = hcol[i];
             double yi = Y(i), vi = V(i);
             if (scaled) {
-                if (a1 != 1.0) yi = a1 * yi;
-                if (a2 != 1.0) yi = a2 * yi;
-                if (a3 != 1.0) yi = a3 * yi;
+                if (!is_one(a1)) yi = a1 * yi;
+                if (!is_one(a2)) yi = a2 * yi;
+                if (!is_one(a3)) yi = a3 * yi;
             }
             yi = fma(ys, h, fma(-yc, vi, yi));
             vi = fma(c, h, s * vi);
@@ -384,7 +383,7 @@ __global__ void __launch_bounds__(32 * kDiagWarps) k_diag(DevProblem P, int J, d
         beta = sc_combine(beta, phi, is);
         const double a = sc_value(phi, is);
         __syncthreads();                                       // last step's rows written
-        if (a != 1.0)
+        if (!is_one(a))
             for (int i = 1 + ((wid - 1) % kDiagWarps + kDiagWarps) % kDiagWarps; i < b; i += kDiagWarps)
                 Y(i) = a * Y(i);
         if (wid == 0) Y(0) = y0;
@@ -497,7 +496,7 @@ __global__ void __launch_bounds__(256) k_part1(DevProblem P, int J) {
     const double alpha = protect_update(fmax(hnrm, fabs(mu)), fabs(ytilde), Yn, is);
     const double a = sc_value(alpha, is);
     unsigned long long mx = 0;
-    if (a != 1.0) {
+    if (!is_one(a)) {
         const double at = a * ytilde;
         for (int i = lane; i < m; i += 32) {
             double yi = fma(-h[i], at, a * y[i]);
@@ -543,7 +542,7 @@ __global__ void __launch_bounds__(256) k_part1(DevProblem P, int J) {
     }
     const double tsc = protect_update(P.Hn[I + (size_t)J * T], z2, Yn, is);
     const double ta = sc_value(tsc, is);
-    if (ta != 1.0) {
+    if (!is_one(ta)) {
         if (!slow) {
             // Materialise Ytilde2 from the fast-path operand.
             for (int q = lane; q < b - 1; q += 32) zs[(size_t)q * Spad] = P.Zs[(size_t)(q + 1) * Spad + k];
@@ -768,10 +767,10 @@ __global__ void __launch_bounds__(32) k_finalize(DevProblem P, double *colnorm, 
                 alpha = act ? sc_upscale(smin, P.beta[(size_t)I * Spad + k], is) : 1.0;
             }
             if (i == 0) {
-                tau1 = alpha * buf[0][lane];
+                tau1 = is_one(alpha) ? buf[0][lane] : alpha * buf[0][lane];
                 continue;
             }
-            const double tau2 = alpha * buf[t][lane];
+            const double tau2 = is_one(alpha) ? buf[t][lane] : alpha * buf[t][lane];
             const double c = act ? P.Cr[(size_t)i * Spad + k] : 0.0;
             const double s = act ? P.Sr[(size_t)i * Spad + k] : 0.0;
             const double out = fma(c, tau1, -(s * tau2));
@@ -843,17 +842,16 @@ cudaError_t launch_gather_cols(double *dst, long long ldd, const double *src, lo
 }
 
 // ------------------------------------------------------- FP64 peak probe
-__global__ void k_probe_dfma(double *out, int iters) {
-    double x[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) x[q] = threadIdx.x * 1e-3 + q;
-    const double a = 0.999999, b = 1e-7;
-    for (int it = 0; it < iters; ++it)
-#pragma unroll
-        for (int q = 0; q < 8; ++q) x[q] = fma(x[q], a, b);
-    double s = 0.0;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) s += x[q];
+// Eight independent FMA chains per thread; a and b are launch arguments so
+// the chains cannot be folded.
+__global__ void k_probe_dfma(double *out, int iters, double a, double b) {
+    double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int it = 0; it < iters; ++it) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    const double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
     if (s == 123456.789) out[0] = s;
 }
 
@@ -876,7 +874,7 @@ __global__ void k_probe_dmma(double *out, int iters) {
 }
 
 cudaError_t launch_probe_dfma(double *out, int blocks, int iters, cudaStream_t st) {
-    k_probe_dfma<<<blocks, 256, 0, st>>>(out, iters);
+    k_probe_dfma<<<blocks, 256, 0, st>>>(out, iters, 0.999, 1e-3);
     return cudaGetLastError();
 }
 cudaError_t launch_probe_dmma(double *out, int blocks, int iters, cudaStream_t st) {
