@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=10000)
+    ap.add_argument("--order", type=int, default=10000, help="n, the order of H")
     ap.add_argument("--nrhs", type=int, default=0, help="0 = all n eigenvalues")
     ap.add_argument("--tlsz", type=int, default=200)
     ap.add_argument("--rhs-tlsz", type=int, default=64)
@@ -298,7 +298,7 @@ def main():
         import torch.distributed as dist
         backend = "nccl" if (args.impl == "gb300" and torch.cuda.is_available()) else "gloo"
         dist.init_process_group(backend=backend)
-    n = args.n
+    n = args.order
     S = args.nrhs or n
     cores = os.cpu_count() or 1
     sample = args.cpu_sample or min(S, 64 * cores)

@@ -17,6 +17,8 @@ HSR_ERR_NOMEM = -2
 HSR_ERR_CUDA = -3
 HSR_ERR_DEVICE = -4
 HSR_ERR_NOT_CONVERGED = 1
+HSR_SCALING_POW2 = 0
+HSR_SCALING_DOUBLE = 1
 
 # Every symbol include/hsrq3in_gb300.h declares.
 EXPORTS = [
@@ -29,7 +31,7 @@ KERNEL_CLASSES = ["setup", "diag", "part1", "gemm", "finalize", "other"]
 
 
 class Options(C.Structure):
-    _fields_ = [("intscale", C.c_int), ("user_rhs", C.c_int),
+    _fields_ = [("scaling", C.c_int), ("user_rhs", C.c_int),
                 ("max_restarts", C.c_int), ("hbm_budget_bytes", C.c_double)]
 
 

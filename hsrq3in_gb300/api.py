@@ -44,11 +44,19 @@ def tiled_inverse_iteration(H: np.ndarray, wr: np.ndarray, tlsz: int, rhs_tlsz: 
     return vr, wr
 
 
+def _scaling(scaling: str) -> int:
+    if scaling not in ("pow2", "double"):
+        raise ValueError("scaling must be 'pow2' or 'double'")
+    return _lib.HSR_SCALING_POW2 if scaling == "pow2" else _lib.HSR_SCALING_DOUBLE
+
+
 def inverse_iteration(H: np.ndarray, wr: np.ndarray, tlsz: int, rhs_tlsz: int = 64,
-                      intscale: bool = False, rhs: np.ndarray | None = None,
+                      scaling: str = "pow2", rhs: np.ndarray | None = None,
                       max_restarts: int = -1, hbm_budget_bytes: float = 0.0):
     """Extended call.  Returns a dict with vr, wr, status, perturbed, scale,
-    tile_scales (num_tiles x nrhs), norm and the library status code."""
+    tile_scales (num_tiles x nrhs), norm and the library status code.
+    scaling: "pow2" (default, base-2 exponents) or "double" (the reference's
+    default build)."""
     lib = _lib.load()
     H = np.asfortranarray(H, dtype=np.float64)
     n = H.shape[0]
@@ -64,7 +72,7 @@ def inverse_iteration(H: np.ndarray, wr: np.ndarray, tlsz: int, rhs_tlsz: int = 
     scale = np.zeros(max(nrhs, 1), dtype=np.float64)
     norm = np.zeros(max(nrhs, 1), dtype=np.float64)
     tiles = np.zeros(max(T * nrhs, 1), dtype=np.float64)
-    opt = _lib.Options(int(bool(intscale)), int(rhs is not None), int(max_restarts), float(hbm_budget_bytes))
+    opt = _lib.Options(_scaling(scaling), int(rhs is not None), int(max_restarts), float(hbm_budget_bytes))
     info = _lib.ColumnInfo(_ptr(status, C.c_int), _ptr(pert, C.c_ubyte), _ptr(scale, C.c_double),
                            _ptr(tiles, C.c_double), _ptr(norm, C.c_double))
     rc = lib.hsr_inverse_iteration_ex(n, H.ctypes.data, H.shape[0], nrhs, wr.ctypes.data, int(tlsz),
@@ -76,7 +84,7 @@ def inverse_iteration(H: np.ndarray, wr: np.ndarray, tlsz: int, rhs_tlsz: int = 
                 rc=rc, launches=lib.hsr_last_launch_count())
 
 
-def inverse_iteration_device(dH, dwr, dvr, tlsz: int, stream=None, intscale: bool = False,
+def inverse_iteration_device(dH, dwr, dvr, tlsz: int, stream=None, scaling: str = "pow2",
                              user_rhs: bool = False, d_status=None, d_scale=None) -> int:
     """Device-resident call on torch tensors (column-major views: pass
     tensors whose .T is contiguous, i.e. created as (cols, rows) and
@@ -86,7 +94,7 @@ def inverse_iteration_device(dH, dwr, dvr, tlsz: int, stream=None, intscale: boo
     ldh = dH.stride(1)
     ldv = dvr.stride(1)
     nrhs = dwr.shape[0]
-    opt = _lib.Options(int(bool(intscale)), int(bool(user_rhs)), -1, 0.0)
+    opt = _lib.Options(_scaling(scaling), int(bool(user_rhs)), -1, 0.0)
     st = None if stream is None else C.c_void_p(stream.cuda_stream)
     rc = lib.hsr_inverse_iteration_device(n, dH.data_ptr(), ldh, nrhs, dwr.data_ptr(), int(tlsz),
                                           dvr.data_ptr(), ldv, C.byref(opt), st,

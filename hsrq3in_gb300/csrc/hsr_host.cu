@@ -324,7 +324,7 @@ int solve_device(int n, const double *dH, long long ldh, int S, double *dwr, int
     s.n = n;
     s.tlsz = tlsz;
     s.T = (n + tlsz - 1) / tlsz;
-    s.is = o.intscale ? 1 : 0;
+    s.is = o.scaling == HSR_SCALING_DOUBLE ? 0 : 1;
     partition(n, s.T, tlsz, s.fr);
     s.H = dH;
     s.ldh = ldh;

@@ -91,6 +91,33 @@ def stress(n: int, seed: int, clusters: int = 50, width: float = 1e-13,
     return _hessenberg_similarity(T, rng), lam
 
 
+def block_scaled(n: int, b: int, seed: int, far: float = 1e250, diag: float = 1e-200,
+                 sub: float = 1e-3):
+    """Adversarial upper-Hessenberg input for the overflow-protection branches
+    of the tile update: entries more than b columns right of the diagonal
+    scaled by `far`, a nearly singular diagonal of magnitude `diag`, and a
+    constant subdiagonal `sub`.  Returns (H, shifts) with shifts near 0."""
+    rng = np.random.default_rng(seed)
+    T = np.triu(rng.standard_normal((n, n)))
+    I, J = np.indices((n, n))
+    T = np.where(J - I > b, T * far, T)
+    T[np.diag_indices(n)] = rng.uniform(0.5, 1.0, n) * diag * np.sign(rng.standard_normal(n))
+    T[np.arange(1, n), np.arange(n - 1)] = sub
+    H = np.asfortranarray(np.triu(T, -1))
+    return H, np.array([0.0, 0.7 * diag, -0.6 * diag, 1e-300])
+
+
+def reduced_triangular(n: int, seed: int, sub: float = 0.0):
+    """Nearly reduced input: upper triangular with a zero diagonal (repeated
+    zero eigenvalue) and subdiagonal `sub`; shifts 0.  Every 1x1 solve is
+    perturbed and the division rescales fire."""
+    rng = np.random.default_rng(seed)
+    T = np.triu(rng.standard_normal((n, n)))
+    T[np.diag_indices(n)] = 0.0
+    T[np.arange(1, n), np.arange(n - 1)] = sub
+    return np.asfortranarray(T), np.zeros(8)
+
+
 def perturbed_shifts(lam: np.ndarray, seed: int, rel: float = 1e-12) -> np.ndarray:
     """lambda_i (1 + rel * N(0,1))."""
     rng = np.random.default_rng(seed)

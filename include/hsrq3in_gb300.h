@@ -51,9 +51,23 @@ void tiled_inverse_iteration(int n, const double *H, int ldH, int nrhs,
                              int ldvr);
 
 /* ---------------------------------------------------- extended host call */
+/* Representation of the overflow-protection scaling factors
+ * (robust.c:24-121, utils.h:17-21). */
+enum {
+    HSR_SCALING_POW2 = 0,   /* default: exact powers of two, kept as base-2 exponents
+                               (the reference's -DINTSCALING build).  Scale factors
+                               cannot underflow, so heavily rescaled columns stay
+                               finite. */
+    HSR_SCALING_DOUBLE = 1  /* the reference's default build: factors such as 0.5/x
+                               kept as doubles; products of many of them underflow
+                               to 0 and give NaN, exactly as the reference does.   */
+};
+/* On every input where no protection decision fires (all unreduced Hessenberg
+ * inputs of the benchmark configurations) both representations give
+ * bit-identical results. */
+
 typedef struct hsr_options {
-    int intscale;      /* 0: double scaling factors (reference default build);
-                          1: base-2 exponents (reference -DINTSCALING build)   */
+    int scaling;       /* HSR_SCALING_POW2 (0, default) or HSR_SCALING_DOUBLE    */
     int user_rhs;      /* 0: eps3 start vectors (inverse_iteration.c:19-34);
                           1: vr holds caller right-hand sides on entry, one
                              solve, no restart (shifted_Hessenberg_solve.h:26) */
@@ -66,7 +80,8 @@ typedef struct hsr_options {
 typedef struct hsr_column_info {
     int *status;            /* 1 converged, 0 not (vrnorms(k,0), shifted_Hessenberg_solve.c:263-273) */
     unsigned char *perturbed; /* 1 if a 1x1 solve was lifted to smin (robust.c:432-435) */
-    double *scale;          /* reconciled scaling factor smin (robust.c:58-82) */
+    double *scale;          /* reconciled scaling factor smin (robust.c:58-82); a base-2
+                               exponent under HSR_SCALING_POW2 */
     double *tile_scales;    /* optional [num_tiles x nrhs] per-tile scaling factors
                                before reconciliation (shifted_Hessenberg_solve.c:105-123) */
     double *norm;           /* 2-norm before normalisation (shifted_Hessenberg_solve.c:229-260) */

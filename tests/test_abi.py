@@ -1,0 +1,72 @@
+"""The C ABI library: it loads and exports every function the header
+declares; argument checking needs no GPU.  No compute calls here."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "hsrq3in_gb300.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    src = "\n".join(ln for ln in src.splitlines() if not ln.lstrip().startswith("#"))
+    return sorted(set(re.findall(r"\b(\w+)\s*\([^;{]*\)\s*;", src)) - {"sizeof"})
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from hsrq3in_gb300 import build, _lib
+    build.build()
+    return _lib.load()
+
+
+def test_header_declares_drop_in_signature():
+    src = open(HEADER).read()
+    assert re.search(r"void\s+tiled_inverse_iteration\s*\(\s*int n,\s*const double \*H,\s*int ldH,\s*int nrhs,"
+                     r"\s*double \*wr,\s*int tlsz,\s*int rhs_tlsz,\s*double \*vr,\s*int ldvr\)", src)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from hsrq3in_gb300 import _lib
+    names = declared_functions()
+    assert "tiled_inverse_iteration" in names
+    for nm in names:
+        assert hasattr(lib, nm), nm
+    assert set(names) == set(_lib.EXPORTS)
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.lib_path()], capture_output=True, text=True).stdout
+    for nm in names:
+        assert re.search(r"\bT %s\b" % nm, out), nm
+
+
+def test_sm103a_code_only(lib):
+    """The library carries sm_103a code (cuobjdump lists the ELF targets; no
+    disassembly is read)."""
+    from hsrq3in_gb300 import _lib
+    r = subprocess.run(["cuobjdump", "--list-elf", _lib.lib_path()], capture_output=True, text=True)
+    assert "sm_103a" in r.stdout
+    assert "sm_100" not in r.stdout.replace("sm_103a", "")
+
+
+def test_argument_errors_without_gpu(lib):
+    from hsrq3in_gb300 import _lib
+    wr = (C.c_double * 4)()
+    vr = (C.c_double * 16)()
+    H = (C.c_double * 16)()
+    cases = [(0, 4, 4, 4), (4, 3, 4, 4), (4, 4, 6, 4), (4, 4, 4, 3)]   # n, ldH, tlsz, ldvr
+    for n, ldH, tlsz, ldvr in cases:
+        lib.tiled_inverse_iteration(n, C.cast(H, C.c_void_p), ldH, 4, C.cast(wr, C.c_void_p), tlsz, 4,
+                                    C.cast(vr, C.c_void_p), ldvr)
+        assert lib.hsr_last_status() == _lib.HSR_ERR_ARG
+    assert lib.hsr_status_string(_lib.HSR_ERR_ARG) == b"invalid argument"
+    opt = _lib.Options(0, 0, -1, 0.0)
+    assert lib.hsr_inverse_iteration_ex(4, C.cast(H, C.c_void_p), 4, 4, C.cast(wr, C.c_void_p), 4, 0,
+                                        C.cast(vr, C.c_void_p), 4, C.byref(opt), None) == _lib.HSR_ERR_ARG
+
+
+def test_version_string(lib):
+    assert b"sm_103a" in lib.hsr_version()
