@@ -26,7 +26,10 @@ EXPORTS = [
     "hsr_inverse_iteration_ex", "hsr_inverse_iteration_device",
     "hsr_last_launch_count", "hsr_set_kernel_timing", "hsr_last_kernel_times",
     "hsr_release_workspace", "hsr_probe_fp64_peak", "hsr_version",
+    "hsr_inverse_iteration_noalloc",
 ]
+NOALLOC_MAX_N = 256
+NOALLOC_MAX_NRHS = 256
 KERNEL_CLASSES = ["setup", "diag", "part1", "gemm", "finalize", "other"]
 
 
@@ -84,5 +87,9 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     lib.hsr_probe_fp64_peak.restype = C.c_int
     lib.hsr_probe_fp64_peak.argtypes = [C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.hsr_version.restype = C.c_char_p
+    lib.hsr_inverse_iteration_noalloc.restype = C.c_int
+    lib.hsr_inverse_iteration_noalloc.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                                  C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                                  C.c_void_p]
     _LIB = lib
     return lib

@@ -121,6 +121,30 @@ int hsr_last_kernel_times(double *ms, long *launches, double *gemm_fma);
 /* Release cached device workspaces of this thread. */
 void hsr_release_workspace(void);
 
+/* ------------------------------------------- no-allocation device call */
+/* No counterpart in the reference.  For callers that may not allocate device
+ * memory while they run -- a serving process whose device memory is owned by
+ * a caching allocator or a fixed pool (where a cudaMalloc would fail or
+ * synchronise the device), or a plug-in host that forbids its plug-ins to
+ * allocate.  Same computation and results as hsr_inverse_iteration_device with
+ * default options (eps3 start vectors, restarts), on device pointers, enqueued
+ * on `stream`; every other buffer comes from one file-scope __device__ array
+ * of HSR_NOALLOC_SCRATCH_BYTES that each GPU loading the library keeps until
+ * the process exits.  Calls no cudaMalloc/cudaFree and allocates no host
+ * memory.  Limits: n <= HSR_NOALLOC_MAX_N, nrhs <= HSR_NOALLOC_MAX_NRHS, and
+ * the workspace of (n, nrhs, tlsz) must fit the array; anything larger returns
+ * HSR_ERR_ARG before any work is enqueued.  The array is shared by all calls:
+ * calls that overlap on the GPU race and must be serialised by the caller.
+ * The first call on a device looks up the array's address on that device;
+ * make that first call before any stream capture.  `status` (host, optional,
+ * [nrhs]) receives 1 for converged columns. */
+#define HSR_NOALLOC_MAX_N 256
+#define HSR_NOALLOC_MAX_NRHS 256
+#define HSR_NOALLOC_SCRATCH_BYTES (8u << 20)
+int hsr_inverse_iteration_noalloc(int n, const double *dH, int lddH, int nrhs,
+                                  double *dwr, int tlsz, double *dvr, int lddvr,
+                                  int scaling, void *stream, int *status);
+
 /* ----------------------------------------------------------- diagnostics */
 /* Measured FP64 throughput of this GPU (GFLOP/s): a DFMA stream and a DMMA
  * (mma.sync m8n8k4 f64) stream, each timed with CUDA events over `ms_target`
