@@ -42,10 +42,12 @@ sys.path.insert(0, HERE)
 
 METRIC = "FP64 eigenvectors/s at n=10k"
 UNIT = "eigenvectors/s"
-# DRAM bytes per GEMM launch, averaged over the launches of the n=4096,
-# S=4096, tlsz=200 capture in profiles/k_gemm_n4096.md, scaled to this
-# workload by the algorithmic FMAs per launch (traffic grows with them).
-GEMM_DRAM_BYTES_PER_FMA = None
+# DRAM bytes per algorithmic FMA of k_gemm, from one ncu capture of the
+# n=4096, S=4096, tlsz=200 case (stage 10 rest launch: 183.61 MB of
+# dram__bytes_read+write for 1696*399*4096 FMAs; profiles/k_gemm_n4096.md).
+# Traffic and FMAs both grow with rows x shifts, so the ratio scales the
+# capture to the launches of this workload.
+GEMM_DRAM_BYTES_PER_FMA = 183.609344e6 / (1696 * 399 * 4096)
 
 
 def parse():
@@ -241,6 +243,7 @@ def run_gpu(args, H, wr, rank, world):
     roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": (achieved / peak) if achieved else None,
             "traffic": (GEMM_DRAM_BYTES_PER_FMA * gemm_fma / max(kl[3], 1)) if GEMM_DRAM_BYTES_PER_FMA else None,
+            "traffic_note": "DRAM bytes per launch, scaled from the n=4096 ncu capture by algorithmic FMAs",
             "kernel": "k_gemm (crossover propagation + tile update, DFMA)",
             "peak_source": "FP64 DFMA stream measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
             "algorithmic_flops_per_launch": 2.0 * gemm_fma / max(kl[3], 1),
