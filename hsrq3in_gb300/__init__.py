@@ -5,9 +5,10 @@ The product is the C-ABI shared library ``libhsrq3in_gb300.so`` declared in
 (``_lib.py``), wraps it for numpy and torch callers (``api.py``), and ships
 the seeded workload generators (``generators.py``).
 """
-from .api import (HsrError, fp64_peak, inverse_iteration, inverse_iteration_device,  # noqa: F401
-                  last_launch_count, tiled_inverse_iteration)
+from .api import (BatchPlan, HsrError, Server, autotune_batch, fp64_peak,  # noqa: F401
+                  inverse_iteration, inverse_iteration_device, last_launch_count,
+                  tiled_inverse_iteration)
 from ._lib import lib_path, load  # noqa: F401
 
-__all__ = ["HsrError", "fp64_peak", "inverse_iteration", "inverse_iteration_device",
+__all__ = ["BatchPlan", "Server", "autotune_batch", "HsrError", "fp64_peak", "inverse_iteration", "inverse_iteration_device",
            "last_launch_count", "tiled_inverse_iteration", "lib_path", "load"]

@@ -27,6 +27,9 @@ EXPORTS = [
     "hsr_last_launch_count", "hsr_set_kernel_timing", "hsr_last_kernel_times",
     "hsr_release_workspace", "hsr_probe_fp64_peak", "hsr_version",
     "hsr_inverse_iteration_noalloc",
+    "hsr_batch_plan_create", "hsr_batch_plan_execute", "hsr_batch_plan_info", "hsr_batch_plan_destroy",
+    "hsr_autotune_tlsz", "hsr_autotune_batch",
+    "hsr_server_create", "hsr_server_replay", "hsr_server_destroy",
 ]
 NOALLOC_MAX_N = 256
 NOALLOC_MAX_NRHS = 256
@@ -42,6 +45,26 @@ class ColumnInfo(C.Structure):
     _fields_ = [("status", C.POINTER(C.c_int)), ("perturbed", C.POINTER(C.c_ubyte)),
                 ("scale", C.POINTER(C.c_double)), ("tile_scales", C.POINTER(C.c_double)),
                 ("norm", C.POINTER(C.c_double))]
+
+
+class BatchProblem(C.Structure):
+    _fields_ = [("n", C.c_int), ("dH", C.c_void_p), ("lddH", C.c_int), ("nrhs", C.c_int),
+                ("dwr", C.c_void_p), ("dvr", C.c_void_p), ("lddvr", C.c_int)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_double), ("tlsz", C.c_int), ("max_active", C.c_int),
+                ("scaling", C.c_int)]
+
+
+class Request(C.Structure):
+    _fields_ = [("n", C.c_int), ("H", C.c_void_p), ("ldH", C.c_int), ("nrhs", C.c_int),
+                ("wr", C.c_void_p), ("vr", C.c_void_p), ("ldvr", C.c_int), ("arrival_s", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("wall_s", C.c_double), ("ticks", C.c_long), ("launches", C.c_long),
+                ("max_active", C.c_int), ("peak_bytes", C.c_double)]
 
 
 _LIB = None
@@ -87,6 +110,27 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     lib.hsr_probe_fp64_peak.restype = C.c_int
     lib.hsr_probe_fp64_peak.argtypes = [C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.hsr_version.restype = C.c_char_p
+    lib.hsr_batch_plan_create.restype = C.c_int
+    lib.hsr_batch_plan_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.POINTER(BatchProblem), C.c_int,
+                                          C.POINTER(Options), C.c_void_p]
+    lib.hsr_batch_plan_execute.restype = C.c_int
+    lib.hsr_batch_plan_execute.argtypes = [C.c_void_p, C.c_void_p]
+    lib.hsr_batch_plan_info.restype = C.c_int
+    lib.hsr_batch_plan_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_long)]
+    lib.hsr_batch_plan_destroy.restype = None
+    lib.hsr_batch_plan_destroy.argtypes = [C.c_void_p]
+    lib.hsr_autotune_tlsz.restype = C.c_int
+    lib.hsr_autotune_tlsz.argtypes = [C.c_int, C.c_int]
+    lib.hsr_autotune_batch.restype = C.c_int
+    lib.hsr_autotune_batch.argtypes = [C.c_int, C.POINTER(BatchProblem), C.POINTER(C.c_int), C.c_int,
+                                       C.POINTER(C.c_double), C.c_void_p]
+    lib.hsr_server_create.restype = C.c_int
+    lib.hsr_server_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(ServerConfig)]
+    lib.hsr_server_replay.restype = C.c_int
+    lib.hsr_server_replay.argtypes = [C.c_void_p, C.c_int, C.POINTER(Request), C.POINTER(C.c_double),
+                                      C.POINTER(C.c_int), C.POINTER(ServerStats)]
+    lib.hsr_server_destroy.restype = None
+    lib.hsr_server_destroy.argtypes = [C.c_void_p]
     lib.hsr_inverse_iteration_noalloc.restype = C.c_int
     lib.hsr_inverse_iteration_noalloc.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
                                                   C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,

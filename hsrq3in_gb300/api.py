@@ -115,3 +115,118 @@ def fp64_peak(ms_target: float = 50.0):
 
 def last_launch_count() -> int:
     return int(_lib.load().hsr_last_launch_count())
+
+
+# ----------------------------------------------------------------- batched
+class BatchPlan:
+    """Many independent problems solved together (hsr_batch_plan_*).
+
+    problems: list of (dH, dwr, dvr) torch tensors on the device, where dH and
+    dvr are column-major views (tensors of shape (cols, ld) holding columns as
+    rows).  tlsz=0 uses the autotuned tile size."""
+
+    def __init__(self, problems, tlsz: int = 0, scaling: str = "pow2", stream=None):
+        lib = _lib.load()
+        self._lib = lib
+        self._keep = problems
+        arr = (_lib.BatchProblem * max(len(problems), 1))()
+        for i, (dH, dwr, dvr) in enumerate(problems):
+            n = dH.shape[0]
+            arr[i] = _lib.BatchProblem(n, dH.data_ptr(), dH.stride(0), dwr.numel(), dwr.data_ptr(),
+                                       dvr.data_ptr(), dvr.stride(0))
+        self._arr = arr
+        self._stream = stream
+        opt = _lib.Options(_scaling(scaling), 0, -1, 0.0)
+        h = C.c_void_p()
+        rc = lib.hsr_batch_plan_create(C.byref(h), len(problems), arr, int(tlsz), C.byref(opt),
+                                       None if stream is None else C.c_void_p(stream.cuda_stream))
+        if rc != 0:
+            raise HsrError(rc)
+        self._h = h
+
+    def execute(self) -> int:
+        rc = self._lib.hsr_batch_plan_execute(self._h, None if self._stream is None
+                                              else C.c_void_p(self._stream.cuda_stream))
+        if rc < 0:
+            raise HsrError(rc)
+        return rc
+
+    def info(self):
+        t, k, n = C.c_int(), C.c_int(), C.c_long()
+        self._lib.hsr_batch_plan_info(self._h, C.byref(t), C.byref(k), C.byref(n))
+        return dict(tlsz=t.value, ticks=k.value, launches=n.value)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.hsr_batch_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def autotune_batch(problems, candidates=(32, 48, 64, 96, 128), stream=None):
+    """Time the batch for each candidate tile size; records and returns the
+    fastest, with the per-candidate times in ms."""
+    lib = _lib.load()
+    arr = (_lib.BatchProblem * len(problems))()
+    for i, (dH, dwr, dvr) in enumerate(problems):
+        arr[i] = _lib.BatchProblem(dH.shape[0], dH.data_ptr(), dH.stride(0), dwr.numel(), dwr.data_ptr(),
+                                   dvr.data_ptr(), dvr.stride(0))
+    cand = (C.c_int * len(candidates))(*candidates)
+    ms = (C.c_double * len(candidates))()
+    best = lib.hsr_autotune_batch(len(problems), arr, cand, len(candidates), ms,
+                                  None if stream is None else C.c_void_p(stream.cuda_stream))
+    if best < 0:
+        raise HsrError(best)
+    return best, list(ms)
+
+
+# ----------------------------------------------------------------- served
+class Server:
+    """The request loop with continuous batching (hsr_server_*)."""
+
+    def __init__(self, hbm_budget_bytes: float = 0.0, tlsz: int = 0, max_active: int = 0,
+                 scaling: str = "pow2"):
+        lib = _lib.load()
+        self._lib = lib
+        cfg = _lib.ServerConfig(float(hbm_budget_bytes), int(tlsz), int(max_active), _scaling(scaling))
+        h = C.c_void_p()
+        rc = lib.hsr_server_create(C.byref(h), C.byref(cfg))
+        if rc != 0:
+            raise HsrError(rc)
+        self._h = h
+
+    def replay(self, requests):
+        """requests: list of dict(H=host Fortran array, wr=host array (in/out),
+        vr=host Fortran array (out), arrival_s=float).  Host arrays should be
+        pinned for copy/compute overlap.  Returns (latencies_s, statuses, stats)."""
+        n = len(requests)
+        arr = (_lib.Request * max(n, 1))()
+        for i, r in enumerate(requests):
+            H, wr, vr = r["H"], r["wr"], r["vr"]
+            arr[i] = _lib.Request(H.shape[0], H.ctypes.data, H.shape[0] if H.flags.f_contiguous else H.strides[1] // 8,
+                                  wr.shape[0], wr.ctypes.data, vr.ctypes.data, vr.shape[0], float(r["arrival_s"]))
+        lat = (C.c_double * max(n, 1))()
+        st = (C.c_int * max(n, 1))()
+        stats = _lib.ServerStats()
+        rc = self._lib.hsr_server_replay(self._h, n, arr, lat, st, C.byref(stats))
+        if rc < 0:
+            raise HsrError(rc)
+        return (list(lat)[:n], list(st)[:n],
+                dict(wall_s=stats.wall_s, ticks=stats.ticks, launches=stats.launches,
+                     max_active=stats.max_active, peak_bytes=stats.peak_bytes))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.hsr_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

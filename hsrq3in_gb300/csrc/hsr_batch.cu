@@ -1,0 +1,852 @@
+// hsr_batch.cu -- batched and served solves: many problems, one tick at a time.
+//
+// A problem with T row tiles needs T stages (J = T-1 .. 0).  Problems start
+// at their own tick and each tick advances every active problem by one stage:
+// one batched launch per phase (diagonal, part 1, GEMM, finalize, normalize)
+// covers the work items of all problems, so thousands of small problems fill
+// the GPU together.  Each work item runs the single-problem kernel body, so
+// every column computes exactly what it computes when its problem is solved
+// alone with the same tile size.
+//
+//   batched (hsr_batch_plan_*): all problems start at tick 0; the whole tick
+//     sequence, with its work lists already on the device, is captured once
+//     into a CUDA graph and replayed by each execute.
+//   served (hsr_server_*): a request loop admits requests in arrival order
+//     while their footprint fits a device pool (HBM budget), copies them in,
+//     runs ticks over the admitted set, and copies finished results out;
+//     requests arriving while others run join at the next tick.
+#include "hsr_common.h"
+#include "hsr_kernels.h"
+#include "../../include/hsrq3in_gb300.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace hsr {
+namespace {
+
+inline size_t up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// ------------------------------------------------------------- layout
+// Device workspace of one problem.  Offsets are relative to the problem's
+// base; every piece starts on a 256-byte boundary.  The pieces that must
+// start at zero (norm accumulators, NaN flags) come first so that one memset
+// clears them.
+struct Layout {
+    int n = 0, S = 0, T = 0, b = 0, Spad = 0;
+    long long ldr = 0;
+    size_t zero_bytes = 0;   // [0, zero_bytes) must be zeroed before setup
+    size_t nbits, nan, fr, R, Cr, Sr, beta, ynorm, W, Zs, vecs, Zslow, slow, pert, colnorm, status, scale;
+    size_t total = 0;
+    void compute(int n_, int S_, int b_) {
+        n = n_;
+        S = S_;
+        b = b_;
+        T = (n + b - 1) / b;
+        Spad = (int)up((size_t)S, 8);
+        ldr = (long long)up((size_t)n, 4);
+        size_t o = 0;
+        auto take = [&](size_t bytes) {
+            o = up(o, 256);
+            const size_t at = o;
+            o += bytes;
+            return at;
+        };
+        const size_t Sp = (size_t)Spad;
+        nbits = take((2 * (size_t)T * T + 2) * 8);
+        nan = take(4 * sizeof(int));
+        zero_bytes = up(o, 256);
+        fr = take((size_t)(T + 1) * sizeof(int));
+        R = take((size_t)ldr * S * 8);
+        Cr = take((size_t)n * Sp * 8);
+        Sr = take((size_t)n * Sp * 8);
+        beta = take((size_t)T * Sp * 8);
+        ynorm = take((size_t)T * Sp * 8);
+        W = take((size_t)b * Sp * 8);
+        Zs = take((size_t)b * Sp * 8);
+        vecs = take(4 * Sp * 8);
+        Zslow = take((size_t)T * b * Sp * 8);
+        slow = take((size_t)T * Sp);
+        pert = take(Sp);
+        colnorm = take(Sp * 8);
+        status = take(Sp * sizeof(int));
+        scale = take(Sp * 8);
+        total = up(o, 256);
+    }
+};
+
+void partition_rows(int n, int T, int b, std::vector<int> &fr) {
+    fr.assign(T + 1, 0);
+    for (int i = 1; i < T; ++i) fr[i] = n - (T - i) * b;   // partition.c:7-17
+    fr[0] = 0;
+    fr[T] = n;
+}
+
+double smlnum_for(int n) {
+    const double eps = DBL_EPSILON / 2;
+    return std::fmax(2 * DBL_MIN, DBL_MIN * ((double)n / eps));
+}
+
+// DevProblem of one problem whose workspace starts at `base`.
+DevProblem make_problem(const Layout &L, char *base, const double *H, long long ldh, double *wr, double *X,
+                        long long ldx, int is, int *err) {
+    DevProblem P{};
+    P.n = L.n;
+    P.T = L.T;
+    P.S = L.S;
+    P.Spad = L.Spad;
+    P.tlsz = L.b;
+    P.fr = reinterpret_cast<const int *>(base + L.fr);
+    P.H = H;
+    P.ldh = ldh;
+    P.wr = wr;
+    P.X = X;
+    P.ldx = ldx;
+    P.R = reinterpret_cast<double *>(base + L.R);
+    P.ldr = L.ldr;
+    P.Cr = reinterpret_cast<double *>(base + L.Cr);
+    P.Sr = reinterpret_cast<double *>(base + L.Sr);
+    P.beta = reinterpret_cast<double *>(base + L.beta);
+    P.ynorm = reinterpret_cast<double *>(base + L.ynorm);
+    P.nbits = reinterpret_cast<unsigned long long *>(base + L.nbits);
+    P.Hn = reinterpret_cast<const double *>(P.nbits);
+    P.hn = reinterpret_cast<const double *>(P.nbits + (size_t)L.T * L.T);
+    P.W = reinterpret_cast<double *>(base + L.W);
+    P.Zs = reinterpret_cast<double *>(base + L.Zs);
+    double *v = reinterpret_cast<double *>(base + L.vecs);
+    P.pi = v;
+    P.ytil = v + L.Spad;
+    P.z2n = v + 2 * (size_t)L.Spad;
+    P.zlast = v + 3 * (size_t)L.Spad;
+    P.Zslow = reinterpret_cast<double *>(base + L.Zslow);
+    P.slow = reinterpret_cast<unsigned char *>(base + L.slow);
+    P.pert = reinterpret_cast<unsigned char *>(base + L.pert);
+    P.smlnum = smlnum_for(L.n);
+    P.is = is;
+    P.err = err;
+    P.colnorm = reinterpret_cast<double *>(base + L.colnorm);
+    P.status = reinterpret_cast<int *>(base + L.status);
+    P.scale = reinterpret_cast<double *>(base + L.scale);
+    P.nanflag = reinterpret_cast<int *>(base + L.nan);
+    return P;
+}
+
+bool make_maps(CUtensorMap *m, const Layout &L, const double *H, long long ldh, char *base) {
+    return encode_tensor_map(&m[0], H, (unsigned long long)L.n, (unsigned long long)L.n,
+                             (unsigned long long)ldh, kGemmBM, kGemmKC) &&
+           encode_tensor_map(&m[1], reinterpret_cast<const double *>(base + L.W), (unsigned long long)L.Spad,
+                             (unsigned long long)L.b, (unsigned long long)L.Spad, kGemmBN, kGemmKC) &&
+           encode_tensor_map(&m[2], reinterpret_cast<const double *>(base + L.Zs), (unsigned long long)L.Spad,
+                             (unsigned long long)L.b, (unsigned long long)L.Spad, kGemmBN, kGemmKC);
+}
+
+// ----------------------------------------------------------- work lists
+enum Phase { phNorms = 0, phInit, phDiag, phPart1, phGemm, phFinal, phNormalize, phCount };
+
+struct TickLists {
+    std::vector<BatchItem> v[phCount];
+    void clear() {
+        for (auto &x : v) x.clear();
+    }
+    size_t size() const {
+        size_t s = 0;
+        for (auto &x : v) s += x.size();
+        return s;
+    }
+};
+
+void add_setup(TickLists &tl, int slot, const Layout &L, const std::vector<int> &fr) {
+    const int rb = (L.n + kNormRows - 1) / kNormRows;
+    for (int r = 0; r < rb; ++r) {
+        tl.v[phNorms].push_back(make_int4(slot, -1, r, 0));
+        const int row0 = r * kNormRows;
+        int I0 = L.T - 1 - (L.n - 1 - row0) / L.b;
+        if (I0 < 0) I0 = 0;
+        for (int J = I0; J < L.T; ++J) tl.v[phNorms].push_back(make_int4(slot, J, r, 0));
+    }
+    for (int k = 0; k < L.S; ++k) tl.v[phInit].push_back(make_int4(slot, 0, k, 0));
+    (void)fr;
+}
+
+void add_stage(TickLists &tl, int slot, const Layout &L, const std::vector<int> &fr, int J) {
+    const int sb32 = (L.S + 31) / 32;
+    for (int x = 0; x < sb32; ++x) tl.v[phDiag].push_back(make_int4(slot, J, x, 0));
+    if (J >= 1) {
+        const int sb8 = (L.S + 7) / 8;
+        for (int I = 0; I < J; ++I)
+            for (int x = 0; x < sb8; ++x) tl.v[phPart1].push_back(make_int4(slot, J, I, x));
+        const int rbs = (fr[J] + kGemmBM - 1) / kGemmBM;
+        const int cbs = (L.S + kGemmBN - 1) / kGemmBN;
+        for (int r = 0; r < rbs; ++r)
+            for (int c = 0; c < cbs; ++c) tl.v[phGemm].push_back(make_int4(slot, J, r, c));
+    } else {
+        for (int x = 0; x < sb32; ++x) tl.v[phFinal].push_back(make_int4(slot, 0, x, 0));
+        const int cb = (L.S + kNormalizeCols - 1) / kNormalizeCols;
+        for (int x = 0; x < cb; ++x) tl.v[phNormalize].push_back(make_int4(slot, 0, x, 0));
+    }
+}
+
+cudaError_t launch_phase(int ph, const DevProblem *probs, const BatchItem *items, int count, int bmax,
+                         const CUtensorMap *maps, cudaStream_t st) {
+    switch (ph) {
+    case phNorms: return launch_norms_b(probs, items, count, st);
+    case phInit: return launch_init_b(probs, items, count, st);
+    case phDiag: return launch_diag_b(probs, items, count, bmax, st);
+    case phPart1: return launch_part1_b(probs, items, count, st);
+    case phGemm: return launch_gemm_b(probs, items, count, maps, st);
+    case phFinal: return launch_finalize_b(probs, items, count, st);
+    case phNormalize: return launch_normalize_b(probs, items, count, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+int validate(const hsr_batch_problem &p, int b) {
+    if (p.n <= 0 || p.lddH < p.n || p.nrhs < 0 || p.lddvr < p.n || !p.dH) return HSR_ERR_ARG;
+    if (p.nrhs > 0 && (!p.dwr || !p.dvr)) return HSR_ERR_ARG;
+    if ((p.lddH & 1) || (reinterpret_cast<uintptr_t>(p.dH) & 15)) return HSR_ERR_ARG;   // TMA source
+    if (b <= 0 || (b % 4) != 0 || b > 384) return HSR_ERR_ARG;
+    return HSR_OK;
+}
+
+// --------------------------------------------------------- autotune table
+std::mutex g_tune_mu;
+std::map<std::pair<int, int>, int> g_tune;   // [n_lo, n_hi] -> tlsz
+
+int default_tlsz(int n_hi) { return n_hi <= 256 ? 32 : 64; }
+
+}  // namespace
+}  // namespace hsr
+
+using namespace hsr;
+
+// ====================================================================== plan
+struct hsr_batch_plan {
+    int nprob = 0, b = 0, is = 1, ticks = 0;
+    long launches = 0;
+    std::vector<hsr_batch_problem> specs;
+    std::vector<Layout> layouts;
+    std::vector<size_t> offsets;
+    char *pool = nullptr;
+    size_t pool_bytes = 0, zero_bytes = 0;   // problem zero regions are laid out first
+    DevProblem *d_probs = nullptr;
+    CUtensorMap *d_maps = nullptr;
+    BatchItem *d_items = nullptr;
+    int *d_err = nullptr;
+    int *d_status = nullptr;                  // statuses of all problems, contiguous
+    std::vector<size_t> status_off;           // first column of each problem in d_status
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~hsr_batch_plan() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (pool) cudaFree(pool);
+        if (d_probs) cudaFree(d_probs);
+        if (d_maps) cudaFree(d_maps);
+        if (d_items) cudaFree(d_items);
+        if (d_err) cudaFree(d_err);
+        if (d_status) cudaFree(d_status);
+    }
+};
+
+namespace {
+#define BP_CK(x)                            \
+    do {                                    \
+        if ((x) != cudaSuccess) {           \
+            delete pl;                      \
+            return HSR_ERR_CUDA;            \
+        }                                   \
+    } while (0)
+}  // namespace
+
+extern "C" int hsr_autotune_tlsz(int n_lo, int n_hi) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    for (auto &kv : g_tune)
+        if (kv.first.first <= n_lo && n_hi <= kv.first.second) return kv.second;
+    return default_tlsz(n_hi);
+}
+
+extern "C" int hsr_batch_plan_create(hsr_batch_plan **out, int nprob, const hsr_batch_problem *probs, int tlsz,
+                                     const hsr_options *opt, void *stream) {
+    if (!out || nprob < 0 || (nprob > 0 && !probs)) return HSR_ERR_ARG;
+    *out = nullptr;
+    int n_lo = 1 << 30, n_hi = 0;
+    for (int i = 0; i < nprob; ++i) {
+        n_lo = std::min(n_lo, probs[i].n);
+        n_hi = std::max(n_hi, probs[i].n);
+    }
+    const int b = tlsz > 0 ? tlsz : hsr_autotune_tlsz(n_lo, n_hi);
+    for (int i = 0; i < nprob; ++i) {
+        const int rc = validate(probs[i], b);
+        if (rc) return rc;
+    }
+    hsr_batch_plan *pl = new hsr_batch_plan();
+    pl->nprob = nprob;
+    pl->b = b;
+    pl->is = (opt && opt->scaling == HSR_SCALING_DOUBLE) ? 0 : 1;
+    pl->specs.assign(probs, probs + nprob);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+
+    // Layout: every problem's zero region first, then the workspaces.
+    pl->layouts.resize(nprob);
+    pl->offsets.resize(nprob);
+    size_t zero_total = 0, ws_total = 0;
+    std::vector<size_t> zoff(nprob);
+    for (int i = 0; i < nprob; ++i) {
+        Layout &L = pl->layouts[i];
+        L.compute(probs[i].n, probs[i].nrhs, b);
+        zoff[i] = zero_total;
+        zero_total += L.zero_bytes;
+        ws_total += L.total - L.zero_bytes;
+    }
+    pl->zero_bytes = zero_total;
+    pl->pool_bytes = zero_total + ws_total + 256;
+    BP_CK(cudaMalloc(&pl->pool, pl->pool_bytes));
+    BP_CK(cudaMalloc(&pl->d_err, 16));
+    size_t ncols = 0;
+    for (int i = 0; i < nprob; ++i) ncols += (size_t)probs[i].nrhs;
+    BP_CK(cudaMalloc(&pl->d_status, sizeof(int) * std::max<size_t>(ncols, 1)));
+    ncols = 0;
+    // Each problem gets a contiguous Layout whose zero region is elsewhere:
+    // carve a virtual base so that base + L.nbits lands in the zero area and
+    // base + L.fr ... in the workspace area.  Easiest: give every problem its
+    // own full Layout in the workspace area and point nbits/nan at the zero
+    // area explicitly.
+    std::vector<DevProblem> hp(nprob);
+    std::vector<CUtensorMap> hm(3 * (size_t)nprob);
+    size_t ws = zero_total;
+    std::vector<std::vector<int>> frs(nprob);
+    for (int i = 0; i < nprob; ++i) {
+        Layout &L = pl->layouts[i];
+        char *base = pl->pool + ws - L.zero_bytes;   // workspace pieces start at L.zero_bytes
+        pl->offsets[i] = ws - L.zero_bytes;
+        ws += L.total - L.zero_bytes;
+        DevProblem P = make_problem(L, base, probs[i].dH, probs[i].lddH, probs[i].dwr, probs[i].dvr,
+                                    probs[i].lddvr, pl->is, pl->d_err);
+        char *zbase = pl->pool + zoff[i];
+        P.nbits = reinterpret_cast<unsigned long long *>(zbase + L.nbits);
+        P.Hn = reinterpret_cast<const double *>(P.nbits);
+        P.hn = reinterpret_cast<const double *>(P.nbits + (size_t)L.T * L.T);
+        P.nanflag = reinterpret_cast<int *>(zbase + L.nan);
+        hp[i] = P;
+        if (!make_maps(&hm[3 * (size_t)i], L, probs[i].dH, probs[i].lddH, base)) {
+            delete pl;
+            return HSR_ERR_CUDA;
+        }
+        partition_rows(L.n, L.T, b, frs[i]);
+        BP_CK(cudaMemcpyAsync(base + L.fr, frs[i].data(), (L.T + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+        P.status = pl->d_status + ncols;
+        hp[i].status = P.status;
+        pl->status_off.push_back(ncols);
+        ncols += (size_t)probs[i].nrhs;
+    }
+    BP_CK(cudaMalloc(&pl->d_probs, sizeof(DevProblem) * std::max(nprob, 1)));
+    BP_CK(cudaMalloc(&pl->d_maps, sizeof(CUtensorMap) * std::max<size_t>(hm.size(), 1)));
+    if (nprob) {
+        BP_CK(cudaMemcpyAsync(pl->d_probs, hp.data(), sizeof(DevProblem) * nprob, cudaMemcpyHostToDevice, st));
+        BP_CK(cudaMemcpyAsync(pl->d_maps, hm.data(), sizeof(CUtensorMap) * hm.size(), cudaMemcpyHostToDevice, st));
+    }
+
+    // Schedule: setup, then ticks; problem i runs stage J = T_i - 1 - t.
+    std::vector<std::pair<int, std::pair<size_t, int>>> seq;   // (phase, (offset, count))
+    std::vector<BatchItem> all;
+    TickLists tl;
+    for (int i = 0; i < nprob; ++i)
+        if (pl->layouts[i].S > 0) add_setup(tl, i, pl->layouts[i], frs[i]);
+    auto flush = [&]() {
+        for (int ph = 0; ph < phCount; ++ph) {
+            if (tl.v[ph].empty()) continue;
+            seq.push_back({ph, {all.size(), (int)tl.v[ph].size()}});
+            all.insert(all.end(), tl.v[ph].begin(), tl.v[ph].end());
+        }
+        tl.clear();
+    };
+    flush();
+    int maxT = 0;
+    for (int i = 0; i < nprob; ++i)
+        if (pl->layouts[i].S > 0) maxT = std::max(maxT, pl->layouts[i].T);
+    for (int t = 0; t < maxT; ++t) {
+        for (int i = 0; i < nprob; ++i) {
+            const Layout &L = pl->layouts[i];
+            if (L.S == 0) continue;
+            const int J = L.T - 1 - t;
+            if (J >= 0) add_stage(tl, i, L, frs[i], J);
+        }
+        flush();
+    }
+    pl->ticks = maxT;
+    BP_CK(cudaMalloc(&pl->d_items, sizeof(BatchItem) * std::max<size_t>(all.size(), 1)));
+    if (!all.empty())
+        BP_CK(cudaMemcpyAsync(pl->d_items, all.data(), sizeof(BatchItem) * all.size(), cudaMemcpyHostToDevice, st));
+    BP_CK(cudaStreamSynchronize(st));
+
+    // Capture: zero the accumulators, then every phase launch in order.
+    cudaStream_t cap = nullptr;
+    BP_CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    // First use sets the kernels' shared-memory attributes outside capture.
+    BP_CK(launch_diag_b(pl->d_probs, pl->d_items, 0, b, cap));
+    bool ok = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) ok = cudaMemsetAsync(pl->pool, 0, std::max<size_t>(zero_total, 1), cap) == cudaSuccess;
+    if (ok) ok = cudaMemsetAsync(pl->d_err, 0, 16, cap) == cudaSuccess;
+    for (auto &e : seq) {
+        if (!ok) break;
+        ok = launch_phase(e.first, pl->d_probs, pl->d_items + e.second.first, e.second.second, b, pl->d_maps, cap) ==
+             cudaSuccess;
+        ++pl->launches;
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (!ok || ce != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        delete pl;
+        return HSR_ERR_CUDA;
+    }
+    pl->graph = g;
+    if (cudaGraphInstantiate(&pl->exec, g, 0) != cudaSuccess) {
+        delete pl;
+        return HSR_ERR_CUDA;
+    }
+    *out = pl;
+    return HSR_OK;
+}
+
+extern "C" int hsr_batch_plan_execute(hsr_batch_plan *pl, void *stream) {
+    if (!pl) return HSR_ERR_ARG;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (cudaGraphLaunch(pl->exec, st) != cudaSuccess) return HSR_ERR_CUDA;
+    // Convergence: status of every column of every problem.
+    int result = HSR_OK;
+    int errw = 0;
+    if (cudaMemcpyAsync(&errw, pl->d_err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return HSR_ERR_CUDA;
+    size_t ncols = 0;
+    for (int i = 0; i < pl->nprob; ++i) ncols += (size_t)pl->specs[i].nrhs;
+    std::vector<int> stv(std::max<size_t>(ncols, 1));
+    if (cudaStreamSynchronize(st) != cudaSuccess) return HSR_ERR_CUDA;
+    if (ncols && cudaMemcpy(stv.data(), pl->d_status, ncols * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return HSR_ERR_CUDA;
+    if (errw) return HSR_ERR_DEVICE;
+    // Problems with columns that did not converge: solved again alone, which
+    // runs the same first pass and then the restart rounds.
+    for (int i = 0; i < pl->nprob; ++i) {
+        bool all = true;
+        for (int k = 0; k < pl->specs[i].nrhs; ++k) all = all && stv[pl->status_off[i] + (size_t)k];
+        if (all) continue;
+        const hsr_batch_problem &p = pl->specs[i];
+        hsr_options o{};
+        o.scaling = pl->is ? HSR_SCALING_POW2 : HSR_SCALING_DOUBLE;
+        o.max_restarts = -1;
+        const int rc = hsr_inverse_iteration_device(p.n, p.dH, p.lddH, p.nrhs, p.dwr, pl->b, p.dvr, p.lddvr, &o,
+                                                    stream, nullptr, nullptr);
+        if (rc < 0) return rc;
+        if (rc == HSR_ERR_NOT_CONVERGED) result = HSR_ERR_NOT_CONVERGED;
+    }
+    return result;
+}
+
+extern "C" int hsr_batch_plan_info(const hsr_batch_plan *pl, int *tlsz, int *ticks, long *launches) {
+    if (!pl) return HSR_ERR_ARG;
+    if (tlsz) *tlsz = pl->b;
+    if (ticks) *ticks = pl->ticks;
+    if (launches) *launches = pl->launches;
+    return HSR_OK;
+}
+
+extern "C" void hsr_batch_plan_destroy(hsr_batch_plan *pl) { delete pl; }
+
+extern "C" int hsr_autotune_batch(int nprob, const hsr_batch_problem *probs, const int *cand, int ncand,
+                                  double *ms_out, void *stream) {
+    if (nprob <= 0 || !probs || !cand || ncand <= 0) return HSR_ERR_ARG;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int n_lo = 1 << 30, n_hi = 0;
+    for (int i = 0; i < nprob; ++i) {
+        n_lo = std::min(n_lo, probs[i].n);
+        n_hi = std::max(n_hi, probs[i].n);
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int best = -1;
+    double best_ms = 1e300;
+    for (int c = 0; c < ncand; ++c) {
+        hsr_batch_plan *pl = nullptr;
+        double ms = 1e300;
+        if (hsr_batch_plan_create(&pl, nprob, probs, cand[c], nullptr, stream) == HSR_OK) {
+            hsr_batch_plan_execute(pl, stream);   // warm-up
+            cudaEventRecord(e0, st);
+            const int reps = 2;
+            for (int r = 0; r < reps; ++r) cudaGraphLaunch(pl->exec, st);
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            float t = 0.f;
+            cudaEventElapsedTime(&t, e0, e1);
+            ms = t / reps;
+            hsr_batch_plan_destroy(pl);
+        }
+        if (ms_out) ms_out[c] = ms;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = cand[c];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best > 0) {
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        g_tune[{n_lo, n_hi}] = best;
+    }
+    return best > 0 ? best : HSR_ERR_CUDA;
+}
+
+// ==================================================================== server
+namespace hsr {
+namespace {
+
+// First-fit allocator over one device pool, with coalescing frees.
+struct PoolAlloc {
+    size_t cap = 0, used = 0, peak = 0;
+    std::map<size_t, size_t> free_;   // offset -> size
+    void reset(size_t c) {
+        cap = c;
+        used = peak = 0;
+        free_.clear();
+        free_[0] = c;
+    }
+    bool alloc(size_t bytes, size_t &off) {
+        bytes = up(bytes, 256);
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= bytes) {
+                off = it->first;
+                const size_t rest = it->second - bytes;
+                free_.erase(it);
+                if (rest) free_[off + bytes] = rest;
+                used += bytes;
+                peak = std::max(peak, used);
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(size_t off, size_t bytes) {
+        bytes = up(bytes, 256);
+        used -= bytes;
+        auto it = free_.emplace(off, bytes).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+};
+
+struct ActiveReq {
+    int req = -1, slot = -1;
+    size_t off = 0, bytes = 0;
+    Layout L;
+    std::vector<int> fr;
+    long long ldh = 0, ldx = 0;
+    int stage = 0;            // next stage to run
+    bool retiring = false;
+    cudaEvent_t done = nullptr;
+    std::vector<int> status;
+};
+
+}  // namespace
+}  // namespace hsr
+
+struct hsr_server {
+    hsr_server_config cfg{};
+    int b = 64, is = 1, max_slots = 4096;
+    cudaStream_t st = nullptr;
+    char *pool = nullptr;
+    size_t pool_bytes = 0;
+    PoolAlloc alloc;
+    DevProblem *d_probs = nullptr;
+    CUtensorMap *d_maps = nullptr;
+    int *d_err = nullptr;
+    BatchItem *d_items[2] = {nullptr, nullptr};
+    BatchItem *h_items[2] = {nullptr, nullptr};
+    size_t items_cap[2] = {0, 0};
+    DevProblem *h_prob_stage = nullptr;   // pinned staging for slot descriptors
+    CUtensorMap *h_map_stage = nullptr;
+    cudaEvent_t tick_ev[2] = {nullptr, nullptr};
+    std::vector<int> free_slots;
+    ~hsr_server() {
+        if (st) cudaStreamSynchronize(st);
+        for (int i = 0; i < 2; ++i) {
+            if (d_items[i]) cudaFree(d_items[i]);
+            if (h_items[i]) cudaFreeHost(h_items[i]);
+            if (tick_ev[i]) cudaEventDestroy(tick_ev[i]);
+        }
+        if (h_prob_stage) cudaFreeHost(h_prob_stage);
+        if (h_map_stage) cudaFreeHost(h_map_stage);
+        if (d_probs) cudaFree(d_probs);
+        if (d_maps) cudaFree(d_maps);
+        if (d_err) cudaFree(d_err);
+        if (pool) cudaFree(pool);
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+namespace {
+size_t request_bytes(const Layout &L, long long ldh, long long ldx) {
+    return L.total + up((size_t)ldh * L.n * 8, 256) + up((size_t)L.S * 8, 256) + up((size_t)ldx * L.S * 8, 256);
+}
+}  // namespace
+
+extern "C" int hsr_server_create(hsr_server **out, const hsr_server_config *cfg) {
+    if (!out) return HSR_ERR_ARG;
+    *out = nullptr;
+    hsr_server *s = new hsr_server();
+    if (cfg) s->cfg = *cfg;
+    s->b = s->cfg.tlsz > 0 ? s->cfg.tlsz : hsr_autotune_tlsz(64, 4096);
+    if (s->b % 4 || s->b > 384) {
+        delete s;
+        return HSR_ERR_ARG;
+    }
+    s->is = s->cfg.scaling == HSR_SCALING_DOUBLE ? 0 : 1;
+    s->max_slots = s->cfg.max_active > 0 ? s->cfg.max_active : 4096;
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    s->pool_bytes = (size_t)(s->cfg.hbm_budget_bytes > 0 ? s->cfg.hbm_budget_bytes : 0.4 * (double)fr);
+    s->pool_bytes = up(s->pool_bytes, 256);
+    bool ok = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaMalloc(&s->pool, s->pool_bytes) == cudaSuccess &&
+              cudaMalloc(&s->d_probs, sizeof(DevProblem) * s->max_slots) == cudaSuccess &&
+              cudaMalloc(&s->d_maps, sizeof(CUtensorMap) * 3 * (size_t)s->max_slots) == cudaSuccess &&
+              cudaMalloc(&s->d_err, 16) == cudaSuccess &&
+              cudaMallocHost(&s->h_prob_stage, sizeof(DevProblem) * s->max_slots) == cudaSuccess &&
+              cudaMallocHost(&s->h_map_stage, sizeof(CUtensorMap) * 3 * (size_t)s->max_slots) == cudaSuccess &&
+              cudaEventCreateWithFlags(&s->tick_ev[0], cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&s->tick_ev[1], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        delete s;
+        return HSR_ERR_NOMEM;
+    }
+    cudaMemset(s->d_err, 0, 16);
+    s->alloc.reset(s->pool_bytes);
+    *out = s;
+    return HSR_OK;
+}
+
+extern "C" void hsr_server_destroy(hsr_server *s) { delete s; }
+
+extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, double *latency, int *status_out,
+                                 hsr_server_stats *stats) {
+    if (!s || nreq < 0 || (nreq > 0 && !reqs)) return HSR_ERR_ARG;
+    using clock = std::chrono::steady_clock;
+    const auto t0 = clock::now();
+    auto elapsed = [&]() { return std::chrono::duration<double>(clock::now() - t0).count(); };
+    cudaStream_t st = s->st;
+    const int b = s->b;
+
+    std::vector<int> order(nreq);
+    for (int i = 0; i < nreq; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int c) { return reqs[a].arrival_s < reqs[c].arrival_s; });
+    for (int i = 0; i < nreq; ++i) {
+        const hsr_request &r = reqs[i];
+        if (r.n <= 0 || r.ldH < r.n || r.nrhs < 0 || r.ldvr < r.n || !r.H || (r.nrhs && (!r.wr || !r.vr)))
+            return HSR_ERR_ARG;
+        if (status_out) status_out[i] = HSR_OK;
+        if (latency) latency[i] = -1.0;
+    }
+    s->free_slots.clear();
+    for (int i = s->max_slots - 1; i >= 0; --i) s->free_slots.push_back(i);
+    std::deque<int> queue;
+    std::vector<ActiveReq> active;
+    size_t next = 0;
+    int completed = 0, max_active = 0, parity = 0;
+    long ticks = 0, launches = 0;
+    bool tick_used[2] = {false, false};
+    TickLists tl;
+    int result = HSR_OK;
+
+    while (completed < nreq) {
+        const double now = elapsed();
+        while (next < (size_t)nreq && reqs[order[next]].arrival_s <= now) queue.push_back(order[next++]);
+
+        // Retire requests whose results reached the host.
+        for (size_t i = 0; i < active.size();) {
+            ActiveReq &a = active[i];
+            if (a.retiring && cudaEventQuery(a.done) == cudaSuccess) {
+                const hsr_request &r = reqs[a.req];
+                cudaMemcpy(a.status.data(), s->pool + a.off + a.L.status, r.nrhs * sizeof(int),
+                           cudaMemcpyDeviceToHost);
+                bool all = true;
+                for (int v : a.status) all = all && v;
+                int rc = HSR_OK;
+                if (!all) {
+                    // Restart rounds: solved again on the plain path.
+                    hsr_options o{};
+                    o.scaling = s->is ? HSR_SCALING_POW2 : HSR_SCALING_DOUBLE;
+                    o.max_restarts = -1;
+                    rc = hsr_inverse_iteration_ex(r.n, r.H, r.ldH, r.nrhs, r.wr, b, 64, r.vr, r.ldvr, &o, nullptr);
+                    if (rc < 0) result = rc;
+                }
+                if (status_out) status_out[a.req] = rc;
+                if (latency) latency[a.req] = elapsed() - r.arrival_s;
+                cudaEventDestroy(a.done);
+                s->alloc.release(a.off, a.bytes);
+                s->free_slots.push_back(a.slot);
+                active[i] = std::move(active.back());
+                active.pop_back();
+                ++completed;
+                continue;
+            }
+            ++i;
+        }
+
+        // Admit in arrival order while the pool and slots allow.
+        tl.clear();
+        std::vector<int> admitted;
+        while (!queue.empty() && !s->free_slots.empty()) {
+            const int ri = queue.front();
+            const hsr_request &r = reqs[ri];
+            if (r.nrhs == 0) {
+                queue.pop_front();
+                if (latency) latency[ri] = elapsed() - r.arrival_s;
+                ++completed;
+                continue;
+            }
+            ActiveReq a;
+            a.req = ri;
+            a.L.compute(r.n, r.nrhs, b);
+            a.ldh = round_up_ll(r.n, 32);
+            a.ldx = round_up_ll(r.n, 4);
+            a.bytes = request_bytes(a.L, a.ldh, a.ldx);
+            if (a.bytes > s->pool_bytes) {   // can never fit
+                queue.pop_front();
+                if (status_out) status_out[ri] = HSR_ERR_NOMEM;
+                result = HSR_ERR_NOMEM;
+                ++completed;
+                continue;
+            }
+            if (!s->alloc.alloc(a.bytes, a.off)) break;   // head of line waits for memory
+            queue.pop_front();
+            a.slot = s->free_slots.back();
+            s->free_slots.pop_back();
+            char *base = s->pool + a.off;
+            double *dH = reinterpret_cast<double *>(base + a.L.total);
+            double *dwr = reinterpret_cast<double *>(base + a.L.total + up((size_t)a.ldh * r.n * 8, 256));
+            double *dX = reinterpret_cast<double *>(reinterpret_cast<char *>(dwr) + up((size_t)r.nrhs * 8, 256));
+            partition_rows(r.n, a.L.T, b, a.fr);
+            cudaMemcpy2DAsync(dH, a.ldh * 8, r.H, (size_t)r.ldH * 8, (size_t)r.n * 8, r.n, cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(dwr, r.wr, (size_t)r.nrhs * 8, cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(base + a.L.fr, a.fr.data(), (a.L.T + 1) * sizeof(int), cudaMemcpyHostToDevice, st);
+            cudaMemsetAsync(base, 0, a.L.zero_bytes, st);
+            DevProblem P = make_problem(a.L, base, dH, a.ldh, dwr, dX, a.ldx, s->is, s->d_err);
+            s->h_prob_stage[a.slot] = P;
+            make_maps(&s->h_map_stage[3 * (size_t)a.slot], a.L, dH, a.ldh, base);
+            cudaMemcpyAsync(s->d_probs + a.slot, s->h_prob_stage + a.slot, sizeof(DevProblem),
+                            cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(s->d_maps + 3 * (size_t)a.slot, s->h_map_stage + 3 * (size_t)a.slot,
+                            3 * sizeof(CUtensorMap), cudaMemcpyHostToDevice, st);
+            add_setup(tl, a.slot, a.L, a.fr);
+            a.stage = a.L.T - 1;
+            a.status.resize(r.nrhs);
+            active.push_back(std::move(a));
+        }
+        int running = 0;
+        for (auto &a : active)
+            if (!a.retiring) ++running;
+        max_active = std::max(max_active, (int)active.size());
+        if (running == 0) {
+            if (completed >= nreq) break;
+            // Idle: wait for an arrival or a completion.
+            bool pending_done = false;
+            for (auto &a : active) pending_done = pending_done || a.retiring;
+            if (!pending_done && next < (size_t)nreq && queue.empty()) {
+                const double wait = reqs[order[next]].arrival_s - elapsed();
+                if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.01)));
+            } else {
+                std::this_thread::sleep_for(std::chrono::microseconds(50));
+            }
+            continue;
+        }
+
+        // Build this tick: each running request runs its next stage.
+        for (auto &a : active) {
+            if (a.retiring) continue;
+            add_stage(tl, a.slot, a.L, a.fr, a.stage);
+        }
+        const size_t count = tl.size();
+        // The item buffer of this parity was last used two ticks ago.
+        if (tick_used[parity]) cudaEventSynchronize(s->tick_ev[parity]);
+        if (count > s->items_cap[parity]) {
+            if (s->d_items[parity]) cudaFree(s->d_items[parity]);
+            if (s->h_items[parity]) cudaFreeHost(s->h_items[parity]);
+            s->items_cap[parity] = std::max<size_t>(count * 2, 4096);
+            if (cudaMalloc(&s->d_items[parity], sizeof(BatchItem) * s->items_cap[parity]) != cudaSuccess ||
+                cudaMallocHost(&s->h_items[parity], sizeof(BatchItem) * s->items_cap[parity]) != cudaSuccess)
+                return HSR_ERR_NOMEM;
+        }
+        size_t off = 0;
+        size_t poff[phCount];
+        for (int ph = 0; ph < phCount; ++ph) {
+            poff[ph] = off;
+            if (!tl.v[ph].empty())
+                memcpy(s->h_items[parity] + off, tl.v[ph].data(), sizeof(BatchItem) * tl.v[ph].size());
+            off += tl.v[ph].size();
+        }
+        cudaMemcpyAsync(s->d_items[parity], s->h_items[parity], sizeof(BatchItem) * count, cudaMemcpyHostToDevice,
+                        st);
+        for (int ph = 0; ph < phCount; ++ph) {
+            if (tl.v[ph].empty()) continue;
+            if (launch_phase(ph, s->d_probs, s->d_items[parity] + poff[ph], (int)tl.v[ph].size(), b, s->d_maps, st) !=
+                cudaSuccess)
+                return HSR_ERR_CUDA;
+            ++launches;
+        }
+        // Requests that finished this tick: copy results to the host.
+        for (auto &a : active) {
+            if (a.retiring) continue;
+            if (a.stage == 0) {
+                const hsr_request &r = reqs[a.req];
+                char *base = s->pool + a.off;
+                double *dwr = reinterpret_cast<double *>(base + a.L.total + up((size_t)a.ldh * r.n * 8, 256));
+                double *dX = reinterpret_cast<double *>(reinterpret_cast<char *>(dwr) + up((size_t)r.nrhs * 8, 256));
+                cudaMemcpy2DAsync(r.vr, (size_t)r.ldvr * 8, dX, a.ldx * 8, (size_t)r.n * 8, r.nrhs,
+                                  cudaMemcpyDeviceToHost, st);
+                cudaEventCreateWithFlags(&a.done, cudaEventDisableTiming);
+                cudaEventRecord(a.done, st);
+                a.retiring = true;
+            } else {
+                --a.stage;
+            }
+        }
+        cudaEventRecord(s->tick_ev[parity], st);
+        tick_used[parity] = true;
+        parity ^= 1;
+        ++ticks;
+    }
+    cudaStreamSynchronize(st);
+    int errw = 0;
+    cudaMemcpy(&errw, s->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (errw) result = HSR_ERR_DEVICE;
+    if (stats) {
+        stats->wall_s = elapsed();
+        stats->ticks = ticks;
+        stats->launches = launches;
+        stats->max_active = max_active;
+        stats->peak_bytes = (double)s->alloc.peak;
+    }
+    return result;
+}

@@ -5,6 +5,7 @@
 // check and the restart rounds (inverse_iteration.c:176-205, restated with the
 // intended semantics), and copies vr and wr back.  Workspaces are cached per
 // host thread and grow on demand.
+#include "hsr_common.h"
 #include "hsr_kernels.h"
 #include "../../include/hsrq3in_gb300.h"
 
@@ -112,10 +113,12 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
+}  // namespace
+
 // 2-D FP64 tensor map: inner extent `inner` (contiguous), outer extent
 // `outer`, row pitch `ld` elements, box {bx, by}; out-of-range reads are 0.
-bool make_map(CUtensorMap *m, const double *base, unsigned long long inner, unsigned long long outer,
-              unsigned long long ld, unsigned bx, unsigned by) {
+bool encode_tensor_map(CUtensorMap *m, const double *base, unsigned long long inner, unsigned long long outer,
+                       unsigned long long ld, unsigned bx, unsigned by) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return false;
     cuuint64_t dims[2] = {inner, outer};
@@ -125,6 +128,13 @@ bool make_map(CUtensorMap *m, const double *base, unsigned long long inner, unsi
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double *>(base), dims, strides, box, es,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+namespace {
+
+bool make_map(CUtensorMap *m, const double *base, unsigned long long inner, unsigned long long outer,
+              unsigned long long ld, unsigned bx, unsigned by) {
+    return encode_tensor_map(m, base, inner, outer, ld, bx, by);
 }
 
 inline long long round_up(long long x, long long m) { return (x + m - 1) / m * m; }

@@ -155,11 +155,13 @@ size_t diag_smem_bytes(int b) {
     return full <= 200 * 1024 ? full : small;
 }
 
-__global__ void __launch_bounds__(32 * kDiagWarps) k_diag(DevProblem P, int J, double *gscratch) {
+// Body of the diagonal kernel for the 32 shifts of block bx; vy_scratch is
+// this block's global v/y region, or null when v/y fit in shared memory.
+__device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, double *vy_scratch) {
     extern __shared__ double sm[];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
-    const int k0 = blockIdx.x * 32;
+    const int k0 = bx * 32;
     const int k = k0 + lane;
     const bool act = k < P.S;
     const int l = P.fr[J], b = P.fr[J + 1] - l;
@@ -170,8 +172,8 @@ __global__ void __launch_bounds__(32 * kDiagWarps) k_diag(DevProblem P, int J, d
     // Per-warp partial maxima, double-buffered by step parity: [2][W][2][32].
     unsigned long long *pmax = reinterpret_cast<unsigned long long *>(sm + 2 * (b + 1));
     double *v, *y;
-    if (gscratch) {
-        v = gscratch + (size_t)blockIdx.x * 64 * b;
+    if (vy_scratch) {
+        v = vy_scratch;
         y = v + (size_t)32 * b;
     } else {
         v = sm + 2 * (b + 1) + 2 * kDiagWarps * 2 * 32;
@@ -439,6 +441,11 @@ __global__ void __launch_bounds__(32 * kDiagWarps) k_diag(DevProblem P, int J, d
 #undef PMAX
 }
 
+__global__ void __launch_bounds__(32 * kDiagWarps) k_diag(DevProblem P, int J, double *gscratch) {
+    const int b = P.fr[J + 1] - P.fr[J];
+    diag_body(P, J, blockIdx.x, gscratch ? gscratch + (size_t)blockIdx.x * 64 * b : nullptr);
+}
+
 cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st) {
     const size_t small = (size_t)(2 * (b + 1)) * sizeof(double) + (size_t)2 * kDiagWarps * 2 * 32 * 8;
     const size_t smem = gscratch ? small : diag_smem_bytes(b);
@@ -457,10 +464,9 @@ cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cud
 // decision of :206-226.  Columns that need a rescaled Ytilde2 (Y scale below
 // X scale, or a Part-2 factor != 1) get it written to Zslow and are flagged
 // for the protected path of the GEMM epilogue.
-__global__ void __launch_bounds__(256) k_part1(DevProblem P, int J) {
+__device__ __forceinline__ void part1_body(const DevProblem &P, int J, int I, int bx) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int I = blockIdx.y;
-    const int k = blockIdx.x * 8 + warp;
+    const int k = bx * 8 + warp;
     if (k >= P.S) return;
     const bool is = P.is != 0;
     const size_t Spad = (size_t)P.Spad;
@@ -563,6 +569,8 @@ __global__ void __launch_bounds__(256) k_part1(DevProblem P, int J) {
     }
 }
 
+__global__ void __launch_bounds__(256) k_part1(DevProblem P, int J) { part1_body(P, J, blockIdx.y, blockIdx.x); }
+
 cudaError_t launch_part1(const DevProblem &P, int J, cudaStream_t st) {
     dim3 g((P.S + 7) / 8, J);
     k_part1<<<g, 256, 0, st>>>(P, J);
@@ -584,17 +592,17 @@ struct GemmSmem {
 
 size_t gemm_smem_bytes() { return sizeof(GemmSmem) + 128; }
 
-__global__ void __launch_bounds__(256, 2)
-k_gemm(DevProblem P, int J, int row_lo, int row_hi, const __grid_constant__ CUtensorMap tmH,
-       const __grid_constant__ CUtensorMap tmW, const __grid_constant__ CUtensorMap tmZ) {
+__device__ __forceinline__ void gemm_body(const DevProblem &P, int J, int row_lo, int row_hi, int bx, int by,
+                                          const CUtensorMap *tmH, const CUtensorMap *tmW,
+                                          const CUtensorMap *tmZ) {
     extern __shared__ unsigned char smraw[];
     GemmSmem &sm = *reinterpret_cast<GemmSmem *>(
         (reinterpret_cast<uintptr_t>(smraw) + 127) & ~uintptr_t(127));
     const int tid = threadIdx.x;
     // Row blocks start at row_lo rounded down to 8, so the TMA x coordinate
     // is always 16-byte aligned; rows outside [row_lo, row_hi) are not stored.
-    const int row0 = (row_lo & ~7) + blockIdx.x * kGemmBM;
-    const int col0 = blockIdx.y * kGemmBN;
+    const int row0 = (row_lo & ~7) + bx * kGemmBM;
+    const int col0 = by * kGemmBN;
     const int l = P.fr[J], b = P.fr[J + 1] - l;
     const int nk = (b + kGemmKC - 1) / kGemmKC;
     const uint32_t bytes = (uint32_t)((kGemmBM + 2 * kGemmBN) * kGemmKC * sizeof(double));
@@ -602,16 +610,16 @@ k_gemm(DevProblem P, int J, int row_lo, int row_hi, const __grid_constant__ CUte
     if (tid == 0) {
         for (int s = 0; s < kGemmStages; ++s) mbar_init(&sm.full[s], 1);
         mbar_fence_init();
-        prefetch_tensormap(&tmH);
-        prefetch_tensormap(&tmW);
-        prefetch_tensormap(&tmZ);
+        prefetch_tensormap(tmH);
+        prefetch_tensormap(tmW);
+        prefetch_tensormap(tmZ);
     }
     __syncthreads();
     auto issue = [&](int s, int kc) {
         mbar_expect_tx(&sm.full[s], bytes);
-        tma_load_2d(&sm.A[s][0][0], &tmH, &sm.full[s], row0, l - 1 + kc * kGemmKC);
-        tma_load_2d(&sm.W[s][0][0], &tmW, &sm.full[s], col0, kc * kGemmKC);
-        tma_load_2d(&sm.Z[s][0][0], &tmZ, &sm.full[s], col0, kc * kGemmKC);
+        tma_load_2d(&sm.A[s][0][0], tmH, &sm.full[s], row0, l - 1 + kc * kGemmKC);
+        tma_load_2d(&sm.W[s][0][0], tmW, &sm.full[s], col0, kc * kGemmKC);
+        tma_load_2d(&sm.Z[s][0][0], tmZ, &sm.full[s], col0, kc * kGemmKC);
     };
     if (tid == 0)
         for (int s = 0; s < kGemmStages && s < nk; ++s) issue(s, s);
@@ -710,6 +718,12 @@ k_gemm(DevProblem P, int J, int row_lo, int row_hi, const __grid_constant__ CUte
     }
 }
 
+__global__ void __launch_bounds__(256, 2)
+k_gemm(DevProblem P, int J, int row_lo, int row_hi, const __grid_constant__ CUtensorMap tmH,
+       const __grid_constant__ CUtensorMap tmW, const __grid_constant__ CUtensorMap tmZ) {
+    gemm_body(P, J, row_lo, row_hi, blockIdx.x, blockIdx.y, &tmH, &tmW, &tmZ);
+}
+
 cudaError_t launch_gemm(const DevProblem &P, int J, int row_lo, int row_hi, const CUtensorMap &tmH,
                         const CUtensorMap &tmW, const CUtensorMap &tmZ, cudaStream_t st) {
     static bool configured = false;
@@ -732,11 +746,11 @@ cudaError_t launch_gemm(const DevProblem &P, int J, int row_lo, int row_hi, cons
 // three-accumulator 2-norm and the convergence test ||y|| > 0.1/sqrt(n)
 // (:33-40, :229-273).  Rows move through shared memory 32 at a time so that
 // the column-major block is read and written coalesced.
-__global__ void __launch_bounds__(32) k_finalize(DevProblem P, double *colnorm, int *status,
-                                                 double *scale_out) {
+__device__ __forceinline__ void finalize_body(const DevProblem &P, int bx, double *colnorm, int *status,
+                                              double *scale_out) {
     __shared__ double buf[32][33];
     const int lane = threadIdx.x;
-    const int k0 = blockIdx.x * 32;
+    const int k0 = bx * 32;
     const int k = k0 + lane;
     const bool act = k < P.S;
     const bool is = P.is != 0;
@@ -799,6 +813,11 @@ __global__ void __launch_bounds__(32) k_finalize(DevProblem P, double *colnorm, 
     }
 }
 
+__global__ void __launch_bounds__(32) k_finalize(DevProblem P, double *colnorm, int *status,
+                                                 double *scale_out) {
+    finalize_body(P, blockIdx.x, colnorm, status, scale_out);
+}
+
 cudaError_t launch_finalize(const DevProblem &P, double *colnorm, int *status, double *scale_out,
                             cudaStream_t st) {
     k_finalize<<<(P.S + 31) / 32, 32, 0, st>>>(P, colnorm, status, scale_out);
@@ -838,6 +857,149 @@ cudaError_t launch_gather_cols(double *dst, long long ldd, const double *src, lo
     if (bx > 64) bx = 64;
     dim3 g(bx, cnt);
     k_gather_cols<<<g, 256, 0, st>>>(dst, ldd, src, lds, n, perm);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ batched
+// Each block reads its work item and its problem's descriptor, then runs the
+// same body as the single-problem kernel, so a column computes exactly what
+// it computes when its problem is solved alone.
+
+__global__ void k_norms_b(const DevProblem *probs, const BatchItem *items) {
+    const BatchItem it = items[blockIdx.x];
+    const DevProblem &P = probs[it.x];
+    const int i = it.z * kNormRows + threadIdx.x;
+    if (i >= P.n || threadIdx.x >= kNormRows) return;
+    const double *row = P.H + i;
+    const int T = P.T;
+    if (it.y < 0) {
+        double sum = 0.0;
+        for (int c = 0; c < P.n; ++c) sum += fabs(row[(size_t)c * P.ldh]);
+        if (sum != sum) atomicOr(P.nanflag, 1);
+        atomicMax(&P.nbits[2 * (size_t)T * T], (unsigned long long)__double_as_longlong(sum));
+        return;
+    }
+    const int J = it.y;
+    int I = T - 1 - (P.n - 1 - i) / P.tlsz;
+    if (I < 0) I = 0;
+    if (J < I) return;
+    const int c0 = P.fr[J], c1 = P.fr[J + 1];
+    double sum = 0.0;
+    for (int c = c0; c < c1; ++c) sum += fabs(row[(size_t)c * P.ldh]);
+    atomicMax(&P.nbits[I + (size_t)J * T], (unsigned long long)__double_as_longlong(sum));
+    if (J > I) atomicMax(&P.nbits[(size_t)T * T + I + (size_t)J * T], abs_bits(row[(size_t)(c0 - 1) * P.ldh]));
+}
+
+// Start vector eps3 = ||H||_oo * eps/2 (inverse_iteration.c:154-158, 19-34),
+// computed on the device from the norm accumulators.
+__global__ void k_init_b(const DevProblem *probs, const BatchItem *items) {
+    const BatchItem it = items[blockIdx.x];
+    const DevProblem &P = probs[it.x];
+    const int k = it.z;
+    const int T = P.T, n = P.n;
+    double hinf = from_bits(P.nbits[2 * (size_t)T * T]);
+    if (P.nanflag[0] & 1) hinf = __longlong_as_double(0x7ff8000000000000LL);
+    const double eps3 = hinf * (DBL_EPSILON / 2);
+    double *x = P.X + (size_t)k * P.ldx;
+    double *r = P.R + (size_t)k * P.ldr;
+    const double *hl = P.H + (size_t)(n - 1) * P.ldh;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double h = hl[i];
+        if (i == n - 1) h = h - P.wr[k];
+        r[i] = h;
+        x[i] = eps3;
+    }
+    for (int I = threadIdx.x; I < T; I += blockDim.x) {
+        P.beta[(size_t)I * P.Spad + k] = sc_one(P.is);
+        P.ynorm[(size_t)I * P.Spad + k] = eps3;
+    }
+    if (threadIdx.x == 0) P.pert[k] = 0;
+}
+
+__global__ void __launch_bounds__(32 * kDiagWarps) k_diag_b(const DevProblem *probs, const BatchItem *items) {
+    const BatchItem it = items[blockIdx.x];
+    diag_body(probs[it.x], it.y, it.z, nullptr);
+}
+
+__global__ void __launch_bounds__(256) k_part1_b(const DevProblem *probs, const BatchItem *items) {
+    const BatchItem it = items[blockIdx.x];
+    part1_body(probs[it.x], it.y, it.z, it.w);
+}
+
+__global__ void __launch_bounds__(256, 2) k_gemm_b(const DevProblem *probs, const BatchItem *items,
+                                                  const CUtensorMap *maps) {
+    const BatchItem it = items[blockIdx.x];
+    const DevProblem &P = probs[it.x];
+    const CUtensorMap *m = maps + 3 * (size_t)it.x;
+    gemm_body(P, it.y, 0, P.fr[it.y], it.z, it.w, m, m + 1, m + 2);
+}
+
+__global__ void __launch_bounds__(32) k_finalize_b(const DevProblem *probs, const BatchItem *items) {
+    const BatchItem it = items[blockIdx.x];
+    const DevProblem &P = probs[it.x];
+    finalize_body(P, it.z, P.colnorm, P.status, P.scale);
+}
+
+__global__ void k_normalize_b(const DevProblem *probs, const BatchItem *items) {
+    const BatchItem it = items[blockIdx.x];
+    const DevProblem &P = probs[it.x];
+    const int k = it.z * kNormalizeCols + (threadIdx.x >> 5);
+    if (k >= P.S || !P.status[k]) return;
+    const double nrm = P.colnorm[k];
+    double *x = P.X + (size_t)k * P.ldx;
+    for (int i = threadIdx.x & 31; i < P.n; i += 32) x[i] = x[i] / nrm;
+}
+
+cudaError_t launch_norms_b(const DevProblem *probs, const BatchItem *items, int n_items, cudaStream_t st) {
+    if (n_items <= 0) return cudaSuccess;
+    k_norms_b<<<n_items, kNormRows, 0, st>>>(probs, items);
+    return cudaGetLastError();
+}
+cudaError_t launch_init_b(const DevProblem *probs, const BatchItem *items, int n_items, cudaStream_t st) {
+    if (n_items <= 0) return cudaSuccess;
+    k_init_b<<<n_items, 128, 0, st>>>(probs, items);
+    return cudaGetLastError();
+}
+cudaError_t launch_diag_b(const DevProblem *probs, const BatchItem *items, int n_items, int bmax,
+                          cudaStream_t st) {
+    const size_t smem = diag_smem_bytes(bmax);
+    if (smem < (size_t)64 * bmax * sizeof(double)) return cudaErrorInvalidValue;   // must fit shared memory
+    static size_t configured = 0;
+    if (smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_diag_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    if (n_items <= 0) return cudaSuccess;
+    k_diag_b<<<n_items, 32 * kDiagWarps, smem, st>>>(probs, items);
+    return cudaGetLastError();
+}
+cudaError_t launch_part1_b(const DevProblem *probs, const BatchItem *items, int n_items, cudaStream_t st) {
+    if (n_items <= 0) return cudaSuccess;
+    k_part1_b<<<n_items, 256, 0, st>>>(probs, items);
+    return cudaGetLastError();
+}
+cudaError_t launch_gemm_b(const DevProblem *probs, const BatchItem *items, int n_items, const CUtensorMap *maps,
+                          cudaStream_t st) {
+    static bool configured = false;
+    const size_t smem = gemm_smem_bytes();
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    if (n_items <= 0) return cudaSuccess;
+    k_gemm_b<<<n_items, 256, smem, st>>>(probs, items, maps);
+    return cudaGetLastError();
+}
+cudaError_t launch_finalize_b(const DevProblem *probs, const BatchItem *items, int n_items, cudaStream_t st) {
+    if (n_items <= 0) return cudaSuccess;
+    k_finalize_b<<<n_items, 32, 0, st>>>(probs, items);
+    return cudaGetLastError();
+}
+cudaError_t launch_normalize_b(const DevProblem *probs, const BatchItem *items, int n_items, cudaStream_t st) {
+    if (n_items <= 0) return cudaSuccess;
+    k_normalize_b<<<n_items, 32 * kNormalizeCols, 0, st>>>(probs, items);
     return cudaGetLastError();
 }
 

@@ -39,7 +39,17 @@ struct DevProblem {
     double smlnum;
     int is;                    // integer (base-2 exponent) scaling factors
     int *err;                  // device error word
+    // Used by the batched kernels, where every problem carries its own:
+    double *colnorm;           // [S] 2-norm before normalisation
+    int *status;               // [S] 1 converged
+    double *scale;             // [S] reconciled scaling factor
+    unsigned long long *nbits; // [2*T*T + 2]: Hn, hn, ||H||_oo, eps3 (as bit patterns)
+    int *nanflag;              // [2]
 };
+
+// Work item of a batched kernel: x = problem, y = tile stage J (or -1),
+// z, w = block indices whose meaning depends on the kernel.
+typedef int4 BatchItem;
 
 // Setup: tile norms, eps3 = ||H||_oo * eps/2.  hnbits/Hnbits/hnorm_bits are
 // zeroed by the caller.
@@ -65,6 +75,27 @@ cudaError_t launch_normalize(const DevProblem &P, const double *colnorm,
 cudaError_t launch_gather_cols(double *dst, long long ldd, const double *src,
                                long long lds, int n, const int *perm, int cnt,
                                cudaStream_t st);
+// Batched kernels: one launch covers work items of many problems.
+//   norms:    (p, J, row block, 0)       J = -1: full row sums for ||H||_oo
+//   init:     (p, 0, column, 0)          start vector eps3 (from the norms)
+//   diag:     (p, J, shift block, 0)
+//   part1:    (p, J, tile I, shift block of 8)
+//   gemm:     (p, J, row block, column block) over rows [0, fr[J])
+//   finalize: (p, 0, shift block, 0)
+//   normalize:(p, 0, column block of 8, 0)
+// `maps` holds three tensor maps per problem: H, W, Zs.
+cudaError_t launch_norms_b(const DevProblem *probs, const BatchItem *items, int n_items, cudaStream_t st);
+cudaError_t launch_init_b(const DevProblem *probs, const BatchItem *items, int n_items, cudaStream_t st);
+cudaError_t launch_diag_b(const DevProblem *probs, const BatchItem *items, int n_items, int bmax,
+                          cudaStream_t st);
+cudaError_t launch_part1_b(const DevProblem *probs, const BatchItem *items, int n_items, cudaStream_t st);
+cudaError_t launch_gemm_b(const DevProblem *probs, const BatchItem *items, int n_items, const CUtensorMap *maps,
+                          cudaStream_t st);
+cudaError_t launch_finalize_b(const DevProblem *probs, const BatchItem *items, int n_items, cudaStream_t st);
+cudaError_t launch_normalize_b(const DevProblem *probs, const BatchItem *items, int n_items, cudaStream_t st);
+constexpr int kNormRows = 128;        // rows per norms item
+constexpr int kNormalizeCols = 8;     // columns per normalize item
+
 // FP64 throughput probe kernels.
 cudaError_t launch_probe_dfma(double *out, int blocks, int iters, cudaStream_t st);
 cudaError_t launch_probe_dmma(double *out, int blocks, int iters, cudaStream_t st);

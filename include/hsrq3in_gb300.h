@@ -121,6 +121,90 @@ int hsr_last_kernel_times(double *ms, long *launches, double *gemm_fma);
 /* Release cached device workspaces of this thread. */
 void hsr_release_workspace(void);
 
+/* ------------------------------------------------------- batched solves */
+/* No counterpart in the reference (it solves one H per call).  Thousands of
+ * independent problems of different orders and shift counts are solved
+ * together: every problem advances one tile stage per "tick" and each tick
+ * launches one batched kernel per phase over all problems, so small problems
+ * fill the GPU together.  Per column the arithmetic is exactly that of
+ * hsr_inverse_iteration_device with the same tlsz, so each problem's result
+ * is bit-identical to solving it alone.  All pointers are device pointers. */
+typedef struct hsr_batch_problem {
+    int n;              /* order of H, n > 0                                  */
+    const double *dH;   /* n x n, leading dimension lddH (even, 16-byte aligned) */
+    int lddH;
+    int nrhs;           /* number of shifts                                   */
+    double *dwr;        /* [nrhs] shifts (reordered only on restart)          */
+    double *dvr;        /* n x nrhs output, leading dimension lddvr           */
+    int lddvr;
+} hsr_batch_problem;
+
+typedef struct hsr_batch_plan hsr_batch_plan;
+
+/* Lay out one device workspace for all problems, build the tick schedule and
+ * capture it in one CUDA graph (replayed by every execute).  tlsz: row tile
+ * size (multiple of 4, at most 384); 0 picks the autotuned size for this GPU
+ * (hsr_autotune_tlsz).  Returns a status code. */
+int hsr_batch_plan_create(hsr_batch_plan **plan, int nprob, const hsr_batch_problem *probs,
+                          int tlsz, const hsr_options *opt, void *stream);
+/* Run the plan on `stream` (one graph launch), then restart the columns that
+ * did not converge, problem by problem.  Synchronises the stream. */
+int hsr_batch_plan_execute(hsr_batch_plan *plan, void *stream);
+/* Tile size, ticks and kernel launches captured in the plan's graph. */
+int hsr_batch_plan_info(const hsr_batch_plan *plan, int *tlsz, int *ticks, long *launches);
+void hsr_batch_plan_destroy(hsr_batch_plan *plan);
+
+/* Tile size for batches whose orders lie in [n_lo, n_hi]: measured by
+ * hsr_autotune_batch on this GPU when a measurement exists, else a default. */
+int hsr_autotune_tlsz(int n_lo, int n_hi);
+/* Time a sample batch for each candidate tile size in `cand` and record the
+ * fastest for [n_lo, n_hi]; returns it.  ms_out[i] gets candidate i's time. */
+int hsr_autotune_batch(int nprob, const hsr_batch_problem *probs, const int *cand, int ncand,
+                       double *ms_out, void *stream);
+
+/* ------------------------------------------------------- served requests */
+/* A request loop with continuous batching.  Requests (host buffers) are
+ * admitted in arrival order while their device footprint fits the HBM budget,
+ * copied to the device, and advanced one tile stage per tick together with
+ * every other admitted request; requests that arrive while others are on the
+ * GPU join at the next tick.  Results are copied back to the request's host
+ * vr and wr. */
+typedef struct hsr_server_config {
+    double hbm_budget_bytes;   /* device pool for admitted requests (0: 40% of free) */
+    int tlsz;                  /* row tile size (0: autotuned)                        */
+    int max_active;            /* admission cap on concurrent requests (0: 4096)      */
+    int scaling;               /* HSR_SCALING_POW2 or HSR_SCALING_DOUBLE             */
+} hsr_server_config;
+
+typedef struct hsr_request {
+    int n;
+    const double *H;        /* host, column-major, leading dimension ldH */
+    int ldH;
+    int nrhs;
+    double *wr;             /* host [nrhs], in/out                         */
+    double *vr;             /* host n x nrhs output, leading dimension ldvr */
+    int ldvr;
+    double arrival_s;       /* arrival time, seconds after the replay starts */
+} hsr_request;
+
+typedef struct hsr_server_stats {
+    double wall_s;          /* replay wall time                          */
+    long ticks;             /* ticks run                                 */
+    long launches;          /* kernel launches                           */
+    int max_active;         /* largest number of concurrently admitted requests */
+    double peak_bytes;      /* largest pool footprint                    */
+} hsr_server_stats;
+
+typedef struct hsr_server hsr_server;
+int hsr_server_create(hsr_server **srv, const hsr_server_config *cfg);
+/* Serve `nreq` requests, each admitted no earlier than its arrival time
+ * (wall clock, measured from the call); latency_s[i] = completion time of
+ * request i (result on the host) minus its arrival time.  status[i] (optional)
+ * is the request's status code. */
+int hsr_server_replay(hsr_server *srv, int nreq, hsr_request *reqs, double *latency_s, int *status,
+                      hsr_server_stats *stats);
+void hsr_server_destroy(hsr_server *srv);
+
 /* ------------------------------------------- no-allocation device call */
 /* No counterpart in the reference.  For callers that may not allocate device
  * memory while they run -- a serving process whose device memory is owned by
