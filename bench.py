@@ -64,6 +64,15 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0, help="shifts in the CPU sample (0 = 64 per core)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "served"],
+                    help="plain: n=10k solve (default); batched: 4096 mixed problems in one graph; "
+                         "served: a Poisson request trace through the request loop")
+    ap.add_argument("--problems", type=int, default=4096, help="batched: number of problems")
+    ap.add_argument("--requests", type=int, default=800, help="served: number of requests")
+    ap.add_argument("--rate", type=float, default=120.0, help="served: arrivals per second")
+    ap.add_argument("--pool", type=int, default=48, help="served: distinct generated matrices")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="served: HBM budget")
+    ap.add_argument("--batch-tlsz", type=int, default=0, help="batched/served tile size (0: autotune)")
     return ap.parse_args()
 
 
@@ -83,6 +92,46 @@ def workload(n: int, seed: int):
     np.savez(tmp, H=H, wr=wr)
     os.replace(tmp, f)
     return H, wr
+
+
+def _gen_one(args):
+    """(H, shifts) of one mixed-size problem; runs in a spawned worker."""
+    n, seed, lo, hi = args
+    from hsrq3in_gb300 import generators as G
+    H, lam = G.real_spectrum(n, seed)
+    rng = np.random.default_rng(seed + 7)
+    wr = G.shift_subset(G.perturbed_shifts(lam, seed + 3), rng, lo, hi)
+    return H, wr
+
+
+def mixed_problems(count: int, nlo: int, nhi: int, flo: float, fhi: float, seed: int):
+    """count problems, n log-uniform in [nlo, nhi], a random fraction U[flo, fhi]
+    of their eigenvalues as shifts; generated in a spawn process pool (before
+    any GPU work)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    rng = np.random.default_rng(seed)
+    ns = np.round(np.exp(rng.uniform(np.log(nlo), np.log(nhi), count))).astype(int)
+    jobs = [(int(n), seed * 100003 + i, flo, fhi) for i, n in enumerate(ns)]
+    order = np.argsort(-ns)                      # big ones first for balance
+    out = [None] * count
+    # One BLAS thread per worker: workers x BLAS threads would oversubscribe
+    # the cores (measured 60x slower).  Spawned workers read the environment.
+    saved = {k: os.environ.get(k) for k in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS")}
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    os.environ["OMP_NUM_THREADS"] = "1"
+    try:
+        with cf.ProcessPoolExecutor(max_workers=os.cpu_count() or 1, mp_context=mp.get_context("spawn")) as ex:
+            futs = {ex.submit(_gen_one, jobs[i]): i for i in order}
+            for f in cf.as_completed(futs):
+                out[futs[f]] = f.result()
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    return out
 
 
 # ------------------------------------------------------------------ clocks
@@ -292,8 +341,163 @@ def run_gpu(args, H, wr, rank, world):
     return out
 
 
+def run_batched(args):
+    """Config 4: independent problems of mixed order in one graph launch."""
+    import torch
+    import hsrq3in_gb300 as hsr
+    probs = mixed_problems(args.problems, 32, 1024, 0.25, 1.0, args.seed)
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    tens = []
+    for H, wr in probs:
+        n = H.shape[0]
+        ld = n + (n & 1)
+        dH = torch.zeros((n, ld), dtype=torch.float64, device=dev)
+        dH[:, :n] = torch.from_numpy(np.ascontiguousarray(H.T)).to(dev)
+        dwr = torch.from_numpy(np.ascontiguousarray(wr)).to(dev)
+        dvr = torch.empty((len(wr), ld), dtype=torch.float64, device=dev)
+        tens.append((dH, dwr, dvr))
+    stream = torch.cuda.Stream(device=dev)
+    tune = None
+    if args.batch_tlsz == 0:
+        rng = np.random.default_rng(5)
+        sample = [tens[i] for i in rng.choice(len(tens), size=min(512, len(tens)), replace=False)]
+        best, ms = hsr.autotune_batch(sample, candidates=(32, 48, 64, 96), stream=stream)
+        tune = {"candidates": [32, 48, 64, 96], "ms": ms, "best": best}
+    plan = hsr.BatchPlan(tens, tlsz=args.batch_tlsz, stream=stream)
+    info = plan.info()
+    for _ in range(args.warmup):
+        plan.execute()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            plan.execute()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    total_shifts = sum(len(wr) for _, wr in probs)
+    flops = sum(2.0 * H.shape[0] ** 2 * len(wr) for H, wr in probs)
+    peak = hsr.fp64_peak(200.0)[0] / 1e3
+    # Looping the plain device path over a sample of the same problems.
+    rng = np.random.default_rng(11)
+    idx = rng.choice(len(tens), size=min(256, len(tens)), replace=False)
+    tl = info["tlsz"]
+    for i in idx[:4]:
+        hsr.inverse_iteration_device(tens[i][0], tens[i][1], tens[i][2], tl, stream=stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in idx:
+        dH, dwr, dvr = tens[i]
+        hsr.inverse_iteration_device(dH, dwr, dvr, tl, stream=stream)
+    torch.cuda.synchronize()
+    loop_s = time.perf_counter() - t0
+    loop_rate = sum(len(probs[i][1]) for i in idx) / loop_s
+    # spot check: the batch's result for a few problems against their lone solve
+    plan.execute()
+    torch.cuda.synchronize()
+    ok = True
+    for i in idx[:8]:
+        H, wr = probs[i]
+        alone = hsr.inverse_iteration(H, wr, tl, 16)
+        got = tens[i][2][:, :H.shape[0]].cpu().numpy().T
+        ok = ok and bool(np.array_equal(got, alone["vr"]))
+    value = total_shifts / (ms / 1e3)
+    return {"metric": "FP64 eigenvectors/s, batched mixed-size problems", "value": value,
+            "unit": "eigenvectors/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded generator)",
+            "config": {"workload": "batched: %d problems, n log-uniform [32,1024], shift fraction U[0.25,1], "
+                                   "one CUDA-graph launch per step" % len(probs),
+                       "problems": len(probs), "total_shifts": total_shifts, "tlsz": tl,
+                       "ticks": info["ticks"], "graph_launches": info["launches"], "autotune": tune},
+            "solves_per_s": len(probs) / (ms / 1e3),
+            "whole_tflops_2n2S": flops / (ms / 1e3) / 1e12, "frac_of_fp64_peak": flops / (ms / 1e3) / 1e12 / peak,
+            "plain_loop": {"eigenvectors_per_s": loop_rate, "sample_problems": int(len(idx)),
+                           "speedup_batched_over_loop": value / loop_rate},
+            "check": {"bitwise_equal_to_lone_solve_8_problems": ok},
+            "clocks": clk.summary()}
+
+
+def run_served(args):
+    """Config 5: a Poisson trace of requests through the request loop."""
+    import torch
+    import hsrq3in_gb300 as hsr
+    base = mixed_problems(args.pool, 64, 4096, 1.0, 1.0, args.seed + 1)
+    rng = np.random.default_rng(args.seed + 2)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, args.requests))
+    arrivals -= arrivals[0]
+    # pinned host buffers: each pool matrix once; outputs per request
+    Hp = []
+    for H, _ in base:
+        t = torch.from_numpy(np.asfortranarray(H).ravel(order="F")).pin_memory()
+        Hp.append((t, H.shape[0]))
+    reqs = []
+    total = 0
+    for i in range(args.requests):
+        j = int(rng.integers(len(base)))
+        H, lam = base[j]
+        n = H.shape[0]
+        m = max(1, int(round(n * rng.uniform(0.1, 1.0))))
+        wr = np.sort(rng.choice(lam, size=m, replace=False))
+        total += m
+        reqs.append((j, n, wr))
+    outs = torch.empty(sum(n * len(wr) for _, n, wr in reqs), dtype=torch.float64).pin_memory()
+    wrs = torch.empty(total, dtype=torch.float64).pin_memory()
+    lib = hsr.load()
+    from hsrq3in_gb300 import _lib
+    arr = (_lib.Request * len(reqs))()
+    o = w = 0
+    for i, (j, n, wr) in enumerate(reqs):
+        wrs.numpy()[w:w + len(wr)] = wr
+        arr[i] = _lib.Request(n, Hp[j][0].data_ptr(), n, len(wr), wrs.data_ptr() + 8 * w,
+                              outs.data_ptr() + 8 * o, n, float(arrivals[i]))
+        o += n * len(wr)
+        w += len(wr)
+    tl = args.batch_tlsz or 64
+    srv = hsr.Server(hbm_budget_bytes=args.budget_gb * 1e9, tlsz=tl)
+    lat = (C.c_double * len(reqs))()
+    st = (C.c_int * len(reqs))()
+    stats = _lib.ServerStats()
+    with ClockSampler(0) as clk:
+        rc = lib.hsr_server_replay(srv._h, len(reqs), arr, lat, st, C.byref(stats))
+    if rc < 0:
+        raise RuntimeError("server replay failed: %d" % rc)
+    lat = np.array(lat[:])
+    served = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+              "eigenvectors_per_s": total / stats.wall_s, "wall_s": stats.wall_s, "ticks": stats.ticks,
+              "max_active": stats.max_active, "peak_pool_gb": stats.peak_bytes / 1e9}
+    # the plain path, one request at a time in arrival order (first 120 requests)
+    k = min(120, len(reqs))
+    t0 = time.perf_counter()
+    done = []
+    for i in range(k):
+        j, n, wr = reqs[i]
+        now = time.perf_counter() - t0
+        if now < arrivals[i]:
+            time.sleep(arrivals[i] - now)
+        H = base[j][0]
+        hsr.inverse_iteration(H, wr, tl, 64)
+        done.append(time.perf_counter() - t0 - arrivals[i])
+    plain = {"requests": k, "p50_s": float(np.percentile(done, 50)), "p99_s": float(np.percentile(done, 99)),
+             "eigenvectors_per_s": sum(len(reqs[i][2]) for i in range(k)) / (time.perf_counter() - t0)}
+    return {"metric": "served eigenvectors/s with p50/p99 latency", "value": served["eigenvectors_per_s"],
+            "unit": "eigenvectors/s", "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": stats.wall_s * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generator)",
+            "config": {"workload": "served: %d Poisson requests at %.0f/s, n log-uniform [64,4096] from %d "
+                                   "distinct generated matrices, shift fraction U[0.1,1], HBM budget %.0f GB"
+                                   % (len(reqs), args.rate, len(base), args.budget_gb), "tlsz": tl},
+            "served": served, "plain_per_request": plain, "clocks": clk.summary()}
+
+
 def main():
     args = parse()
+    if args.workload != "plain":
+        line = run_batched(args) if args.workload == "batched" else run_served(args)
+        print(json.dumps(line), flush=True)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:

@@ -86,13 +86,15 @@ def inverse_iteration(H: np.ndarray, wr: np.ndarray, tlsz: int, rhs_tlsz: int = 
 
 def inverse_iteration_device(dH, dwr, dvr, tlsz: int, stream=None, scaling: str = "pow2",
                              user_rhs: bool = False, d_status=None, d_scale=None) -> int:
-    """Device-resident call on torch tensors (column-major views: pass
-    tensors whose .T is contiguous, i.e. created as (cols, rows) and
-    transposed).  Returns the status code."""
+    """Device-resident call on torch tensors.  Column-major blocks are passed
+    as tensors of shape (columns, ld) whose rows are the columns: dH is
+    (n, ldh), dvr is (nrhs, ldvr), as BatchPlan takes them.  Returns the
+    status code (0, or 1 when some columns did not converge); raises on
+    errors."""
     lib = _lib.load()
     n = dH.shape[0]
-    ldh = dH.stride(1)
-    ldv = dvr.stride(1)
+    ldh = dH.stride(0)
+    ldv = dvr.stride(0)
     nrhs = dwr.shape[0]
     opt = _lib.Options(_scaling(scaling), int(bool(user_rhs)), -1, 0.0)
     st = None if stream is None else C.c_void_p(stream.cuda_stream)
@@ -100,6 +102,8 @@ def inverse_iteration_device(dH, dwr, dvr, tlsz: int, stream=None, scaling: str 
                                           dvr.data_ptr(), ldv, C.byref(opt), st,
                                           None if d_status is None else d_status.data_ptr(),
                                           None if d_scale is None else d_scale.data_ptr())
+    if rc < 0:
+        raise HsrError(rc)
     return rc
 
 

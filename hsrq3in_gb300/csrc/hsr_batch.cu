@@ -168,13 +168,7 @@ struct TickLists {
 
 void add_setup(TickLists &tl, int slot, const Layout &L, const std::vector<int> &fr) {
     const int rb = (L.n + kNormRows - 1) / kNormRows;
-    for (int r = 0; r < rb; ++r) {
-        tl.v[phNorms].push_back(make_int4(slot, -1, r, 0));
-        const int row0 = r * kNormRows;
-        int I0 = L.T - 1 - (L.n - 1 - row0) / L.b;
-        if (I0 < 0) I0 = 0;
-        for (int J = I0; J < L.T; ++J) tl.v[phNorms].push_back(make_int4(slot, J, r, 0));
-    }
+    for (int r = 0; r < rb; ++r) tl.v[phNorms].push_back(make_int4(slot, 0, r, 0));
     for (int k = 0; k < L.S; ++k) tl.v[phInit].push_back(make_int4(slot, 0, k, 0));
     (void)fr;
 }
@@ -184,8 +178,7 @@ void add_stage(TickLists &tl, int slot, const Layout &L, const std::vector<int> 
     for (int x = 0; x < sb32; ++x) tl.v[phDiag].push_back(make_int4(slot, J, x, 0));
     if (J >= 1) {
         const int sb8 = (L.S + 7) / 8;
-        for (int I = 0; I < J; ++I)
-            for (int x = 0; x < sb8; ++x) tl.v[phPart1].push_back(make_int4(slot, J, I, x));
+        for (int x = 0; x < sb8; ++x) tl.v[phPart1].push_back(make_int4(slot, J, x, 0));
         const int rbs = (fr[J] + kGemmBM - 1) / kGemmBM;
         const int cbs = (L.S + kGemmBN - 1) / kGemmBN;
         for (int r = 0; r < rbs; ++r)

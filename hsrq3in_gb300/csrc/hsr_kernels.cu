@@ -865,6 +865,9 @@ cudaError_t launch_gather_cols(double *dst, long long ldd, const double *src, lo
 // same body as the single-problem kernel, so a column computes exactly what
 // it computes when its problem is solved alone.
 
+// One pass per row: the row sum over all columns (||H||_oo) and, at every
+// tile boundary at or right of the row's own tile, that tile's row sum; each
+// sum accumulates its columns in order, as dlange does.
 __global__ void k_norms_b(const DevProblem *probs, const BatchItem *items) {
     const BatchItem it = items[blockIdx.x];
     const DevProblem &P = probs[it.x];
@@ -872,22 +875,25 @@ __global__ void k_norms_b(const DevProblem *probs, const BatchItem *items) {
     if (i >= P.n || threadIdx.x >= kNormRows) return;
     const double *row = P.H + i;
     const int T = P.T;
-    if (it.y < 0) {
-        double sum = 0.0;
-        for (int c = 0; c < P.n; ++c) sum += fabs(row[(size_t)c * P.ldh]);
-        if (sum != sum) atomicOr(P.nanflag, 1);
-        atomicMax(&P.nbits[2 * (size_t)T * T], (unsigned long long)__double_as_longlong(sum));
-        return;
-    }
-    const int J = it.y;
     int I = T - 1 - (P.n - 1 - i) / P.tlsz;
     if (I < 0) I = 0;
-    if (J < I) return;
-    const int c0 = P.fr[J], c1 = P.fr[J + 1];
-    double sum = 0.0;
-    for (int c = c0; c < c1; ++c) sum += fabs(row[(size_t)c * P.ldh]);
-    atomicMax(&P.nbits[I + (size_t)J * T], (unsigned long long)__double_as_longlong(sum));
-    if (J > I) atomicMax(&P.nbits[(size_t)T * T + I + (size_t)J * T], abs_bits(row[(size_t)(c0 - 1) * P.ldh]));
+    double full = 0.0;
+    for (int J = 0; J < T; ++J) {
+        const int c0 = P.fr[J], c1 = P.fr[J + 1];
+        double tsum = 0.0;
+        for (int c = c0; c < c1; ++c) {
+            const double a = fabs(row[(size_t)c * P.ldh]);
+            full += a;
+            tsum += a;
+        }
+        if (J >= I) {
+            atomicMax(&P.nbits[I + (size_t)J * T], (unsigned long long)__double_as_longlong(tsum));
+            if (J > I)
+                atomicMax(&P.nbits[(size_t)T * T + I + (size_t)J * T], abs_bits(row[(size_t)(c0 - 1) * P.ldh]));
+        }
+    }
+    if (full != full) atomicOr(P.nanflag, 1);
+    atomicMax(&P.nbits[2 * (size_t)T * T], (unsigned long long)__double_as_longlong(full));
 }
 
 // Start vector eps3 = ||H||_oo * eps/2 (inverse_iteration.c:154-158, 19-34),
@@ -921,9 +927,11 @@ __global__ void __launch_bounds__(32 * kDiagWarps) k_diag_b(const DevProblem *pr
     diag_body(probs[it.x], it.y, it.z, nullptr);
 }
 
+// One block per (problem, stage, 8 shifts); the tiles above the diagonal
+// tile are visited in turn.
 __global__ void __launch_bounds__(256) k_part1_b(const DevProblem *probs, const BatchItem *items) {
     const BatchItem it = items[blockIdx.x];
-    part1_body(probs[it.x], it.y, it.z, it.w);
+    for (int I = 0; I < it.y; ++I) part1_body(probs[it.x], it.y, I, it.z);
 }
 
 __global__ void __launch_bounds__(256, 2) k_gemm_b(const DevProblem *probs, const BatchItem *items,

@@ -76,10 +76,10 @@ cudaError_t launch_gather_cols(double *dst, long long ldd, const double *src,
                                long long lds, int n, const int *perm, int cnt,
                                cudaStream_t st);
 // Batched kernels: one launch covers work items of many problems.
-//   norms:    (p, J, row block, 0)       J = -1: full row sums for ||H||_oo
+//   norms:    (p, 0, row block, 0)       row sums over all columns and per tile
 //   init:     (p, 0, column, 0)          start vector eps3 (from the norms)
 //   diag:     (p, J, shift block, 0)
-//   part1:    (p, J, tile I, shift block of 8)
+//   part1:    (p, J, shift block of 8, 0) over all tiles I < J
 //   gemm:     (p, J, row block, column block) over rows [0, fr[J])
 //   finalize: (p, 0, shift block, 0)
 //   normalize:(p, 0, column block of 8, 0)
