@@ -73,6 +73,8 @@ def parse():
     ap.add_argument("--pool", type=int, default=48, help="served: distinct generated matrices")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="served: HBM budget")
     ap.add_argument("--batch-tlsz", type=int, default=0, help="batched/served tile size (0: autotune)")
+    ap.add_argument("--only-plain", action="store_true",
+                    help="default run: skip the batched and served sub-measurements")
     return ap.parse_args()
 
 
@@ -420,82 +422,128 @@ def run_batched(args):
             "clocks": clk.summary()}
 
 
-def run_served(args):
-    """Config 5: a Poisson trace of requests through the request loop."""
-    import torch
-    import hsrq3in_gb300 as hsr
+def served_pool(args):
+    """Distinct served matrices (n log-uniform [64, 4096], all eigenvalues),
+    generated once per host and cached in the temp directory."""
+    d = os.path.join(tempfile.gettempdir(), "hsrq3in_bench")
+    os.makedirs(d, exist_ok=True)
+    f = os.path.join(d, "served_pool_%d_s%d_v1.npz" % (args.pool, args.seed))
+    if os.path.exists(f):
+        z = np.load(f)
+        return [(np.asfortranarray(z["H%d" % i]), z["w%d" % i]) for i in range(args.pool)]
     base = mixed_problems(args.pool, 64, 4096, 1.0, 1.0, args.seed + 1)
-    rng = np.random.default_rng(args.seed + 2)
-    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, args.requests))
-    arrivals -= arrivals[0]
-    # pinned host buffers: each pool matrix once; outputs per request
-    Hp = []
-    for H, _ in base:
-        t = torch.from_numpy(np.asfortranarray(H).ravel(order="F")).pin_memory()
-        Hp.append((t, H.shape[0]))
+    tmp = f + ".%d.tmp.npz" % os.getpid()
+    np.savez(tmp, **{("H%d" % i): H for i, (H, _) in enumerate(base)},
+             **{("w%d" % i): w for i, (_, w) in enumerate(base)})
+    os.replace(tmp, f)
+    return base
+
+
+def served_trace(args, base, nreq, rate, seed):
+    """Requests drawing a pool matrix and a random 10-100% subset of its
+    eigenvalues; Poisson arrivals at `rate` per second (rate 0: all at t=0)."""
+    rng = np.random.default_rng(seed)
+    if rate > 0:
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+        arrivals -= arrivals[0]
+    else:
+        arrivals = np.zeros(nreq)
     reqs = []
-    total = 0
-    for i in range(args.requests):
+    for i in range(nreq):
         j = int(rng.integers(len(base)))
         H, lam = base[j]
         n = H.shape[0]
         m = max(1, int(round(n * rng.uniform(0.1, 1.0))))
-        wr = np.sort(rng.choice(lam, size=m, replace=False))
-        total += m
-        reqs.append((j, n, wr))
-    outs = torch.empty(sum(n * len(wr) for _, n, wr in reqs), dtype=torch.float64).pin_memory()
-    wrs = torch.empty(total, dtype=torch.float64).pin_memory()
-    lib = hsr.load()
+        reqs.append((j, n, np.sort(rng.choice(lam, size=m, replace=False)), float(arrivals[i])))
+    return reqs
+
+
+def replay_served(base, reqs, tl, budget_gb):
+    """Replay a trace through the request loop; pinned host buffers."""
+    import torch
+    import hsrq3in_gb300 as hsr
     from hsrq3in_gb300 import _lib
+    lib = hsr.load()
+    Hp = [torch.from_numpy(np.asfortranarray(H).ravel(order="F")).pin_memory() for H, _ in base]
+    total = sum(len(wr) for _, _, wr, _ in reqs)
+    outs = torch.empty(sum(n * len(wr) for _, n, wr, _ in reqs), dtype=torch.float64).pin_memory()
+    wrs = torch.empty(total, dtype=torch.float64).pin_memory()
     arr = (_lib.Request * len(reqs))()
     o = w = 0
-    for i, (j, n, wr) in enumerate(reqs):
+    for i, (j, n, wr, t) in enumerate(reqs):
         wrs.numpy()[w:w + len(wr)] = wr
-        arr[i] = _lib.Request(n, Hp[j][0].data_ptr(), n, len(wr), wrs.data_ptr() + 8 * w,
-                              outs.data_ptr() + 8 * o, n, float(arrivals[i]))
+        arr[i] = _lib.Request(n, Hp[j].data_ptr(), n, len(wr), wrs.data_ptr() + 8 * w, outs.data_ptr() + 8 * o,
+                              n, t)
         o += n * len(wr)
         w += len(wr)
-    tl = args.batch_tlsz or 64
-    srv = hsr.Server(hbm_budget_bytes=args.budget_gb * 1e9, tlsz=tl)
+    srv = hsr.Server(hbm_budget_bytes=budget_gb * 1e9, tlsz=tl)
     lat = (C.c_double * len(reqs))()
     st = (C.c_int * len(reqs))()
     stats = _lib.ServerStats()
-    with ClockSampler(0) as clk:
-        rc = lib.hsr_server_replay(srv._h, len(reqs), arr, lat, st, C.byref(stats))
+    rc = lib.hsr_server_replay(srv._h, len(reqs), arr, lat, st, C.byref(stats))
+    srv.close()
     if rc < 0:
         raise RuntimeError("server replay failed: %d" % rc)
     lat = np.array(lat[:])
-    served = {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
-              "eigenvectors_per_s": total / stats.wall_s, "wall_s": stats.wall_s, "ticks": stats.ticks,
-              "max_active": stats.max_active, "peak_pool_gb": stats.peak_bytes / 1e9}
-    # the plain path, one request at a time in arrival order (first 120 requests)
-    k = min(120, len(reqs))
+    return {"requests": len(reqs), "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "eigenvectors_per_s": total / stats.wall_s, "wall_s": stats.wall_s, "ticks": stats.ticks,
+            "launches": stats.launches, "max_active": stats.max_active, "peak_pool_gb": stats.peak_bytes / 1e9}
+
+
+def plain_served(base, reqs, tl, limit_s=12.0):
+    """The plain path, one request at a time in arrival order, through the
+    drop-in entry point; stops after limit_s."""
+    import hsrq3in_gb300 as hsr
     t0 = time.perf_counter()
-    done = []
-    for i in range(k):
-        j, n, wr = reqs[i]
+    lat, shifts, k = [], 0, 0
+    for (j, n, wr, t) in reqs:
         now = time.perf_counter() - t0
-        if now < arrivals[i]:
-            time.sleep(arrivals[i] - now)
-        H = base[j][0]
-        hsr.inverse_iteration(H, wr, tl, 64)
-        done.append(time.perf_counter() - t0 - arrivals[i])
-    plain = {"requests": k, "p50_s": float(np.percentile(done, 50)), "p99_s": float(np.percentile(done, 99)),
-             "eigenvectors_per_s": sum(len(reqs[i][2]) for i in range(k)) / (time.perf_counter() - t0)}
-    return {"metric": "served eigenvectors/s with p50/p99 latency", "value": served["eigenvectors_per_s"],
-            "unit": "eigenvectors/s", "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": stats.wall_s * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded generator)",
-            "config": {"workload": "served: %d Poisson requests at %.0f/s, n log-uniform [64,4096] from %d "
-                                   "distinct generated matrices, shift fraction U[0.1,1], HBM budget %.0f GB"
-                                   % (len(reqs), args.rate, len(base), args.budget_gb), "tlsz": tl},
-            "served": served, "plain_per_request": plain, "clocks": clk.summary()}
+        if now > limit_s:
+            break
+        if now < t:
+            time.sleep(t - now)
+        hsr.inverse_iteration(base[j][0], wr, tl, 64)
+        lat.append(time.perf_counter() - t0 - t)
+        shifts += len(wr)
+        k += 1
+    wall = time.perf_counter() - t0
+    return {"requests": k, "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "eigenvectors_per_s": shifts / wall}
+
+
+def run_served(args):
+    """Config 5: a Poisson trace through the request loop (latency at the
+    configured rate), and the same request mix arriving at once (capacity);
+    each against the plain path run per request."""
+    base = served_pool(args)
+    tl = args.batch_tlsz or 64
+    with ClockSampler(0) as clk:
+        paced = served_trace(args, base, args.requests, args.rate, args.seed + 2)
+        r_paced = replay_served(base, paced, tl, args.budget_gb)
+        burst = served_trace(args, base, args.requests, 0.0, args.seed + 3)
+        r_burst = replay_served(base, burst, tl, args.budget_gb)
+    p_paced = plain_served(base, paced, tl)
+    p_burst = plain_served(base, burst, tl)
+    return {"paced": {"rate_per_s": args.rate, "server": r_paced, "plain_per_request": p_paced},
+            "saturated": {"server": r_burst, "plain_per_request": p_burst,
+                          "speedup_server_over_plain": r_burst["eigenvectors_per_s"] / p_burst["eigenvectors_per_s"]},
+            "config": "%d requests, n log-uniform [64,4096] from %d distinct generated matrices, shift fraction "
+                      "U[0.1,1], HBM budget %.0f GB, tlsz %d" % (args.requests, len(base), args.budget_gb, tl),
+            "clocks": clk.summary()}
 
 
 def main():
     args = parse()
-    if args.workload != "plain":
-        line = run_batched(args) if args.workload == "batched" else run_served(args)
+    if args.workload == "batched":
+        print(json.dumps(run_batched(args)), flush=True)
+        return
+    if args.workload == "served":
+        sv = run_served(args)
+        line = {"metric": "served eigenvectors/s with p50/p99 latency",
+                "value": sv["saturated"]["server"]["eigenvectors_per_s"], "unit": "eigenvectors/s",
+                "n_gpus": 1, "steps": 1, "warmup": 0, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+                "config": {"workload": "served: " + sv["config"]}, "served": sv}
         print(json.dumps(line), flush=True)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -545,6 +593,13 @@ def main():
               "whole_solve_tflops_2n2S", "whole_solve_frac", "check"):
         if k in g:
             line[k] = g[k]
+    if rank == 0 and world == 1 and not args.only_plain:
+        b = run_batched(args)
+        line["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "solves_per_s", "whole_tflops_2n2S",
+                                              "frac_of_fp64_peak", "plain_loop", "check")}
+        line["batched"]["config"] = b["config"]
+        sv = run_served(args)
+        line["served"] = sv
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, t, c = cpu_sample(H, wr, args.tlsz, args.rhs_tlsz, sample, 1, 0)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": c, "kind": "port",

@@ -535,18 +535,22 @@ int host_call(int n, const double *H, int ldH, int nrhs, double *wr, int tlsz, i
     Workspace &w = ws();
     if (!w.stream) HSR_CK(cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking));
     cudaStream_t st = w.stream;
-    const long long ldh = round_up(n, 32);
-    const long long ldx = round_up(n, 32);
+    // Keep the caller's leading dimensions on the device when they allow it
+    // (TMA needs an even pitch for H), so each transfer is one contiguous copy.
+    const long long ldh = (ldH % 2 == 0) ? ldH : round_up(n, 32);
+    const long long ldx = ldvr;
     HSR_CK(w.H.ensure((size_t)ldh * n * 8));
     HSR_CK(w.X.ensure((size_t)ldx * nrhs * 8));
     HSR_CK(w.wr.ensure((size_t)nrhs * 8));
-    HSR_CK(cudaMemcpy2DAsync(w.H.p, ldh * 8, H, (size_t)ldH * 8, (size_t)n * 8, n, cudaMemcpyHostToDevice, st));
+    if (ldh == ldH)
+        HSR_CK(cudaMemcpyAsync(w.H.p, H, ((size_t)ldH * (n - 1) + n) * 8, cudaMemcpyHostToDevice, st));
+    else
+        HSR_CK(cudaMemcpy2DAsync(w.H.p, ldh * 8, H, (size_t)ldH * 8, (size_t)n * 8, n, cudaMemcpyHostToDevice, st));
     HSR_CK(cudaMemcpyAsync(w.wr.p, wr, (size_t)nrhs * 8, cudaMemcpyHostToDevice, st));
     hsr_options o{};
     if (opt) o = *opt;
     if (o.user_rhs)
-        HSR_CK(cudaMemcpy2DAsync(w.X.p, ldx * 8, vr, (size_t)ldvr * 8, (size_t)n * 8, nrhs,
-                                 cudaMemcpyHostToDevice, st));
+        HSR_CK(cudaMemcpyAsync(w.X.p, vr, ((size_t)ldvr * (nrhs - 1) + n) * 8, cudaMemcpyHostToDevice, st));
     std::vector<int> hs;
     std::vector<unsigned char> hp;
     std::vector<double> hsc, hn, hts;
@@ -556,7 +560,11 @@ int host_call(int n, const double *H, int ldH, int nrhs, double *wr, int tlsz, i
                       want && info->perturbed ? &hp : nullptr, want && info->scale ? &hsc : nullptr,
                       want && info->norm ? &hn : nullptr, want && info->tile_scales ? &hts : nullptr);
     if (rc < 0) return rc;
-    HSR_CK(cudaMemcpy2DAsync(vr, (size_t)ldvr * 8, w.X.p, ldx * 8, (size_t)n * 8, nrhs, cudaMemcpyDeviceToHost, st));
+    if (ldvr == n)   // no padding rows in the caller's block: one contiguous copy
+        HSR_CK(cudaMemcpyAsync(vr, w.X.p, (size_t)n * nrhs * 8, cudaMemcpyDeviceToHost, st));
+    else             // leave the caller's padding rows untouched
+        HSR_CK(cudaMemcpy2DAsync(vr, (size_t)ldvr * 8, w.X.p, ldx * 8, (size_t)n * 8, nrhs,
+                                 cudaMemcpyDeviceToHost, st));
     HSR_CK(cudaMemcpyAsync(wr, w.wr.p, (size_t)nrhs * 8, cudaMemcpyDeviceToHost, st));
     HSR_CK(cudaStreamSynchronize(st));
     if (want) {
