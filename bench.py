@@ -245,8 +245,8 @@ def run_gpu(args, H, wr, rank, world):
     torch.cuda.synchronize()
     dfma, dmma = hsr.fp64_peak(200.0)          # after warm-up: clocks ramped
     lib.hsr_set_kernel_timing(1)
-    kms = np.zeros(6)
-    kl = np.zeros(6, dtype=np.int64)
+    kms = np.zeros(8)
+    kl = np.zeros(8, dtype=np.int64)
     gemm_fma = 0.0
     launches = 0
     if world > 1:
@@ -261,8 +261,8 @@ def run_gpu(args, H, wr, rank, world):
             rcs = []
             for _ in range(args.steps):
                 rcs.append(step())
-                ms = (C.c_double * 6)()
-                ln = (C.c_long * 6)()
+                ms = (C.c_double * 8)()
+                ln = (C.c_long * 8)()
                 fm = C.c_double()
                 lib.hsr_last_kernel_times(ms, ln, C.byref(fm))
                 kms += np.array(ms[:])
@@ -337,7 +337,14 @@ def run_gpu(args, H, wr, rank, world):
             tt = torch.tensor([te], device=dev)
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
             te = float(tt.item())
+        lib.hsr_set_kernel_timing(1)
+        e2e_step()
+        torch.cuda.synchronize()
+        ms8 = (C.c_double * 8)()
+        lib.hsr_last_kernel_times(ms8, None, None)
+        lib.hsr_set_kernel_timing(0)
         out["e2e"] = {"value": world * S / te, "unit": UNIT, "h2d_bytes_per_step": 8 * (n * n + S),
+                      "kernel_ms_one_step": {k: round(ms8[i], 2) for i, k in enumerate(_lib.KERNEL_CLASSES)},
                       "d2h_bytes_per_step": 8 * (n * S + S), "ms_per_step": te * 1e3,
                       "api": "tiled_inverse_iteration (C ABI, pinned host buffers)"}
     return out
@@ -487,7 +494,9 @@ def replay_served(base, reqs, tl, budget_gb):
     lat = np.array(lat[:])
     return {"requests": len(reqs), "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
             "eigenvectors_per_s": total / stats.wall_s, "wall_s": stats.wall_s, "ticks": stats.ticks,
-            "launches": stats.launches, "max_active": stats.max_active, "peak_pool_gb": stats.peak_bytes / 1e9}
+            "launches": stats.launches, "max_active": stats.max_active, "peak_pool_gb": stats.peak_bytes / 1e9,
+            "tflops_2n2S": stats.flops / stats.wall_s / 1e12,
+            "phase_ms": {k: round(stats.phase_ms[i], 2) for i, k in enumerate(_lib.SERVER_PHASES)}}
 
 
 def plain_served(base, reqs, tl, limit_s=12.0):

@@ -33,7 +33,9 @@ EXPORTS = [
 ]
 NOALLOC_MAX_N = 256
 NOALLOC_MAX_NRHS = 256
-KERNEL_CLASSES = ["setup", "diag", "part1", "gemm", "finalize", "other"]
+KERNEL_CLASSES = ["setup", "diag", "part1", "gemm", "finalize", "other", "h2d", "d2h"]
+SERVER_PHASES = ["norms", "init", "diag_first", "part1", "gemm_top", "diag_next", "gemm_rest", "finalize",
+                 "normalize"]
 
 
 class Options(C.Structure):
@@ -64,7 +66,8 @@ class Request(C.Structure):
 
 class ServerStats(C.Structure):
     _fields_ = [("wall_s", C.c_double), ("ticks", C.c_long), ("launches", C.c_long),
-                ("max_active", C.c_int), ("peak_bytes", C.c_double)]
+                ("max_active", C.c_int), ("peak_bytes", C.c_double), ("phase_ms", C.c_double * 9),
+                ("flops", C.c_double), ("host_wait_s", C.c_double)]
 
 
 _LIB = None

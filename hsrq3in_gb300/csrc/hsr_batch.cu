@@ -1,12 +1,14 @@
 // hsr_batch.cu -- batched and served solves: many problems, one tick at a time.
 //
 // A problem with T row tiles needs T stages (J = T-1 .. 0).  Problems start
-// at their own tick and each tick advances every active problem by one stage:
-// one batched launch per phase (diagonal, part 1, GEMM, finalize, normalize)
-// covers the work items of all problems, so thousands of small problems fill
-// the GPU together.  Each work item runs the single-problem kernel body, so
-// every column computes exactly what it computes when its problem is solved
-// alone with the same tile size.
+// at their own tick and each tick advances every active problem by one stage,
+// with the single-problem look-ahead: part 1 of stage J, the GEMM rows of
+// tile J-1, then the diagonal solve of tile J-1 on a side stream while the
+// GEMM rows above tile J-1 run on the main stream.  One batched launch per
+// phase covers the work items of all problems, so thousands of small
+// problems fill the GPU together.  Each work item runs the single-problem
+// kernel body, so every column computes exactly what it computes when its
+// problem is solved alone with the same tile size.
 //
 //   batched (hsr_batch_plan_*): all problems start at tick 0; the whole tick
 //     sequence, with its work lists already on the device, is captured once
@@ -73,9 +75,11 @@ struct Layout {
         Sr = take((size_t)n * Sp * 8);
         beta = take((size_t)T * Sp * 8);
         ynorm = take((size_t)T * Sp * 8);
-        W = take((size_t)b * Sp * 8);
-        Zs = take((size_t)b * Sp * 8);
-        vecs = take(4 * Sp * 8);
+        // Stage operands, two copies (even and odd tiles): the diagonal solve
+        // of tile J-1 writes one while the GEMM of stage J reads the other.
+        W = take(2 * (size_t)b * Sp * 8);
+        Zs = take(2 * (size_t)b * Sp * 8);
+        vecs = take(2 * 4 * Sp * 8);
         Zslow = take((size_t)T * b * Sp * 8);
         slow = take((size_t)T * Sp);
         pert = take(Sp);
@@ -98,9 +102,11 @@ double smlnum_for(int n) {
     return std::fmax(2 * DBL_MIN, DBL_MIN * ((double)n / eps));
 }
 
-// DevProblem of one problem whose workspace starts at `base`.
+// DevProblem of one problem whose workspace starts at `base`, with the stage
+// operands of tiles of the given parity.
 DevProblem make_problem(const Layout &L, char *base, const double *H, long long ldh, double *wr, double *X,
-                        long long ldx, int is, int *err) {
+                        long long ldx, int is, int *err, int parity) {
+    const size_t stage = (size_t)L.b * L.Spad;
     DevProblem P{};
     P.n = L.n;
     P.T = L.T;
@@ -122,9 +128,9 @@ DevProblem make_problem(const Layout &L, char *base, const double *H, long long 
     P.nbits = reinterpret_cast<unsigned long long *>(base + L.nbits);
     P.Hn = reinterpret_cast<const double *>(P.nbits);
     P.hn = reinterpret_cast<const double *>(P.nbits + (size_t)L.T * L.T);
-    P.W = reinterpret_cast<double *>(base + L.W);
-    P.Zs = reinterpret_cast<double *>(base + L.Zs);
-    double *v = reinterpret_cast<double *>(base + L.vecs);
+    P.W = reinterpret_cast<double *>(base + L.W) + parity * stage;
+    P.Zs = reinterpret_cast<double *>(base + L.Zs) + parity * stage;
+    double *v = reinterpret_cast<double *>(base + L.vecs) + parity * 4 * (size_t)L.Spad;
     P.pi = v;
     P.ytil = v + L.Spad;
     P.z2n = v + 2 * (size_t)L.Spad;
@@ -142,17 +148,27 @@ DevProblem make_problem(const Layout &L, char *base, const double *H, long long 
     return P;
 }
 
-bool make_maps(CUtensorMap *m, const Layout &L, const double *H, long long ldh, char *base) {
+bool make_maps(CUtensorMap *m, const Layout &L, const double *H, long long ldh, char *base, int parity) {
+    const size_t stage = (size_t)L.b * L.Spad;
     return encode_tensor_map(&m[0], H, (unsigned long long)L.n, (unsigned long long)L.n,
                              (unsigned long long)ldh, kGemmBM, kGemmKC) &&
-           encode_tensor_map(&m[1], reinterpret_cast<const double *>(base + L.W), (unsigned long long)L.Spad,
-                             (unsigned long long)L.b, (unsigned long long)L.Spad, kGemmBN, kGemmKC) &&
-           encode_tensor_map(&m[2], reinterpret_cast<const double *>(base + L.Zs), (unsigned long long)L.Spad,
+           encode_tensor_map(&m[1], reinterpret_cast<const double *>(base + L.W) + parity * stage,
+                             (unsigned long long)L.Spad, (unsigned long long)L.b, (unsigned long long)L.Spad,
+                             kGemmBN, kGemmKC) &&
+           encode_tensor_map(&m[2], reinterpret_cast<const double *>(base + L.Zs) + parity * stage,
+                             (unsigned long long)L.Spad,
                              (unsigned long long)L.b, (unsigned long long)L.Spad, kGemmBN, kGemmKC);
 }
 
 // ----------------------------------------------------------- work lists
-enum Phase { phNorms = 0, phInit, phDiag, phPart1, phGemm, phFinal, phNormalize, phCount };
+// Phases of a tick in launch order.  phDiagNext runs on the side stream,
+// after phGemmTop and concurrently with phGemmRest.
+enum Phase {
+    phNorms = 0, phInit, phDiagFirst, phPart1, phGemmTop, phDiagNext, phGemmRest, phFinal, phNormalize, phCount
+};
+
+// Descriptor of a problem slot for the stage operands of tiles of parity J.
+inline int desc(int slot, int J) { return 2 * slot + (J & 1); }
 
 struct TickLists {
     std::vector<BatchItem> v[phCount];
@@ -166,28 +182,38 @@ struct TickLists {
     }
 };
 
-void add_setup(TickLists &tl, int slot, const Layout &L, const std::vector<int> &fr) {
+// Setup of a new problem: norms, start vectors, diagonal solve of tile T-1.
+void add_setup(TickLists &tl, int slot, const Layout &L) {
     const int rb = (L.n + kNormRows - 1) / kNormRows;
-    for (int r = 0; r < rb; ++r) tl.v[phNorms].push_back(make_int4(slot, 0, r, 0));
-    for (int k = 0; k < L.S; ++k) tl.v[phInit].push_back(make_int4(slot, 0, k, 0));
-    (void)fr;
+    for (int r = 0; r < rb; ++r) tl.v[phNorms].push_back(make_int4(desc(slot, 0), 0, r, 0));
+    for (int k = 0; k < L.S; ++k) tl.v[phInit].push_back(make_int4(desc(slot, 0), 0, k, 0));
+    const int J = L.T - 1, sb32 = (L.S + 31) / 32;
+    for (int x = 0; x < sb32; ++x) tl.v[phDiagFirst].push_back(make_int4(desc(slot, J), J, x, 0));
 }
 
-void add_stage(TickLists &tl, int slot, const Layout &L, const std::vector<int> &fr, int J) {
+// One tick of a problem whose diagonal tile J is solved: part 1 and the GEMM
+// of stage J, the diagonal solve of tile J-1, and at the end finalize and
+// normalize.  Returns true when the problem finishes in this tick.
+bool add_stage(TickLists &tl, int slot, const Layout &L, const std::vector<int> &fr, int J) {
     const int sb32 = (L.S + 31) / 32;
-    for (int x = 0; x < sb32; ++x) tl.v[phDiag].push_back(make_int4(slot, J, x, 0));
     if (J >= 1) {
-        const int sb8 = (L.S + 7) / 8;
-        for (int x = 0; x < sb8; ++x) tl.v[phPart1].push_back(make_int4(slot, J, x, 0));
-        const int rbs = (fr[J] + kGemmBM - 1) / kGemmBM;
+        const int p = desc(slot, J), pn = desc(slot, J - 1);
+        const int sbp = (L.S + kPart1Shifts - 1) / kPart1Shifts;
+        for (int x = 0; x < sbp; ++x) tl.v[phPart1].push_back(make_int4(p, J, x, 0));
         const int cbs = (L.S + kGemmBN - 1) / kGemmBN;
-        for (int r = 0; r < rbs; ++r)
-            for (int c = 0; c < cbs; ++c) tl.v[phGemm].push_back(make_int4(slot, J, r, c));
-    } else {
-        for (int x = 0; x < sb32; ++x) tl.v[phFinal].push_back(make_int4(slot, 0, x, 0));
-        const int cb = (L.S + kNormalizeCols - 1) / kNormalizeCols;
-        for (int x = 0; x < cb; ++x) tl.v[phNormalize].push_back(make_int4(slot, 0, x, 0));
+        const int top = (fr[J] - (fr[J - 1] & ~7) + kGemmBM - 1) / kGemmBM;
+        for (int r = 0; r < top; ++r)
+            for (int c = 0; c < cbs; ++c) tl.v[phGemmTop].push_back(make_int4(p, J, r | kGemmTopFlag, c));
+        for (int x = 0; x < sb32; ++x) tl.v[phDiagNext].push_back(make_int4(pn, J - 1, x, 0));
+        const int rest = (fr[J - 1] + kGemmBM - 1) / kGemmBM;
+        for (int r = 0; r < rest; ++r)
+            for (int c = 0; c < cbs; ++c) tl.v[phGemmRest].push_back(make_int4(p, J, r, c));
     }
+    if (J > 1) return false;
+    for (int x = 0; x < sb32; ++x) tl.v[phFinal].push_back(make_int4(desc(slot, 0), 0, x, 0));
+    const int cb = (L.S + kNormalizeCols - 1) / kNormalizeCols;
+    for (int x = 0; x < cb; ++x) tl.v[phNormalize].push_back(make_int4(desc(slot, 0), 0, x, 0));
+    return true;
 }
 
 cudaError_t launch_phase(int ph, const DevProblem *probs, const BatchItem *items, int count, int bmax,
@@ -195,13 +221,83 @@ cudaError_t launch_phase(int ph, const DevProblem *probs, const BatchItem *items
     switch (ph) {
     case phNorms: return launch_norms_b(probs, items, count, st);
     case phInit: return launch_init_b(probs, items, count, st);
-    case phDiag: return launch_diag_b(probs, items, count, bmax, st);
+    case phDiagFirst:
+    case phDiagNext: return launch_diag_b(probs, items, count, bmax, st);
     case phPart1: return launch_part1_b(probs, items, count, st);
-    case phGemm: return launch_gemm_b(probs, items, count, maps, st);
+    case phGemmTop:
+    case phGemmRest: return launch_gemm_b(probs, items, count, maps, st);
     case phFinal: return launch_finalize_b(probs, items, count, st);
     case phNormalize: return launch_normalize_b(probs, items, count, st);
     }
     return cudaErrorInvalidValue;
+}
+
+// Items of one tick, by phase: [off, off + cnt) of the item array.
+struct PhaseSpan {
+    size_t off = 0;
+    int cnt = 0;
+};
+
+// Copies a tick's lists into `dst` (phase order) and records their spans.
+void pack_tick(const TickLists &tl, BatchItem *dst, size_t base, PhaseSpan *sp) {
+    size_t off = 0;
+    for (int ph = 0; ph < phCount; ++ph) {
+        sp[ph].off = base + off;
+        sp[ph].cnt = (int)tl.v[ph].size();
+        if (!tl.v[ph].empty()) memcpy(dst + off, tl.v[ph].data(), sizeof(BatchItem) * tl.v[ph].size());
+        off += tl.v[ph].size();
+    }
+}
+
+// Optional device timing of the phases: an event pair around every launch.
+struct PhaseTimer {
+    std::vector<cudaEvent_t> ev;
+    std::vector<std::pair<int, size_t>> starts;   // (phase, index of its start event)
+    size_t record(cudaStream_t st) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        cudaEventRecord(e, st);
+        ev.push_back(e);
+        return ev.size() - 1;
+    }
+    void add_to(double *ms) const {
+        for (auto &x : starts) {
+            float t = 0.f;
+            if (x.second + 1 < ev.size() && cudaEventElapsedTime(&t, ev[x.second], ev[x.second + 1]) == cudaSuccess)
+                ms[x.first] += t;
+        }
+    }
+    ~PhaseTimer() {
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    }
+};
+
+// Launches one tick: main stream M, side stream D joined back into M.
+cudaError_t launch_tick(const PhaseSpan *sp, const DevProblem *probs, const BatchItem *items, int bmax,
+                        const CUtensorMap *maps, cudaStream_t M, cudaStream_t D, cudaEvent_t fork,
+                        cudaEvent_t join, long &launches, PhaseTimer *tm) {
+    auto run = [&](int ph, cudaStream_t st) -> cudaError_t {
+        if (sp[ph].cnt == 0) return cudaSuccess;
+        if (tm) tm->starts.push_back({ph, tm->record(st)});
+        const cudaError_t e = launch_phase(ph, probs, items + sp[ph].off, sp[ph].cnt, bmax, maps, st);
+        if (tm) tm->record(st);
+        ++launches;
+        return e;
+    };
+    cudaError_t e = cudaSuccess;
+    for (int ph : {phNorms, phInit, phDiagFirst, phPart1, phGemmTop})
+        if ((e = run(ph, M)) != cudaSuccess) return e;
+    const bool side = sp[phDiagNext].cnt > 0;
+    if (side) {
+        if ((e = cudaEventRecord(fork, M)) != cudaSuccess || (e = cudaStreamWaitEvent(D, fork, 0)) != cudaSuccess ||
+            (e = run(phDiagNext, D)) != cudaSuccess || (e = cudaEventRecord(join, D)) != cudaSuccess)
+            return e;
+    }
+    if ((e = run(phGemmRest, M)) != cudaSuccess) return e;
+    if (side && (e = cudaStreamWaitEvent(M, join, 0)) != cudaSuccess) return e;
+    for (int ph : {phFinal, phNormalize})
+        if ((e = run(ph, M)) != cudaSuccess) return e;
+    return cudaSuccess;
 }
 
 int validate(const hsr_batch_problem &p, int b) {
@@ -315,8 +411,8 @@ extern "C" int hsr_batch_plan_create(hsr_batch_plan **out, int nprob, const hsr_
     // base + L.fr ... in the workspace area.  Easiest: give every problem its
     // own full Layout in the workspace area and point nbits/nan at the zero
     // area explicitly.
-    std::vector<DevProblem> hp(nprob);
-    std::vector<CUtensorMap> hm(3 * (size_t)nprob);
+    std::vector<DevProblem> hp(2 * (size_t)nprob);   // two descriptors per problem (tile parity)
+    std::vector<CUtensorMap> hm(6 * (size_t)nprob);
     size_t ws = zero_total;
     std::vector<std::vector<int>> frs(nprob);
     for (int i = 0; i < nprob; ++i) {
@@ -324,89 +420,103 @@ extern "C" int hsr_batch_plan_create(hsr_batch_plan **out, int nprob, const hsr_
         char *base = pl->pool + ws - L.zero_bytes;   // workspace pieces start at L.zero_bytes
         pl->offsets[i] = ws - L.zero_bytes;
         ws += L.total - L.zero_bytes;
-        DevProblem P = make_problem(L, base, probs[i].dH, probs[i].lddH, probs[i].dwr, probs[i].dvr,
-                                    probs[i].lddvr, pl->is, pl->d_err);
         char *zbase = pl->pool + zoff[i];
-        P.nbits = reinterpret_cast<unsigned long long *>(zbase + L.nbits);
-        P.Hn = reinterpret_cast<const double *>(P.nbits);
-        P.hn = reinterpret_cast<const double *>(P.nbits + (size_t)L.T * L.T);
-        P.nanflag = reinterpret_cast<int *>(zbase + L.nan);
-        hp[i] = P;
-        if (!make_maps(&hm[3 * (size_t)i], L, probs[i].dH, probs[i].lddH, base)) {
-            delete pl;
-            return HSR_ERR_CUDA;
+        for (int par = 0; par < 2; ++par) {
+            DevProblem P = make_problem(L, base, probs[i].dH, probs[i].lddH, probs[i].dwr, probs[i].dvr,
+                                        probs[i].lddvr, pl->is, pl->d_err, par);
+            P.nbits = reinterpret_cast<unsigned long long *>(zbase + L.nbits);
+            P.Hn = reinterpret_cast<const double *>(P.nbits);
+            P.hn = reinterpret_cast<const double *>(P.nbits + (size_t)L.T * L.T);
+            P.nanflag = reinterpret_cast<int *>(zbase + L.nan);
+            P.status = pl->d_status + ncols;
+            hp[desc(i, par)] = P;
+            if (!make_maps(&hm[3 * (size_t)desc(i, par)], L, probs[i].dH, probs[i].lddH, base, par)) {
+                delete pl;
+                return HSR_ERR_CUDA;
+            }
         }
         partition_rows(L.n, L.T, b, frs[i]);
         BP_CK(cudaMemcpyAsync(base + L.fr, frs[i].data(), (L.T + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
-        P.status = pl->d_status + ncols;
-        hp[i].status = P.status;
         pl->status_off.push_back(ncols);
         ncols += (size_t)probs[i].nrhs;
     }
-    BP_CK(cudaMalloc(&pl->d_probs, sizeof(DevProblem) * std::max(nprob, 1)));
+    BP_CK(cudaMalloc(&pl->d_probs, sizeof(DevProblem) * std::max<size_t>(hp.size(), 1)));
     BP_CK(cudaMalloc(&pl->d_maps, sizeof(CUtensorMap) * std::max<size_t>(hm.size(), 1)));
     if (nprob) {
-        BP_CK(cudaMemcpyAsync(pl->d_probs, hp.data(), sizeof(DevProblem) * nprob, cudaMemcpyHostToDevice, st));
+        BP_CK(cudaMemcpyAsync(pl->d_probs, hp.data(), sizeof(DevProblem) * hp.size(), cudaMemcpyHostToDevice, st));
         BP_CK(cudaMemcpyAsync(pl->d_maps, hm.data(), sizeof(CUtensorMap) * hm.size(), cudaMemcpyHostToDevice, st));
     }
 
-    // Schedule: setup, then ticks; problem i runs stage J = T_i - 1 - t.
-    std::vector<std::pair<int, std::pair<size_t, int>>> seq;   // (phase, (offset, count))
+    // Schedule: every problem is set up in tick 0; problem i runs the stage
+    // of tile T_i - 1 - t in tick t.
     std::vector<BatchItem> all;
+    std::vector<std::vector<PhaseSpan>> ticks;
     TickLists tl;
+    std::vector<int> stage(nprob, -1);
+    int live = 0;
     for (int i = 0; i < nprob; ++i)
-        if (pl->layouts[i].S > 0) add_setup(tl, i, pl->layouts[i], frs[i]);
-    auto flush = [&]() {
-        for (int ph = 0; ph < phCount; ++ph) {
-            if (tl.v[ph].empty()) continue;
-            seq.push_back({ph, {all.size(), (int)tl.v[ph].size()}});
-            all.insert(all.end(), tl.v[ph].begin(), tl.v[ph].end());
+        if (pl->layouts[i].S > 0) {
+            add_setup(tl, i, pl->layouts[i]);
+            stage[i] = pl->layouts[i].T - 1;
+            ++live;
         }
-        tl.clear();
-    };
-    flush();
-    int maxT = 0;
-    for (int i = 0; i < nprob; ++i)
-        if (pl->layouts[i].S > 0) maxT = std::max(maxT, pl->layouts[i].T);
-    for (int t = 0; t < maxT; ++t) {
+    while (live > 0) {
         for (int i = 0; i < nprob; ++i) {
-            const Layout &L = pl->layouts[i];
-            if (L.S == 0) continue;
-            const int J = L.T - 1 - t;
-            if (J >= 0) add_stage(tl, i, L, frs[i], J);
+            if (stage[i] < 0) continue;
+            if (add_stage(tl, i, pl->layouts[i], frs[i], stage[i])) {
+                stage[i] = -1;
+                --live;
+            } else {
+                --stage[i];
+            }
         }
-        flush();
+        ticks.emplace_back(phCount);
+        const size_t at = all.size();
+        all.resize(at + tl.size());
+        pack_tick(tl, all.data() + at, at, ticks.back().data());
+        tl.clear();
     }
-    pl->ticks = maxT;
+    pl->ticks = (int)ticks.size();
     BP_CK(cudaMalloc(&pl->d_items, sizeof(BatchItem) * std::max<size_t>(all.size(), 1)));
     if (!all.empty())
         BP_CK(cudaMemcpyAsync(pl->d_items, all.data(), sizeof(BatchItem) * all.size(), cudaMemcpyHostToDevice, st));
     BP_CK(cudaStreamSynchronize(st));
 
-    // Capture: zero the accumulators, then every phase launch in order.
-    cudaStream_t cap = nullptr;
-    BP_CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    // Capture: zero the accumulators, then every tick, the diagonal solves of
+    // the next tiles on a forked high-priority stream.
+    cudaStream_t cap = nullptr, side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    int lo_prio = 0, hi_prio = 0;
+    cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+    bool ok = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi_prio) == cudaSuccess &&
+              cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&join, cudaEventDisableTiming) == cudaSuccess;
     // First use sets the kernels' shared-memory attributes outside capture.
-    BP_CK(launch_diag_b(pl->d_probs, pl->d_items, 0, b, cap));
-    bool ok = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) ok = launch_diag_b(pl->d_probs, pl->d_items, 0, b, cap) == cudaSuccess &&
+                 launch_gemm_b(pl->d_probs, pl->d_items, 0, pl->d_maps, cap) == cudaSuccess;
+    if (ok) ok = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    bool capturing = ok;
     if (ok) ok = cudaMemsetAsync(pl->pool, 0, std::max<size_t>(zero_total, 1), cap) == cudaSuccess;
     if (ok) ok = cudaMemsetAsync(pl->d_err, 0, 16, cap) == cudaSuccess;
-    for (auto &e : seq) {
+    for (auto &t : ticks) {
         if (!ok) break;
-        ok = launch_phase(e.first, pl->d_probs, pl->d_items + e.second.first, e.second.second, b, pl->d_maps, cap) ==
-             cudaSuccess;
-        ++pl->launches;
+        ok = launch_tick(t.data(), pl->d_probs, pl->d_items, b, pl->d_maps, cap, side, fork, join, pl->launches,
+                         nullptr) == cudaSuccess;
     }
     cudaGraph_t g = nullptr;
-    const cudaError_t ce = cudaStreamEndCapture(cap, &g);
-    cudaStreamDestroy(cap);
+    const cudaError_t ce = capturing ? cudaStreamEndCapture(cap, &g) : cudaErrorInvalidValue;
+    if (cap) cudaStreamDestroy(cap);
+    if (side) cudaStreamDestroy(side);
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
     if (!ok || ce != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
         delete pl;
         return HSR_ERR_CUDA;
     }
     pl->graph = g;
-    if (cudaGraphInstantiate(&pl->exec, g, 0) != cudaSuccess) {
+    if (cudaGraphInstantiateWithFlags(&pl->exec, g, cudaGraphInstantiateFlagUseNodePriority) != cudaSuccess) {
         delete pl;
         return HSR_ERR_CUDA;
     }
@@ -555,10 +665,11 @@ struct ActiveReq {
     Layout L;
     std::vector<int> fr;
     long long ldh = 0, ldx = 0;
-    int stage = 0;            // next stage to run
-    bool retiring = false;
+    int stage = 0;            // diagonal tile solved last; its stage runs next
+    bool finishing = false;   // the current tick completes the request
+    bool retiring = false;    // results are on their way to the host
     cudaEvent_t done = nullptr;
-    std::vector<int> status;
+    int *h_status = nullptr;  // pinned, [nrhs]
 };
 
 }  // namespace
@@ -567,7 +678,8 @@ struct ActiveReq {
 struct hsr_server {
     hsr_server_config cfg{};
     int b = 64, is = 1, max_slots = 4096;
-    cudaStream_t st = nullptr;
+    cudaStream_t st = nullptr, side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     char *pool = nullptr;
     size_t pool_bytes = 0;
     PoolAlloc alloc;
@@ -583,6 +695,9 @@ struct hsr_server {
     std::vector<int> free_slots;
     ~hsr_server() {
         if (st) cudaStreamSynchronize(st);
+        if (side) cudaStreamDestroy(side);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
         for (int i = 0; i < 2; ++i) {
             if (d_items[i]) cudaFree(d_items[i]);
             if (h_items[i]) cudaFreeHost(h_items[i]);
@@ -620,13 +735,19 @@ extern "C" int hsr_server_create(hsr_server **out, const hsr_server_config *cfg)
     cudaMemGetInfo(&fr, &tot);
     s->pool_bytes = (size_t)(s->cfg.hbm_budget_bytes > 0 ? s->cfg.hbm_budget_bytes : 0.4 * (double)fr);
     s->pool_bytes = up(s->pool_bytes, 256);
+    int lo_prio = 0, hi_prio = 0;
+    cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+    const size_t ndesc = 2 * (size_t)s->max_slots;   // two descriptors per slot (tile parity)
     bool ok = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, hi_prio) == cudaSuccess &&
+              cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming) == cudaSuccess &&
               cudaMalloc(&s->pool, s->pool_bytes) == cudaSuccess &&
-              cudaMalloc(&s->d_probs, sizeof(DevProblem) * s->max_slots) == cudaSuccess &&
-              cudaMalloc(&s->d_maps, sizeof(CUtensorMap) * 3 * (size_t)s->max_slots) == cudaSuccess &&
+              cudaMalloc(&s->d_probs, sizeof(DevProblem) * ndesc) == cudaSuccess &&
+              cudaMalloc(&s->d_maps, sizeof(CUtensorMap) * 3 * ndesc) == cudaSuccess &&
               cudaMalloc(&s->d_err, 16) == cudaSuccess &&
-              cudaMallocHost(&s->h_prob_stage, sizeof(DevProblem) * s->max_slots) == cudaSuccess &&
-              cudaMallocHost(&s->h_map_stage, sizeof(CUtensorMap) * 3 * (size_t)s->max_slots) == cudaSuccess &&
+              cudaMallocHost(&s->h_prob_stage, sizeof(DevProblem) * ndesc) == cudaSuccess &&
+              cudaMallocHost(&s->h_map_stage, sizeof(CUtensorMap) * 3 * ndesc) == cudaSuccess &&
               cudaEventCreateWithFlags(&s->tick_ev[0], cudaEventDisableTiming) == cudaSuccess &&
               cudaEventCreateWithFlags(&s->tick_ev[1], cudaEventDisableTiming) == cudaSuccess;
     if (!ok) {
@@ -670,7 +791,27 @@ extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, dou
     long ticks = 0, launches = 0;
     bool tick_used[2] = {false, false};
     TickLists tl;
+    PhaseSpan spans[phCount];
     int result = HSR_OK;
+    double flops = 0.0, wait_s = 0.0;
+    // Optional device timing of the phases (hsr_set_kernel_timing).
+    PhaseTimer timer;
+    PhaseTimer *tm = stats && kernel_timing_enabled() ? &timer : nullptr;
+    // Convergence flags come back through one pinned array (a slice per request).
+    struct PinnedInts {
+        int *p = nullptr;
+        ~PinnedInts() {
+            if (p) cudaFreeHost(p);
+        }
+    } h_status;
+    std::vector<size_t> status_at(nreq);
+    size_t total_cols = 0;
+    for (int i = 0; i < nreq; ++i) {
+        status_at[i] = total_cols;
+        total_cols += (size_t)reqs[i].nrhs;
+    }
+    if (cudaMallocHost(&h_status.p, sizeof(int) * std::max<size_t>(total_cols, 1)) != cudaSuccess)
+        return HSR_ERR_NOMEM;
 
     while (completed < nreq) {
         const double now = elapsed();
@@ -681,10 +822,8 @@ extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, dou
             ActiveReq &a = active[i];
             if (a.retiring && cudaEventQuery(a.done) == cudaSuccess) {
                 const hsr_request &r = reqs[a.req];
-                cudaMemcpy(a.status.data(), s->pool + a.off + a.L.status, r.nrhs * sizeof(int),
-                           cudaMemcpyDeviceToHost);
                 bool all = true;
-                for (int v : a.status) all = all && v;
+                for (int k = 0; k < r.nrhs; ++k) all = all && a.h_status[k];
                 int rc = HSR_OK;
                 if (!all) {
                     // Restart rounds: solved again on the plain path.
@@ -741,20 +880,23 @@ extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, dou
             double *dwr = reinterpret_cast<double *>(base + a.L.total + up((size_t)a.ldh * r.n * 8, 256));
             double *dX = reinterpret_cast<double *>(reinterpret_cast<char *>(dwr) + up((size_t)r.nrhs * 8, 256));
             partition_rows(r.n, a.L.T, b, a.fr);
+            a.h_status = h_status.p + status_at[ri];
             cudaMemcpy2DAsync(dH, a.ldh * 8, r.H, (size_t)r.ldH * 8, (size_t)r.n * 8, r.n, cudaMemcpyHostToDevice, st);
             cudaMemcpyAsync(dwr, r.wr, (size_t)r.nrhs * 8, cudaMemcpyHostToDevice, st);
             cudaMemcpyAsync(base + a.L.fr, a.fr.data(), (a.L.T + 1) * sizeof(int), cudaMemcpyHostToDevice, st);
             cudaMemsetAsync(base, 0, a.L.zero_bytes, st);
-            DevProblem P = make_problem(a.L, base, dH, a.ldh, dwr, dX, a.ldx, s->is, s->d_err);
-            s->h_prob_stage[a.slot] = P;
-            make_maps(&s->h_map_stage[3 * (size_t)a.slot], a.L, dH, a.ldh, base);
-            cudaMemcpyAsync(s->d_probs + a.slot, s->h_prob_stage + a.slot, sizeof(DevProblem),
+            const int d0 = desc(a.slot, 0);
+            for (int par = 0; par < 2; ++par) {
+                s->h_prob_stage[d0 + par] = make_problem(a.L, base, dH, a.ldh, dwr, dX, a.ldx, s->is, s->d_err, par);
+                make_maps(&s->h_map_stage[3 * (size_t)(d0 + par)], a.L, dH, a.ldh, base, par);
+            }
+            cudaMemcpyAsync(s->d_probs + d0, s->h_prob_stage + d0, 2 * sizeof(DevProblem), cudaMemcpyHostToDevice,
+                            st);
+            cudaMemcpyAsync(s->d_maps + 3 * (size_t)d0, s->h_map_stage + 3 * (size_t)d0, 6 * sizeof(CUtensorMap),
                             cudaMemcpyHostToDevice, st);
-            cudaMemcpyAsync(s->d_maps + 3 * (size_t)a.slot, s->h_map_stage + 3 * (size_t)a.slot,
-                            3 * sizeof(CUtensorMap), cudaMemcpyHostToDevice, st);
-            add_setup(tl, a.slot, a.L, a.fr);
+            add_setup(tl, a.slot, a.L);
+            flops += 2.0 * (double)r.n * r.n * r.nrhs;
             a.stage = a.L.T - 1;
-            a.status.resize(r.nrhs);
             active.push_back(std::move(a));
         }
         int running = 0;
@@ -778,11 +920,15 @@ extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, dou
         // Build this tick: each running request runs its next stage.
         for (auto &a : active) {
             if (a.retiring) continue;
-            add_stage(tl, a.slot, a.L, a.fr, a.stage);
+            a.finishing = add_stage(tl, a.slot, a.L, a.fr, a.stage);
         }
         const size_t count = tl.size();
         // The item buffer of this parity was last used two ticks ago.
-        if (tick_used[parity]) cudaEventSynchronize(s->tick_ev[parity]);
+        if (tick_used[parity]) {
+            const double w0 = elapsed();
+            cudaEventSynchronize(s->tick_ev[parity]);
+            wait_s += elapsed() - w0;
+        }
         if (count > s->items_cap[parity]) {
             if (s->d_items[parity]) cudaFree(s->d_items[parity]);
             if (s->h_items[parity]) cudaFreeHost(s->h_items[parity]);
@@ -791,33 +937,23 @@ extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, dou
                 cudaMallocHost(&s->h_items[parity], sizeof(BatchItem) * s->items_cap[parity]) != cudaSuccess)
                 return HSR_ERR_NOMEM;
         }
-        size_t off = 0;
-        size_t poff[phCount];
-        for (int ph = 0; ph < phCount; ++ph) {
-            poff[ph] = off;
-            if (!tl.v[ph].empty())
-                memcpy(s->h_items[parity] + off, tl.v[ph].data(), sizeof(BatchItem) * tl.v[ph].size());
-            off += tl.v[ph].size();
-        }
+        pack_tick(tl, s->h_items[parity], 0, spans);
         cudaMemcpyAsync(s->d_items[parity], s->h_items[parity], sizeof(BatchItem) * count, cudaMemcpyHostToDevice,
                         st);
-        for (int ph = 0; ph < phCount; ++ph) {
-            if (tl.v[ph].empty()) continue;
-            if (launch_phase(ph, s->d_probs, s->d_items[parity] + poff[ph], (int)tl.v[ph].size(), b, s->d_maps, st) !=
-                cudaSuccess)
-                return HSR_ERR_CUDA;
-            ++launches;
-        }
+        if (launch_tick(spans, s->d_probs, s->d_items[parity], b, s->d_maps, st, s->side, s->fork, s->join, launches,
+                        tm) != cudaSuccess)
+            return HSR_ERR_CUDA;
         // Requests that finished this tick: copy results to the host.
         for (auto &a : active) {
             if (a.retiring) continue;
-            if (a.stage == 0) {
+            if (a.finishing) {
                 const hsr_request &r = reqs[a.req];
                 char *base = s->pool + a.off;
                 double *dwr = reinterpret_cast<double *>(base + a.L.total + up((size_t)a.ldh * r.n * 8, 256));
                 double *dX = reinterpret_cast<double *>(reinterpret_cast<char *>(dwr) + up((size_t)r.nrhs * 8, 256));
                 cudaMemcpy2DAsync(r.vr, (size_t)r.ldvr * 8, dX, a.ldx * 8, (size_t)r.n * 8, r.nrhs,
                                   cudaMemcpyDeviceToHost, st);
+                cudaMemcpyAsync(a.h_status, base + a.L.status, r.nrhs * sizeof(int), cudaMemcpyDeviceToHost, st);
                 cudaEventCreateWithFlags(&a.done, cudaEventDisableTiming);
                 cudaEventRecord(a.done, st);
                 a.retiring = true;
@@ -840,6 +976,10 @@ extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, dou
         stats->launches = launches;
         stats->max_active = max_active;
         stats->peak_bytes = (double)s->alloc.peak;
+        stats->flops = flops;
+        stats->host_wait_s = wait_s;
+        for (int ph = 0; ph < phCount; ++ph) stats->phase_ms[ph] = 0.0;
+        timer.add_to(stats->phase_ms);
     }
     return result;
 }

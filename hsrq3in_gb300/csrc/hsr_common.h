@@ -12,6 +12,10 @@ namespace hsr {
 bool encode_tensor_map(CUtensorMap *m, const double *base, unsigned long long inner, unsigned long long outer,
                        unsigned long long ld, unsigned bx, unsigned by);
 
+// True while per-kernel-class timing (hsr_set_kernel_timing) is on for the
+// calling thread.
+bool kernel_timing_enabled();
+
 inline long long round_up_ll(long long x, long long m) { return (x + m - 1) / m * m; }
 
 }  // namespace hsr

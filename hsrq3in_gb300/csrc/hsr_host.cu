@@ -24,7 +24,7 @@ thread_local long g_launches = 0;
 
 // Optional per-kernel-class device timing: an event pair around every launch
 // on the launching stream, resolved after the call's final synchronisation.
-enum KernelClass { kcSetup = 0, kcDiag, kcPart1, kcGemm, kcFinal, kcOther, kcCount };
+enum KernelClass { kcSetup = 0, kcDiag, kcPart1, kcGemm, kcFinal, kcOther, kcH2D, kcD2H, kcCount };
 struct Timing {
     bool enabled = false;
     std::vector<cudaEvent_t> pool;
@@ -542,11 +542,13 @@ int host_call(int n, const double *H, int ldH, int nrhs, double *wr, int tlsz, i
     HSR_CK(w.H.ensure((size_t)ldh * n * 8));
     HSR_CK(w.X.ensure((size_t)ldx * nrhs * 8));
     HSR_CK(w.wr.ensure((size_t)nrhs * 8));
+    g_timing.begin(kcH2D, st);
     if (ldh == ldH)
         HSR_CK(cudaMemcpyAsync(w.H.p, H, ((size_t)ldH * (n - 1) + n) * 8, cudaMemcpyHostToDevice, st));
     else
         HSR_CK(cudaMemcpy2DAsync(w.H.p, ldh * 8, H, (size_t)ldH * 8, (size_t)n * 8, n, cudaMemcpyHostToDevice, st));
     HSR_CK(cudaMemcpyAsync(w.wr.p, wr, (size_t)nrhs * 8, cudaMemcpyHostToDevice, st));
+    g_timing.end(st);
     hsr_options o{};
     if (opt) o = *opt;
     if (o.user_rhs)
@@ -560,13 +562,16 @@ int host_call(int n, const double *H, int ldH, int nrhs, double *wr, int tlsz, i
                       want && info->perturbed ? &hp : nullptr, want && info->scale ? &hsc : nullptr,
                       want && info->norm ? &hn : nullptr, want && info->tile_scales ? &hts : nullptr);
     if (rc < 0) return rc;
+    g_timing.begin(kcD2H, st);
     if (ldvr == n)   // no padding rows in the caller's block: one contiguous copy
         HSR_CK(cudaMemcpyAsync(vr, w.X.p, (size_t)n * nrhs * 8, cudaMemcpyDeviceToHost, st));
     else             // leave the caller's padding rows untouched
         HSR_CK(cudaMemcpy2DAsync(vr, (size_t)ldvr * 8, w.X.p, ldx * 8, (size_t)n * 8, nrhs,
                                  cudaMemcpyDeviceToHost, st));
     HSR_CK(cudaMemcpyAsync(wr, w.wr.p, (size_t)nrhs * 8, cudaMemcpyDeviceToHost, st));
+    g_timing.end(st);
     HSR_CK(cudaStreamSynchronize(st));
+    g_timing.resolve();
     if (want) {
         if (info->status) memcpy(info->status, hs.data(), (size_t)nrhs * sizeof(int));
         if (info->perturbed) memcpy(info->perturbed, hp.data(), (size_t)nrhs);
@@ -704,3 +709,5 @@ int hsr_probe_fp64_peak(double ms_target, double *dfma_gflops, double *dmma_gflo
 const char *hsr_version(void) { return "hsrq3in_gb300 0.1 (sm_103a, FP64 DFMA)"; }
 
 }  // extern "C"
+
+bool hsr::kernel_timing_enabled() { return g_timing.enabled; }

@@ -137,26 +137,35 @@ cudaError_t launch_init(const DevProblem &P, int mode, const double *eps3_dev, i
 }
 
 // -------------------------------------------------------------- diagonal
-// 32 shifts per CTA, one per lane, and four warps per CTA: the FP64 unit is
-// per SM sub-partition, so the vector part of each step (the updates of
-// y(0:j-2) and of the running column) is split over the four warps by row
-// (i mod 4), while every warp evaluates the short scalar chain of the step
-// (Givens, 1x1 solve, overflow decisions) itself -- identical arithmetic, no
-// broadcast.  v (running column) and y (solution tile) live in shared memory
-// as [row][lane]; the column of H needed by step j is staged one step ahead
-// with cp.async and read as a broadcast.  Per-warp maxima of |y| and |v|
-// meet in shared memory once per step.  When 2*32*b doubles do not fit, v/y
-// live in a global scratch region instead (same code, generic pointers).
-constexpr int kDiagWarps = 4;
+// 32 shifts per CTA, one per lane, and NW warps per CTA.  The FP64 unit is
+// per SM sub-partition, so with NW = 4 the vector part of each step (the
+// updates of y(0:j-2) and of the running column) is split over the four
+// warps by row (i mod 4) and a lone CTA keeps all four sub-partitions busy,
+// while every warp evaluates the short scalar chain of the step (Givens, 1x1
+// solve, overflow decisions) itself -- identical arithmetic, no broadcast.
+// That replication costs FP64 issue slots, so where many CTAs share the GPU
+// (the batched engine) NW = 1 does the same work with the fewest FP64
+// instructions.  v (running column) and y (solution tile) live in shared
+// memory as [row][lane]; the column of H needed by step j is staged one step
+// ahead with cp.async and read as a broadcast.  Per-warp maxima of |y| and
+// |v| meet in shared memory once per step.  When 2*32*b doubles do not fit,
+// v/y live in a global scratch region instead (same code, generic pointers).
+constexpr int kDiagWarps = 4;     // single-problem path
+constexpr int kDiagWarpsB = 1;    // batched path
 
-size_t diag_smem_bytes(int b) {
-    const size_t small = (size_t)(2 * (b + 1)) * sizeof(double) + (size_t)2 * kDiagWarps * 2 * 32 * 8;
+constexpr size_t diag_small_bytes(int b, int nw) {
+    return (size_t)(2 * (b + 1)) * sizeof(double) + (size_t)2 * nw * 2 * 32 * 8;
+}
+size_t diag_smem_bytes_nw(int b, int nw) {
+    const size_t small = diag_small_bytes(b, nw);
     const size_t full = small + (size_t)64 * b * sizeof(double);
     return full <= 200 * 1024 ? full : small;
 }
+size_t diag_smem_bytes(int b) { return diag_smem_bytes_nw(b, kDiagWarps); }
 
 // Body of the diagonal kernel for the 32 shifts of block bx; vy_scratch is
 // this block's global v/y region, or null when v/y fit in shared memory.
+template <int kDiagWarps>
 __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, double *vy_scratch) {
     extern __shared__ double sm[];
     const int lane = threadIdx.x & 31;
@@ -416,7 +425,8 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
             pk = pk * sq;
         }
         P.pi[k] = pk;
-    } else if (wid == 1) {
+    }
+    if (wid == (kDiagWarps > 1 ? 1 : 0)) {
         // Ytilde2 = G_{b-1}^T ... G_1^T (c_0 x_0, x_1, ...) (update-task.c:193-220);
         // Zs(q) = Ytilde2(q-1), Zs(0) = 0, zlast = Ytilde2(b-1).
         unsigned long long zmx = 0;
@@ -443,11 +453,11 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
 
 __global__ void __launch_bounds__(32 * kDiagWarps) k_diag(DevProblem P, int J, double *gscratch) {
     const int b = P.fr[J + 1] - P.fr[J];
-    diag_body(P, J, blockIdx.x, gscratch ? gscratch + (size_t)blockIdx.x * 64 * b : nullptr);
+    diag_body<kDiagWarps>(P, J, blockIdx.x, gscratch ? gscratch + (size_t)blockIdx.x * 64 * b : nullptr);
 }
 
 cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st) {
-    const size_t small = (size_t)(2 * (b + 1)) * sizeof(double) + (size_t)2 * kDiagWarps * 2 * 32 * 8;
+    const size_t small = diag_small_bytes(b, kDiagWarps);
     const size_t smem = gscratch ? small : diag_smem_bytes(b);
     static size_t configured = 0;
     if (smem > configured) {
@@ -460,14 +470,38 @@ cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cud
 }
 
 // --------------------------------------------------------------- Part 1
-// One warp per (tile I < J, shift k): update-task.c:68-174 and the Part-2
-// decision of :206-226.  Columns that need a rescaled Ytilde2 (Y scale below
-// X scale, or a Part-2 factor != 1) get it written to Zslow and are flagged
-// for the protected path of the GEMM epilogue.
-__device__ __forceinline__ void part1_body(const DevProblem &P, int J, int I, int bx) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int k = bx * 8 + warp;
-    if (k >= P.S) return;
+// Part 1 of stage J for tile I < J and shift k (update-task.c:68-174, with
+// the Part-2 decision of :206-226) is the rank-1 update
+//   y(I) -= (H(I, l-1) - mu e_last) * ytilde,   ytilde = -s_0 x_0,
+// bracketed by three scaling decisions.  Where the operands' exponents show
+// that none of the decisions can fire (part1_fast), each returns 1 exactly,
+// and the update itself is left to the GEMM epilogue of stage J, which
+// applies it to every row right before the tile update -- the same
+// operations in the same order.  Otherwise the warp runs the full Part 1 for
+// that (tile, shift) here (part1_full).  The flag byte of (I, k) tells the
+// GEMM epilogue what remains:
+//   bit 0  protected path: Ytilde2 rescaled in Zslow
+//   bit 1  apply the Part-1 update in the epilogue
+
+// Exact test for the case where no decision fires.  Xs == Ys: neither
+// consistency branch runs.  hn, |mu|, |ytilde| < 2^496 and Yn < 2^993: the
+// Part-1 protect_update takes its shortcut (factor 1), and every updated
+// entry has |y'| <= (2^993 + 2^992)(1+u) < 2^994, the shift row
+// |y''| <= (2^994 + 2^992)(1+u) < 2^995, so with Hn, ||Ytilde2||_oo < 2^497
+// the Part-2 protect_update takes its shortcut as well.  NaN fails every
+// comparison and takes the full path.
+__device__ __forceinline__ bool part1_fast(double Xs, double Ys, double hn, double mu, double yt, double Yn,
+                                           double Hn, double z2) {
+    return ubits(Xs) == ubits(Ys) && mag(hn) < pow2_bits(496) && mag(mu) < pow2_bits(496) &&
+           mag(yt) < pow2_bits(496) && mag(Yn) < pow2_bits(993) && mag(Hn) < pow2_bits(497) &&
+           mag(z2) < pow2_bits(497);
+}
+
+// Full Part 1 for (tile I, shift k), by the whole warp.  Columns that need a
+// rescaled Ytilde2 (Y scale below X scale, or a Part-2 factor != 1) get it
+// written to Zslow and are flagged for the protected path of the epilogue.
+__device__ __noinline__ void part1_full(const DevProblem &P, int J, int I, int k) {
+    const int lane = threadIdx.x & 31;
     const bool is = P.is != 0;
     const size_t Spad = (size_t)P.Spad;
     const int T = P.T;
@@ -567,13 +601,64 @@ __device__ __forceinline__ void part1_body(const DevProblem &P, int J, int I, in
         P.ynorm[(size_t)I * Spad + k] = 0.0;   // the GEMM epilogue folds the new bound
         P.slow[(size_t)I * Spad + k] = slow ? 1 : 0;
     }
+    __syncwarp();
 }
 
-__global__ void __launch_bounds__(256) k_part1(DevProblem P, int J) { part1_body(P, J, blockIdx.y, blockIdx.x); }
+// Part 1 of stage J for the shifts [k0, k0 + kPart1Shifts), a lane per shift
+// and 32 shifts per warp, over every tile I < J.  First pass: the exact
+// test, and for the (tile, shift) pairs that pass, the flag for the epilogue
+// and the reset of the tile's norm bound (the epilogue folds the new one).
+// Second pass, only in warps where some pair failed: the full Part 1 for
+// each failed pair in turn.
+__device__ __forceinline__ void part1_block(const DevProblem &P, int J, int k0) {
+    const int lane = threadIdx.x & 31;
+    const int kw = k0 + (threadIdx.x >> 5) * 32;
+    if (kw >= P.S) return;                                    // warp-uniform
+    const int k = kw + lane;
+    const bool act = k < P.S;
+    const size_t Spad = (size_t)P.Spad;
+    const size_t T = (size_t)P.T;
+    double mu = 0.0, yt = 0.0, z2 = 0.0, Xs = 0.0;
+    if (act) {
+        mu = P.wr[k];
+        yt = P.ytil[k];
+        z2 = P.z2n[k];
+        Xs = P.beta[(size_t)J * Spad + k];
+    }
+    bool any = false;
+    if (act) {
+#pragma unroll 4
+        for (int I = 0; I < J; ++I) {
+            const size_t ik = (size_t)I * Spad + k;
+            if (part1_fast(Xs, P.beta[ik], P.hn[I + J * T], mu, yt, P.ynorm[ik], P.Hn[I + J * T], z2)) {
+                P.ynorm[ik] = 0.0;
+                P.slow[ik] = 2;
+            } else {
+                any = true;
+            }
+        }
+    }
+    if (!__any_sync(0xffffffffu, any)) return;
+    for (int I = 0; I < J; ++I) {
+        bool pend = false;
+        if (act) {
+            // Pairs that passed keep passing: their norm bound is now 0.
+            const size_t ik = (size_t)I * Spad + k;
+            pend = !part1_fast(Xs, P.beta[ik], P.hn[I + J * T], mu, yt, P.ynorm[ik], P.Hn[I + J * T], z2);
+        }
+        unsigned m = __ballot_sync(0xffffffffu, pend);
+        while (m) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            part1_full(P, J, I, kw + src);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_part1(DevProblem P, int J) { part1_block(P, J, blockIdx.x * kPart1Shifts); }
 
 cudaError_t launch_part1(const DevProblem &P, int J, cudaStream_t st) {
-    dim3 g((P.S + 7) / 8, J);
-    k_part1<<<g, 256, 0, st>>>(P, J);
+    k_part1<<<(P.S + kPart1Shifts - 1) / kPart1Shifts, 256, 0, st>>>(P, J);
     return cudaGetLastError();
 }
 
@@ -582,7 +667,10 @@ cudaError_t launch_part1(const DevProblem &P, int J, cudaStream_t st) {
 // a 4x4 block of both accumulators.  A = H(rows, l-1 .. l+b-2) and the two
 // B tiles arrive by TMA in 16-column chunks through a 3-stage mbarrier ring.
 // Each accumulator sums k = 0 .. b-1 in order with fma, the same order as
-// the oracle's dot products.
+// the oracle's dot products.  Warp w owns rows 8w .. 8w+7 of the tile, so a
+// warp whose rows all lie outside [row_lo, row_hi) -- the partial blocks at
+// the ragged first tile and at unaligned tile starts -- skips the FMA loop:
+// masked lanes would cost the FP64 pipe as much as live ones.
 struct GemmSmem {
     double A[kGemmStages][kGemmKC][kGemmBM];
     double W[kGemmStages][kGemmKC][kGemmBN];
@@ -624,7 +712,9 @@ __device__ __forceinline__ void gemm_body(const DevProblem &P, int J, int row_lo
     if (tid == 0)
         for (int s = 0; s < kGemmStages && s < nk; ++s) issue(s, s);
 
-    const int tr = tid & 15, tc = tid >> 4;
+    const int tc = tid & 15, tr = tid >> 4;
+    const int wrow = row0 + 8 * (tid >> 5);
+    const bool live = wrow + 8 > row_lo && wrow < row_hi;      // warp-uniform
     double aw[4][4], az[4][4];
 #pragma unroll
     for (int r = 0; r < 4; ++r)
@@ -638,7 +728,7 @@ __device__ __forceinline__ void gemm_body(const DevProblem &P, int J, int row_lo
         const uint32_t par = (uint32_t)((kc / kGemmStages) & 1);
         const bool got = mbar_wait(&sm.full[s], par, P.err);
         if (!__syncthreads_and(got)) { ok = false; break; }
-        const int kmax = min(kGemmKC, b - kc * kGemmKC);
+        const int kmax = live ? min(kGemmKC, b - kc * kGemmKC) : 0;
         for (int kk = 0; kk < kmax; ++kk) {
             const double2 a01 = *reinterpret_cast<const double2 *>(&sm.A[s][kk][4 * tr]);
             const double2 a23 = *reinterpret_cast<const double2 *>(&sm.A[s][kk][4 * tr + 2]);
@@ -671,30 +761,60 @@ __device__ __forceinline__ void gemm_body(const DevProblem &P, int J, int row_lo
         return;
     }
 
-    // Epilogue.
+    // Epilogue.  The accumulators go through shared memory (the operand ring
+    // is free once every warp has left the k-loop), so that each thread then
+    // owns one row of 16 columns: the reads and writes of R and X coalesce
+    // along the rows, and the per-tile maxima of |y| are reduced across the
+    // warp before one atomic per (tile, column).
+    constexpr int kEpiLd = kGemmBM + 2;                       // padded pitch: spreads the banks
+    static_assert(2 * kGemmBN * kEpiLd * sizeof(double) <= sizeof(sm.A) + sizeof(sm.W) + sizeof(sm.Z),
+                  "epilogue staging must fit the operand ring");
+    __syncthreads();
+    double *eaw = &sm.A[0][0][0];
+    double *eaz = eaw + kGemmBN * kEpiLd;
+    if (live) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+            for (int r = 0; r < 4; r += 2) {
+                const int at = (4 * tc + c) * kEpiLd + 4 * tr + r;
+                *reinterpret_cast<double2 *>(&eaw[at]) = make_double2(aw[r][c], aw[r + 1][c]);
+                *reinterpret_cast<double2 *>(&eaz[at]) = make_double2(az[r][c], az[r + 1][c]);
+            }
+    }
+    __syncthreads();
+
     const size_t Spad = (size_t)P.Spad;
     unsigned long long *ynb = reinterpret_cast<unsigned long long *>(P.ynorm);
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        const int col = col0 + 4 * tc + c;
-        if (col >= P.S) continue;
-        const double pik = P.pi[col], w0 = P.W[col], zl = P.zlast[col], mu = P.wr[col];
-        int curI = -1;
-        unsigned long long mx = 0;
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int row = row0 + 4 * tr + r;
-            if (row < row_lo || row >= row_hi) continue;
+    const int lane = tid & 31;
+    const int er = tid & (kGemmBM - 1), cg = tid >> 6;       // row; 16-column group (warp-uniform)
+    const int row = row0 + er;
+    const bool rowok = row >= row_lo && row < row_hi;
+    int I = P.T - 1 - (P.n - 1 - row) / P.tlsz;
+    if (I < 0) I = 0;
+    const int key = rowok ? I : -1;                           // tile of the row; rows are consecutive
+    const double hl1 = rowok ? P.H[row + (size_t)(l - 1) * P.ldh] : 0.0;   // Part-1 column
+    for (int j = 0; j < kGemmBN / 4; ++j) {
+        const int cc = cg * (kGemmBN / 4) + j;
+        const int col = col0 + cc;
+        if (col >= P.S) break;
+        const double pik = P.pi[col], w0 = P.W[col], zl = P.zlast[col], mu = P.wr[col], yt = P.ytil[col];
+        unsigned long long m = 0;
+        if (rowok) {
             const size_t ir = row + (size_t)col * P.ldr;
             const size_t ix = row + (size_t)col * P.ldx;
             const double rold = P.R[ir];
-            double rnew = fma(pik, rold, aw[r][c]);
+            double rnew = fma(pik, rold, eaw[cc * kEpiLd + er]);
             if (row == l - 1) rnew = fma(-mu, w0, rnew);
             P.R[ir] = rnew;
-            int I = P.T - 1 - (P.n - 1 - row) / P.tlsz;
-            if (I < 0) I = 0;
             double yv = P.X[ix];
-            if (P.slow[(size_t)I * Spad + col]) {
+            const unsigned char fl = P.slow[(size_t)I * Spad + col];
+            if (fl & 2) {
+                // Part 1 (update-task.c:134-139): y -= (H(i, l-1) - mu [i == l-1]) ytilde.
+                yv = fma(-hl1, yt, yv);
+                if (row == l - 1) yv = fma(mu, yt, yv);
+            }
+            if (fl & 1) {
                 // Protected path: rescaled Ytilde2 of this (tile, shift).
                 const double *zs = P.Zslow + (size_t)I * P.tlsz * Spad + col;
                 const double *hr = P.H + row + (size_t)l * P.ldh;
@@ -703,18 +823,22 @@ __device__ __forceinline__ void gemm_body(const DevProblem &P, int J, int row_lo
                 yv = yv - acc;
                 yv = fma(-rold, zs[(size_t)(b - 1) * Spad], yv);
             } else {
-                yv = yv - az[r][c];
+                yv = yv - eaz[cc * kEpiLd + er];
                 yv = fma(-rold, zl, yv);
             }
             P.X[ix] = yv;
-            if (I != curI) {
-                if (curI >= 0) atomicMax(&ynb[(size_t)curI * Spad + col], mx);
-                curI = I;
-                mx = 0;
-            }
-            mx = umax64(mx, abs_bits(yv));
+            m = abs_bits(yv);
         }
-        if (curI >= 0) atomicMax(&ynb[(size_t)curI * Spad + col], mx);
+        // Segmented max over runs of lanes in the same tile (inclusive scan);
+        // the last lane of each run holds its maximum.
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned long long mo = __shfl_up_sync(0xffffffffu, m, d);
+            const int ko = __shfl_up_sync(0xffffffffu, key, d);
+            if (lane >= d && ko == key) m = umax64(m, mo);
+        }
+        const int kn = __shfl_down_sync(0xffffffffu, key, 1);
+        if (rowok && (lane == 31 || kn != key)) atomicMax(&ynb[(size_t)I * Spad + col], m);
     }
 }
 
@@ -922,24 +1046,36 @@ __global__ void k_init_b(const DevProblem *probs, const BatchItem *items) {
     if (threadIdx.x == 0) P.pert[k] = 0;
 }
 
-__global__ void __launch_bounds__(32 * kDiagWarps) k_diag_b(const DevProblem *probs, const BatchItem *items) {
+__global__ void __launch_bounds__(32 * kDiagWarpsB) k_diag_b(const DevProblem *probs, const BatchItem *items) {
     const BatchItem it = items[blockIdx.x];
-    diag_body(probs[it.x], it.y, it.z, nullptr);
+    diag_body<kDiagWarpsB>(probs[it.x], it.y, it.z, nullptr);
 }
 
 // One block per (problem, stage, 8 shifts); the tiles above the diagonal
 // tile are visited in turn.
 __global__ void __launch_bounds__(256) k_part1_b(const DevProblem *probs, const BatchItem *items) {
     const BatchItem it = items[blockIdx.x];
-    for (int I = 0; I < it.y; ++I) part1_body(probs[it.x], it.y, I, it.z);
+    part1_block(probs[it.x], it.y, it.z * kPart1Shifts);
 }
 
-__global__ void __launch_bounds__(256, 2) k_gemm_b(const DevProblem *probs, const BatchItem *items,
+__global__ void __launch_bounds__(256, 2) k_gemm_b(const DevProblem *__restrict__ probs,
+                                                  const BatchItem *__restrict__ items,
                                                   const CUtensorMap *maps) {
+    // The descriptor is staged in shared memory: its fields are reloaded
+    // where used instead of occupying registers next to the accumulators.
+    __shared__ DevProblem Ps;
+    static_assert(sizeof(DevProblem) % 8 == 0 && sizeof(DevProblem) / 8 <= 256, "descriptor copy");
     const BatchItem it = items[blockIdx.x];
-    const DevProblem &P = probs[it.x];
+    if (threadIdx.x < sizeof(DevProblem) / 8)
+        reinterpret_cast<long long *>(&Ps)[threadIdx.x] =
+            reinterpret_cast<const long long *>(probs + it.x)[threadIdx.x];
+    __syncthreads();
+    const DevProblem &P = Ps;
     const CUtensorMap *m = maps + 3 * (size_t)it.x;
-    gemm_body(P, it.y, 0, P.fr[it.y], it.z, it.w, m, m + 1, m + 2);
+    const int J = it.y;
+    const bool top = (it.z & kGemmTopFlag) != 0;
+    const int lo = top ? P.fr[J - 1] : 0, hi = top ? P.fr[J] : P.fr[J - 1];
+    gemm_body(P, J, lo, hi, it.z & ~kGemmTopFlag, it.w, m, m + 1, m + 2);
 }
 
 __global__ void __launch_bounds__(32) k_finalize_b(const DevProblem *probs, const BatchItem *items) {
@@ -970,7 +1106,7 @@ cudaError_t launch_init_b(const DevProblem *probs, const BatchItem *items, int n
 }
 cudaError_t launch_diag_b(const DevProblem *probs, const BatchItem *items, int n_items, int bmax,
                           cudaStream_t st) {
-    const size_t smem = diag_smem_bytes(bmax);
+    const size_t smem = diag_smem_bytes_nw(bmax, kDiagWarpsB);
     if (smem < (size_t)64 * bmax * sizeof(double)) return cudaErrorInvalidValue;   // must fit shared memory
     static size_t configured = 0;
     if (smem > configured) {
@@ -979,7 +1115,7 @@ cudaError_t launch_diag_b(const DevProblem *probs, const BatchItem *items, int n
         configured = smem;
     }
     if (n_items <= 0) return cudaSuccess;
-    k_diag_b<<<n_items, 32 * kDiagWarps, smem, st>>>(probs, items);
+    k_diag_b<<<n_items, 32 * kDiagWarpsB, smem, st>>>(probs, items);
     return cudaGetLastError();
 }
 cudaError_t launch_part1_b(const DevProblem *probs, const BatchItem *items, int n_items, cudaStream_t st) {

@@ -75,15 +75,18 @@ cudaError_t launch_normalize(const DevProblem &P, const double *colnorm,
 cudaError_t launch_gather_cols(double *dst, long long ldd, const double *src,
                                long long lds, int n, const int *perm, int cnt,
                                cudaStream_t st);
-// Batched kernels: one launch covers work items of many problems.
+// Batched kernels: one launch covers work items of many problems.  p indexes
+// the descriptor array; a problem has two descriptors (stage operands of
+// even and odd tiles, as in the single-problem look-ahead).
 //   norms:    (p, 0, row block, 0)       row sums over all columns and per tile
 //   init:     (p, 0, column, 0)          start vector eps3 (from the norms)
 //   diag:     (p, J, shift block, 0)
-//   part1:    (p, J, shift block of 8, 0) over all tiles I < J
-//   gemm:     (p, J, row block, column block) over rows [0, fr[J])
+//   part1:    (p, J, shift block of kPart1Shifts, 0) over all tiles I < J
+//   gemm:     (p, J, row block [| kGemmTopFlag], column block): rows of tile
+//             J-1, [fr[J-1], fr[J]), with the flag; rows [0, fr[J-1]) without
 //   finalize: (p, 0, shift block, 0)
 //   normalize:(p, 0, column block of 8, 0)
-// `maps` holds three tensor maps per problem: H, W, Zs.
+// `maps` holds three tensor maps per descriptor: H, W, Zs.
 cudaError_t launch_norms_b(const DevProblem *probs, const BatchItem *items, int n_items, cudaStream_t st);
 cudaError_t launch_init_b(const DevProblem *probs, const BatchItem *items, int n_items, cudaStream_t st);
 cudaError_t launch_diag_b(const DevProblem *probs, const BatchItem *items, int n_items, int bmax,
@@ -95,11 +98,13 @@ cudaError_t launch_finalize_b(const DevProblem *probs, const BatchItem *items, i
 cudaError_t launch_normalize_b(const DevProblem *probs, const BatchItem *items, int n_items, cudaStream_t st);
 constexpr int kNormRows = 128;        // rows per norms item
 constexpr int kNormalizeCols = 8;     // columns per normalize item
+constexpr int kPart1Shifts = 256;     // shifts per part-1 block (a lane per shift)
 
 // FP64 throughput probe kernels.
 cudaError_t launch_probe_dfma(double *out, int blocks, int iters, cudaStream_t st);
 cudaError_t launch_probe_dmma(double *out, int blocks, int iters, cudaStream_t st);
 
 constexpr int kGemmBM = 64, kGemmBN = 64, kGemmKC = 16, kGemmStages = 3;
+constexpr int kGemmTopFlag = 1 << 30;   // batched GEMM item: rows of tile J-1
 
 }  // namespace hsr

@@ -111,10 +111,11 @@ int hsr_inverse_iteration_device(int n, const double *dH, int lddH, int nrhs,
 long hsr_last_launch_count(void);
 
 /* Per-kernel-class device timing (CUDA events on the launching stream
- * around every launch), off by default.  hsr_last_kernel_times fills
- * ms[6] and launches[6] for the classes {setup, diagonal, part1, gemm,
- * finalize, other} of the last call, and the algorithmic FMA count of its
- * GEMM launches; returns the number of classes.  No reference counterpart. */
+ * around every launch and copy), off by default.  hsr_last_kernel_times
+ * fills ms[8] and launches[8] for the classes {setup, diagonal, part1, gemm,
+ * finalize, other, host-to-device copy, device-to-host copy} of the last
+ * call, and the algorithmic FMA count of its GEMM launches; returns the
+ * number of classes.  No reference counterpart. */
 void hsr_set_kernel_timing(int enable);
 int hsr_last_kernel_times(double *ms, long *launches, double *gemm_fma);
 
@@ -193,6 +194,14 @@ typedef struct hsr_server_stats {
     long launches;          /* kernel launches                           */
     int max_active;         /* largest number of concurrently admitted requests */
     double peak_bytes;      /* largest pool footprint                    */
+    double phase_ms[9];     /* device time per phase (norms, init, first
+                               diagonal, part1, gemm of tile J-1's rows,
+                               next diagonal (overlaps the next phase),
+                               gemm of the rows above, finalize,
+                               normalize) when hsr_set_kernel_timing(1)
+                               is on; else 0                             */
+    double flops;           /* 2 n^2 nrhs summed over served requests    */
+    double host_wait_s;     /* host time blocked on the device's ticks   */
 } hsr_server_stats;
 
 typedef struct hsr_server hsr_server;
