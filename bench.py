@@ -47,7 +47,7 @@ UNIT = "eigenvectors/s"
 # dram__bytes_read+write for 1696*399*4096 FMAs; profiles/k_gemm_n4096.md).
 # Traffic and FMAs both grow with rows x shifts, so the ratio scales the
 # capture to the launches of this workload.
-GEMM_DRAM_BYTES_PER_FMA = 183.609344e6 / (1696 * 399 * 4096)
+GEMM_DRAM_BYTES_PER_FMA = (127.772928e6 + 54.166528e6) / (1696 * 399 * 4096)
 
 
 def parse():
@@ -245,8 +245,9 @@ def run_gpu(args, H, wr, rank, world):
     torch.cuda.synchronize()
     dfma, dmma = hsr.fp64_peak(200.0)          # after warm-up: clocks ramped
     lib.hsr_set_kernel_timing(1)
-    kms = np.zeros(8)
-    kl = np.zeros(8, dtype=np.int64)
+    ncls = len(_lib.KERNEL_CLASSES)
+    kms = np.zeros(ncls)
+    kl = np.zeros(ncls, dtype=np.int64)
     gemm_fma = 0.0
     launches = 0
     if world > 1:
@@ -261,8 +262,8 @@ def run_gpu(args, H, wr, rank, world):
             rcs = []
             for _ in range(args.steps):
                 rcs.append(step())
-                ms = (C.c_double * 8)()
-                ln = (C.c_long * 8)()
+                ms = (C.c_double * ncls)()
+                ln = (C.c_long * ncls)()
                 fm = C.c_double()
                 lib.hsr_last_kernel_times(ms, ln, C.byref(fm))
                 kms += np.array(ms[:])
@@ -295,7 +296,8 @@ def run_gpu(args, H, wr, rank, world):
             "frac": (achieved / peak) if achieved else None,
             "traffic": (GEMM_DRAM_BYTES_PER_FMA * gemm_fma / max(kl[3], 1)) if GEMM_DRAM_BYTES_PER_FMA else None,
             "traffic_note": "DRAM bytes per launch, scaled from the n=4096 ncu capture by algorithmic FMAs",
-            "kernel": "k_gemm (crossover propagation + tile update, DFMA)",
+            "kernel": "k_gemm (crossover propagation + tile update, DFMA; the launches over the rows above "
+                      "the next diagonal tile, which share the GPU with that tile's GEMM and diagonal solve)",
             "peak_source": "FP64 DFMA stream measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
             "algorithmic_flops_per_launch": 2.0 * gemm_fma / max(kl[3], 1),
             "avg_launch_ms": gemm_ms / max(kl[3], 1)}
@@ -340,7 +342,7 @@ def run_gpu(args, H, wr, rank, world):
         lib.hsr_set_kernel_timing(1)
         e2e_step()
         torch.cuda.synchronize()
-        ms8 = (C.c_double * 8)()
+        ms8 = (C.c_double * len(_lib.KERNEL_CLASSES))()
         lib.hsr_last_kernel_times(ms8, None, None)
         lib.hsr_set_kernel_timing(0)
         out["e2e"] = {"value": world * S / te, "unit": UNIT, "h2d_bytes_per_step": 8 * (n * n + S),

@@ -33,7 +33,7 @@ EXPORTS = [
 ]
 NOALLOC_MAX_N = 256
 NOALLOC_MAX_NRHS = 256
-KERNEL_CLASSES = ["setup", "diag", "part1", "gemm", "finalize", "other", "h2d", "d2h"]
+KERNEL_CLASSES = ["setup", "diag", "part1", "gemm", "finalize", "other", "h2d", "d2h", "gemm_top"]
 SERVER_PHASES = ["norms", "init", "diag_first", "part1", "gemm_top", "diag_next", "gemm_rest", "finalize",
                  "normalize"]
 

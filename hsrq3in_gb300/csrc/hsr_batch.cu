@@ -2,9 +2,10 @@
 //
 // A problem with T row tiles needs T stages (J = T-1 .. 0).  Problems start
 // at their own tick and each tick advances every active problem by one stage,
-// with the single-problem look-ahead: part 1 of stage J, the GEMM rows of
-// tile J-1, then the diagonal solve of tile J-1 on a side stream while the
-// GEMM rows above tile J-1 run on the main stream.  One batched launch per
+// with the single-problem look-ahead: part 1 of stage J, then on a
+// high-priority side stream the GEMM rows of tile J-1 followed by the
+// diagonal solve of tile J-1, while the GEMM rows above tile J-1 run on the
+// main stream.  One batched launch per
 // phase covers the work items of all problems, so thousands of small
 // problems fill the GPU together.  Each work item runs the single-problem
 // kernel body, so every column computes exactly what it computes when its
@@ -161,8 +162,8 @@ bool make_maps(CUtensorMap *m, const Layout &L, const double *H, long long ldh, 
 }
 
 // ----------------------------------------------------------- work lists
-// Phases of a tick in launch order.  phDiagNext runs on the side stream,
-// after phGemmTop and concurrently with phGemmRest.
+// Phases of a tick in launch order.  phGemmTop and then phDiagNext run on the
+// side stream, concurrently with phGemmRest.
 enum Phase {
     phNorms = 0, phInit, phDiagFirst, phPart1, phGemmTop, phDiagNext, phGemmRest, phFinal, phNormalize, phCount
 };
@@ -285,12 +286,13 @@ cudaError_t launch_tick(const PhaseSpan *sp, const DevProblem *probs, const Batc
         return e;
     };
     cudaError_t e = cudaSuccess;
-    for (int ph : {phNorms, phInit, phDiagFirst, phPart1, phGemmTop})
+    for (int ph : {phNorms, phInit, phDiagFirst, phPart1})
         if ((e = run(ph, M)) != cudaSuccess) return e;
-    const bool side = sp[phDiagNext].cnt > 0;
+    const bool side = sp[phGemmTop].cnt > 0 || sp[phDiagNext].cnt > 0;
     if (side) {
         if ((e = cudaEventRecord(fork, M)) != cudaSuccess || (e = cudaStreamWaitEvent(D, fork, 0)) != cudaSuccess ||
-            (e = run(phDiagNext, D)) != cudaSuccess || (e = cudaEventRecord(join, D)) != cudaSuccess)
+            (e = run(phGemmTop, D)) != cudaSuccess || (e = run(phDiagNext, D)) != cudaSuccess ||
+            (e = cudaEventRecord(join, D)) != cudaSuccess)
             return e;
     }
     if ((e = run(phGemmRest, M)) != cudaSuccess) return e;
@@ -358,11 +360,21 @@ namespace {
     } while (0)
 }  // namespace
 
+// The tuned entry whose order range overlaps [n_lo, n_hi] the most (a
+// sample rarely spans the extremes of the batch it was drawn from); the
+// default when none overlaps.
 extern "C" int hsr_autotune_tlsz(int n_lo, int n_hi) {
     std::lock_guard<std::mutex> g(g_tune_mu);
-    for (auto &kv : g_tune)
-        if (kv.first.first <= n_lo && n_hi <= kv.first.second) return kv.second;
-    return default_tlsz(n_hi);
+    long best_overlap = 0;
+    int best = 0;
+    for (auto &kv : g_tune) {
+        const long ov = (long)std::min(n_hi, kv.first.second) - std::max(n_lo, kv.first.first) + 1;
+        if (ov > best_overlap) {
+            best_overlap = ov;
+            best = kv.second;
+        }
+    }
+    return best > 0 ? best : default_tlsz(n_hi);
 }
 
 extern "C" int hsr_batch_plan_create(hsr_batch_plan **out, int nprob, const hsr_batch_problem *probs, int tlsz,

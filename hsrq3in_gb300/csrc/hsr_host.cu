@@ -24,7 +24,7 @@ thread_local long g_launches = 0;
 
 // Optional per-kernel-class device timing: an event pair around every launch
 // on the launching stream, resolved after the call's final synchronisation.
-enum KernelClass { kcSetup = 0, kcDiag, kcPart1, kcGemm, kcFinal, kcOther, kcH2D, kcD2H, kcCount };
+enum KernelClass { kcSetup = 0, kcDiag, kcPart1, kcGemm, kcFinal, kcOther, kcH2D, kcD2H, kcGemmTop, kcCount };
 struct Timing {
     bool enabled = false;
     std::vector<cudaEvent_t> pool;
@@ -32,7 +32,7 @@ struct Timing {
     std::vector<int> cls;
     double ms[kcCount] = {0};
     long launches[kcCount] = {0};
-    double gemm_fma[1] = {0};   // algorithmic FMAs of the timed GEMM launches
+    double gemm_fma[1] = {0};   // algorithmic FMAs of the timed kcGemm launches
     void reset() {
         used = 0;
         cls.clear();
@@ -269,12 +269,13 @@ DevProblem problem_for(const Solver &s, int off, int cnt, int parity = 0) {
 }
 
 // Runs columns [off, off+cnt) through one pass; mode as launch_init.
-// Per stage J (main stream M, side stream D):
-//   M: part1(J) -> gemm(J) on the rows of tile J-1 -> [ev_top] -> gemm(J) on
-//      rows above tile J-1 -> wait ev_diag
-//   D: wait ev_top -> diag(J-1) -> [ev_diag]
-// so diag(J-1), a latency-bound sequential kernel, overlaps the bulk of the
-// FP64-bound GEMM of stage J.  Stage operands alternate buffers by parity.
+// Per stage J (main stream M, high-priority side stream D):
+//   M: part1(J) -> [ev_top] -> gemm(J) on rows above tile J-1 -> wait ev_diag
+//   D: wait ev_top -> gemm(J) on the rows of tile J-1 -> diag(J-1) -> [ev_diag]
+// so the short GEMM of tile J-1's rows and then diag(J-1), a latency-bound
+// sequential kernel, run beside the bulk of the FP64-bound GEMM of stage J,
+// and the last wave of the short GEMM leaves no SM idle.  Stage operands
+// alternate buffers by parity.
 int run_pass(Solver &s, int mode, int its, int off, int cnt) {
     Workspace &w = *s.w;
     HSR_CK(w.ensure_side());
@@ -297,15 +298,16 @@ int run_pass(Solver &s, int mode, int its, int off, int cnt) {
             DevProblem P = problem_for(s, off + c0, cc, J & 1);
             DevProblem Pn = problem_for(s, off + c0, cc, (J - 1) & 1);
             HSR_LAUNCH_C(kcPart1, M, launch_part1(P, J, M));
-            HSR_LAUNCH_C(kcGemm, M, launch_gemm(P, J, s.fr[J - 1], s.fr[J], s.tmH, s.tmW[J & 1], s.tmZ[J & 1], M));
             HSR_CK(cudaEventRecord(w.ev_top, M));
             HSR_CK(cudaStreamWaitEvent(D, w.ev_top, 0));
+            HSR_LAUNCH_C(kcGemmTop, D,
+                         launch_gemm(P, J, s.fr[J - 1], s.fr[J], s.tmH, s.tmW[J & 1], s.tmZ[J & 1], D));
             HSR_LAUNCH_C(kcDiag, D, launch_diag(Pn, J - 1, s.fr[J] - s.fr[J - 1], gs, D));
             HSR_CK(cudaEventRecord(w.ev_diag, D));
             if (s.fr[J - 1] > 0)
                 HSR_LAUNCH_C(kcGemm, M, launch_gemm(P, J, 0, s.fr[J - 1], s.tmH, s.tmW[J & 1], s.tmZ[J & 1], M));
             HSR_CK(cudaStreamWaitEvent(M, w.ev_diag, 0));
-            if (g_timing.enabled) g_timing.gemm_fma[0] += (double)s.fr[J] * (2.0 * bj - 1.0) * cc;
+            if (g_timing.enabled) g_timing.gemm_fma[0] += (double)s.fr[J - 1] * (2.0 * bj - 1.0) * cc;
         }
         DevProblem P = problem_for(s, off + c0, cc, 0);
         HSR_LAUNCH_C(kcFinal, M, launch_finalize(P, s.d_colnorm + off + c0, s.d_status + off + c0,

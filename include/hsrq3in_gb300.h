@@ -112,10 +112,11 @@ long hsr_last_launch_count(void);
 
 /* Per-kernel-class device timing (CUDA events on the launching stream
  * around every launch and copy), off by default.  hsr_last_kernel_times
- * fills ms[8] and launches[8] for the classes {setup, diagonal, part1, gemm,
- * finalize, other, host-to-device copy, device-to-host copy} of the last
- * call, and the algorithmic FMA count of its GEMM launches; returns the
- * number of classes.  No reference counterpart. */
+ * fills ms[9] and launches[9] for the classes {setup, diagonal, part1, gemm
+ * (rows above the next diagonal tile), finalize, other, host-to-device copy,
+ * device-to-host copy, gemm of the next diagonal tile's rows} of the last
+ * call, and the algorithmic FMA count of its gemm-class launches; returns
+ * the number of classes.  No reference counterpart. */
 void hsr_set_kernel_timing(int enable);
 int hsr_last_kernel_times(double *ms, long *launches, double *gemm_fma);
 
@@ -155,8 +156,9 @@ int hsr_batch_plan_execute(hsr_batch_plan *plan, void *stream);
 int hsr_batch_plan_info(const hsr_batch_plan *plan, int *tlsz, int *ticks, long *launches);
 void hsr_batch_plan_destroy(hsr_batch_plan *plan);
 
-/* Tile size for batches whose orders lie in [n_lo, n_hi]: measured by
- * hsr_autotune_batch on this GPU when a measurement exists, else a default. */
+/* Tile size for batches whose orders lie in [n_lo, n_hi]: the size that
+ * hsr_autotune_batch measured fastest on this GPU for the sample whose order
+ * range overlaps [n_lo, n_hi] the most, else a default. */
 int hsr_autotune_tlsz(int n_lo, int n_hi);
 /* Time a sample batch for each candidate tile size in `cand` and record the
  * fastest for [n_lo, n_hi]; returns it.  ms_out[i] gets candidate i's time. */
@@ -196,10 +198,10 @@ typedef struct hsr_server_stats {
     double peak_bytes;      /* largest pool footprint                    */
     double phase_ms[9];     /* device time per phase (norms, init, first
                                diagonal, part1, gemm of tile J-1's rows,
-                               next diagonal (overlaps the next phase),
-                               gemm of the rows above, finalize,
-                               normalize) when hsr_set_kernel_timing(1)
-                               is on; else 0                             */
+                               next diagonal -- these two on a side stream
+                               beside the next phase -- gemm of the rows
+                               above, finalize, normalize) when
+                               hsr_set_kernel_timing(1) is on; else 0    */
     double flops;           /* 2 n^2 nrhs summed over served requests    */
     double host_wait_s;     /* host time blocked on the device's ticks   */
 } hsr_server_stats;
