@@ -153,8 +153,10 @@ cudaError_t launch_init(const DevProblem &P, int mode, const double *eps3_dev, i
 constexpr int kDiagWarps = 4;     // single-problem path
 constexpr int kDiagWarpsB = 1;    // batched path
 
+constexpr int kDiagBcast = 8;      // per-lane step results broadcast by warp 0
 constexpr size_t diag_small_bytes(int b, int nw) {
-    return (size_t)(2 * (b + 1)) * sizeof(double) + (size_t)2 * nw * 2 * 32 * 8;
+    return (size_t)(2 * (b + 1)) * sizeof(double) + (size_t)2 * nw * 2 * 32 * 8 +
+           (nw > 1 ? (size_t)kDiagBcast * 32 * 8 : 0);
 }
 size_t diag_smem_bytes_nw(int b, int nw) {
     const size_t small = diag_small_bytes(b, nw);
@@ -177,20 +179,25 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
     const bool is = P.is != 0;
     const size_t Spad = (size_t)P.Spad;
 
+    // With several warps, warp 0 alone evaluates each step's scalar chain and
+    // hands its per-lane results to the others through shared memory.
+    constexpr bool kBcast = kDiagWarps > 1;
     double *hc = sm;                                          // [2][b+1]
     // Per-warp partial maxima, double-buffered by step parity: [2][W][2][32].
     unsigned long long *pmax = reinterpret_cast<unsigned long long *>(sm + 2 * (b + 1));
+    double *bc = sm + 2 * (b + 1) + 2 * kDiagWarps * 2 * 32;  // [kDiagBcast][32]
     double *v, *y;
     if (vy_scratch) {
         v = vy_scratch;
         y = v + (size_t)32 * b;
     } else {
-        v = sm + 2 * (b + 1) + 2 * kDiagWarps * 2 * 32;
+        v = bc + (kBcast ? kDiagBcast * 32 : 0);
         y = v + (size_t)32 * b;
     }
 #define V(i) v[(size_t)(i) * 32 + lane]
 #define Y(i) y[(size_t)(i) * 32 + lane]
 #define PMAX(par, w, which) pmax[(((par) * kDiagWarps + (w)) * 2 + (which)) * 32 + lane]
+#define BC(q) bc[(q) * 32 + lane]
 
     // Load the crossover column and the right-hand side tile, transposed.
     for (int c = wid; c < 32; c += kDiagWarps) {
@@ -247,53 +254,80 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
         __syncthreads();                                       // previous step's rows and column j-1 visible
         const double *hcol = hc + buf * (b + 1);              // column j-1 of the tile
         if (wid == 0 && j >= 2) stage_col(j - 2, hc + (buf ^ 1) * (b + 1));
-        unsigned long long ymax = 0, vmax = 0;
+        double c = 0.0, s = 0.0, yc = 0.0, ys = 0.0, a1 = 1.0, a2 = 1.0, a3 = 1.0;
+        double yj = 0.0, yjm1 = 0.0, hdiag = 0.0, vjm1 = 0.0;
+        if (!kBcast || wid == 0) {
+            unsigned long long ymax = 0, vmax = 0;
 #pragma unroll
-        for (int w = 0; w < kDiagWarps; ++w) {
-            ymax = umax64(ymax, PMAX(par, w, 0));
-            vmax = umax64(vmax, PMAX(par, w, 1));
-        }
-        const double hsub = hcol[j];
-        const double hdiag = hcol[j - 1] - mu;
-        const double vj = vcar, vjm1 = V(j - 1);
-        double yj = ycar, yjm1 = Y(j - 1);
+            for (int w = 0; w < kDiagWarps; ++w) {
+                ymax = umax64(ymax, PMAX(par, w, 0));
+                vmax = umax64(vmax, PMAX(par, w, 1));
+            }
+            const double hsub = hcol[j];
+            hdiag = hcol[j - 1] - mu;
+            const double vj = vcar;
+            vjm1 = V(j - 1);
+            yj = ycar;
+            yjm1 = Y(j - 1);
 
-        double c, s;
-        givens(vj, hsub, c, s);
-        if (act && wid == 0) {
-            P.Cr[(size_t)(l + j) * Spad + k] = c;
-            P.Sr[(size_t)(l + j) * Spad + k] = s;
-        }
-        // y(j) := y(j) / R(j,j) robustly (solve-task.c:76-81).
-        double phi = sc_one(is);
-        pert |= solve_1x1(smin, c * vj, s * hsub, yj, phi, is);
-        beta = sc_combine(beta, phi, is);
-        const double a1 = sc_value(phi, is);
-        if (!is_one(a1)) {
-            yjm1 = a1 * yjm1;
-            ymax = abs_bits(a1 * from_bits(ymax));
-        }
-        // y(j-1) (solve-task.c:84-90).
-        phi = protect_double_update(fabs(vjm1), fabs(yj), fabs(hdiag), fabs(yj), fabs(yjm1), is);
-        const double a2 = sc_value(phi, is);
-        if (!is_one(a2)) {
-            yj = a2 * yj;
-            yjm1 = a2 * yjm1;
-            ymax = abs_bits(a2 * from_bits(ymax));
-        }
-        beta = sc_combine(beta, phi, is);
-        double yc = yj * c, ys = yj * s;
-        yjm1 = fma(ys, hdiag, fma(-yc, vjm1, yjm1));
-        // y(0:j-2) (solve-task.c:92-100).
-        phi = protect_double_update(from_bits(vmax), fabs(yj), Hnorm, fabs(yj), from_bits(ymax), is);
-        const double a3 = sc_value(phi, is);
-        if (!is_one(a3)) {
-            yj = a3 * yj;
-            yjm1 = a3 * yjm1;
+            givens(vj, hsub, c, s);
+            if (act && wid == 0) {
+                P.Cr[(size_t)(l + j) * Spad + k] = c;
+                P.Sr[(size_t)(l + j) * Spad + k] = s;
+            }
+            // y(j) := y(j) / R(j,j) robustly (solve-task.c:76-81).
+            double phi = sc_one(is);
+            pert |= solve_1x1(smin, c * vj, s * hsub, yj, phi, is);
+            beta = sc_combine(beta, phi, is);
+            a1 = sc_value(phi, is);
+            if (!is_one(a1)) {
+                yjm1 = a1 * yjm1;
+                ymax = abs_bits(a1 * from_bits(ymax));
+            }
+            // y(j-1) (solve-task.c:84-90).
+            phi = protect_double_update(fabs(vjm1), fabs(yj), fabs(hdiag), fabs(yj), fabs(yjm1), is);
+            a2 = sc_value(phi, is);
+            if (!is_one(a2)) {
+                yj = a2 * yj;
+                yjm1 = a2 * yjm1;
+                ymax = abs_bits(a2 * from_bits(ymax));
+            }
+            beta = sc_combine(beta, phi, is);
             yc = yj * c;
             ys = yj * s;
+            yjm1 = fma(ys, hdiag, fma(-yc, vjm1, yjm1));
+            // y(0:j-2) (solve-task.c:92-100).
+            phi = protect_double_update(from_bits(vmax), fabs(yj), Hnorm, fabs(yj), from_bits(ymax), is);
+            a3 = sc_value(phi, is);
+            if (!is_one(a3)) {
+                yj = a3 * yj;
+                yjm1 = a3 * yjm1;
+                yc = yj * c;
+                ys = yj * s;
+            }
+            beta = sc_combine(beta, phi, is);
+            if (kBcast) {
+                BC(0) = c;
+                BC(1) = s;
+                BC(2) = yc;
+                BC(3) = ys;
+                BC(4) = a1;
+                BC(5) = a2;
+                BC(6) = a3;
+            }
         }
-        beta = sc_combine(beta, phi, is);
+        if (kBcast) {
+            __syncthreads();                                   // this step's scalars visible
+            if (wid != 0) {
+                c = BC(0);
+                s = BC(1);
+                yc = BC(2);
+                ys = BC(3);
+                a1 = BC(4);
+                a2 = BC(5);
+                a3 = BC(6);
+            }
+        }
         const bool scaled = (!is_one(a1)) || (!is_one(a2)) || (!is_one(a3));
         if (scaled) {
             // Rare: the whole-vector scale() also reaches the solved rows j+1 .. b-1.
@@ -361,39 +395,54 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
         }
         PMAX(par ^ 1, wid, 0) = ymx;
         PMAX(par ^ 1, wid, 1) = vmx;
-        if (j % kDiagWarps == wid) Y(j) = yj;                 // solved entry, by its owner
-        // Next annihilation column entry (solve-task.c:105-108) and y(j-1).
-        vcar = fma(c, hdiag, s * vjm1);
-        ycar = yjm1;
+        if (kBcast ? wid == 0 : j % kDiagWarps == wid) Y(j) = yj;   // solved entry, by the chain warp
+        if (!kBcast || wid == 0) {
+            // Next annihilation column entry (solve-task.c:105-108) and y(j-1).
+            vcar = fma(c, hdiag, s * vjm1);
+            ycar = yjm1;
+        }
         buf ^= 1;
         par ^= 1;
     }
 
     double c0 = 0.0, s0 = 0.0;
     {
-        double v0 = b >= 2 ? vcar : V(0);
-        double y0 = b >= 2 ? ycar : Y(0);
-        double hleft = 0.0;
-        if (J > 0) {
-            // Final rotation with H(l, l-1) (reduce.c:53-61, solve-task.c:111-118).
-            hleft = P.H[l + (size_t)(l - 1) * P.ldh];
-            if (hleft != 0) {
-                givens(v0, hleft, c0, s0);
-            } else {
-                c0 = 1.0;
-                s0 = 0.0;
+        double y0 = 0.0, a = 1.0;
+        if (!kBcast || wid == 0) {
+            double v0 = b >= 2 ? vcar : V(0);
+            y0 = b >= 2 ? ycar : Y(0);
+            double hleft = 0.0;
+            if (J > 0) {
+                // Final rotation with H(l, l-1) (reduce.c:53-61, solve-task.c:111-118).
+                hleft = P.H[l + (size_t)(l - 1) * P.ldh];
+                if (hleft != 0) {
+                    givens(v0, hleft, c0, s0);
+                } else {
+                    c0 = 1.0;
+                    s0 = 0.0;
+                }
+                if (act && wid == 0) {
+                    P.Cr[(size_t)l * Spad + k] = c0;
+                    P.Sr[(size_t)l * Spad + k] = s0;
+                }
+                v0 = fma(v0, c0, -(hleft * s0));
             }
-            if (act && wid == 0) {
-                P.Cr[(size_t)l * Spad + k] = c0;
-                P.Sr[(size_t)l * Spad + k] = s0;
+            double phi = sc_one(is);
+            pert |= solve_1x1(smin, v0, 0.0, y0, phi, is);
+            beta = sc_combine(beta, phi, is);
+            a = sc_value(phi, is);
+            if (kBcast) {
+                BC(0) = c0;
+                BC(1) = s0;
+                BC(2) = a;
             }
-            v0 = fma(v0, c0, -(hleft * s0));
         }
-        double phi = sc_one(is);
-        pert |= solve_1x1(smin, v0, 0.0, y0, phi, is);
-        beta = sc_combine(beta, phi, is);
-        const double a = sc_value(phi, is);
-        __syncthreads();                                       // last step's rows written
+        __syncthreads();                                       // last step's rows (and the scalars) written
+        if (kBcast && wid != 0) {
+            c0 = BC(0);
+            s0 = BC(1);
+            a = BC(2);
+        }
         if (!is_one(a))
             for (int i = 1 + ((wid - 1) % kDiagWarps + kDiagWarps) % kDiagWarps; i < b; i += kDiagWarps)
                 Y(i) = a * Y(i);
@@ -449,6 +498,7 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
 #undef V
 #undef Y
 #undef PMAX
+#undef BC
 }
 
 __global__ void __launch_bounds__(32 * kDiagWarps) k_diag(DevProblem P, int J, double *gscratch) {
