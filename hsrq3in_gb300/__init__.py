@@ -7,8 +7,8 @@ the seeded workload generators (``generators.py``).
 """
 from .api import (BatchPlan, HsrError, Server, autotune_batch, fp64_peak,  # noqa: F401
                   inverse_iteration, inverse_iteration_device, last_launch_count,
-                  tiled_inverse_iteration)
+                  residuals_device, tiled_inverse_iteration)
 from ._lib import lib_path, load  # noqa: F401
 
 __all__ = ["BatchPlan", "Server", "autotune_batch", "HsrError", "fp64_peak", "inverse_iteration", "inverse_iteration_device",
-           "last_launch_count", "tiled_inverse_iteration", "lib_path", "load"]
+           "last_launch_count", "residuals_device", "tiled_inverse_iteration", "lib_path", "load"]

@@ -107,6 +107,23 @@ def inverse_iteration_device(dH, dwr, dvr, tlsz: int, stream=None, scaling: str 
     return rc
 
 
+def residuals_device(dH, dwr, dvr, stream=None):
+    """||H x_k - wr_k x_k|| / (||H||_F ||x_k||) per column, on the device.
+    Tensors as for inverse_iteration_device: dH (n, ldh), dvr (ncols, ldvr)
+    with rows = columns, dwr (ncols,).  Returns a float64 device tensor."""
+    import torch
+    lib = _lib.load()
+    n = dH.shape[0]
+    ncols = dwr.shape[0]
+    res = torch.empty(ncols, dtype=torch.float64, device=dH.device)
+    st = None if stream is None else C.c_void_p(stream.cuda_stream)
+    rc = lib.hsr_residuals_device(n, dH.data_ptr(), dH.stride(0), ncols, dwr.data_ptr(), dvr.data_ptr(),
+                                  dvr.stride(0), res.data_ptr(), st)
+    if rc < 0:
+        raise HsrError(rc)
+    return res
+
+
 def fp64_peak(ms_target: float = 50.0):
     """(DFMA GFLOP/s, DMMA GFLOP/s) measured on the current GPU."""
     lib = _lib.load()

@@ -123,6 +123,18 @@ int hsr_last_kernel_times(double *ms, long *launches, double *gemm_fma);
 /* Release cached device workspaces of this thread. */
 void hsr_release_workspace(void);
 
+/* ------------------------------------------------- residuals on the device */
+/* Replaces the residual check of validate_real_eigenvectors
+ * (validation.c:145-166) for device-resident results: d_res[k] =
+ * ||H x_k - wr[k] x_k||_2 / (||H||_F ||x_k||_2) over the Hessenberg part of H,
+ * computed with exact power-of-two prescaling so that no input magnitude
+ * overflows (NaN for a non-finite H or x_k, +Inf for a zero x_k).  Costs about
+ * n^2/2 FMAs per column.  Enqueued on `stream` without synchronising; all
+ * pointers are device pointers. */
+int hsr_residuals_device(int n, const double *dH, int lddH, int ncols,
+                         const double *dwr, const double *dX, int lddX,
+                         double *d_res, void *stream);
+
 /* ------------------------------------------------------- batched solves */
 /* No counterpart in the reference (it solves one H per call).  Thousands of
  * independent problems of different orders and shift counts are solved
