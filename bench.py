@@ -64,7 +64,7 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0, help="shifts in the CPU sample (0 = 64 per core)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "served"],
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "served", "stress"],
                     help="plain: n=10k solve (default); batched: 4096 mixed problems in one graph; "
                          "served: a Poisson request trace through the request loop")
     ap.add_argument("--problems", type=int, default=4096, help="batched: number of problems")
@@ -73,6 +73,7 @@ def parse():
     ap.add_argument("--pool", type=int, default=48, help="served: distinct generated matrices")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="served: HBM budget")
     ap.add_argument("--batch-tlsz", type=int, default=0, help="batched/served tile size (0: autotune)")
+    ap.add_argument("--stress-order", type=int, default=5000, help="stress: n of the robustness-stress problem")
     ap.add_argument("--only-plain", action="store_true",
                     help="default run: skip the batched and served sub-measurements")
     return ap.parse_args()
@@ -94,6 +95,22 @@ def workload(n: int, seed: int):
     np.savez(tmp, H=H, wr=wr)
     os.replace(tmp, f)
     return H, wr
+
+
+def stress_workload(n: int, seed: int):
+    """Robustness-stress problem (H, eigenvalues), cached like workload()."""
+    from hsrq3in_gb300 import generators as G
+    d = os.path.join(tempfile.gettempdir(), "hsrq3in_bench")
+    os.makedirs(d, exist_ok=True)
+    f = os.path.join(d, "stress_n%d_s%d_v1.npz" % (n, seed))
+    if os.path.exists(f):
+        z = np.load(f)
+        return np.asfortranarray(z["H"]), z["lam"]
+    H, lam = G.stress(n, seed)
+    tmp = f + ".%d.tmp.npz" % os.getpid()
+    np.savez(tmp, H=H, lam=lam)
+    os.replace(tmp, f)
+    return H, lam
 
 
 def _gen_one(args):
@@ -467,22 +484,32 @@ def served_trace(args, base, nreq, rate, seed):
     return reqs
 
 
+SHARED_OUTPUT_ABOVE = 2000   # requests; beyond this, outputs on one matrix share a host buffer
+
+
 def replay_served(base, reqs, tl, budget_gb):
-    """Replay a trace through the request loop; pinned host buffers."""
+    """Replay a trace through the request loop; pinned host buffers.  Traces
+    longer than SHARED_OUTPUT_ABOVE requests give all requests on one matrix
+    the same output buffer (n x n per matrix), which bounds the pinned host
+    memory; their results are then not kept."""
     import torch
     import hsrq3in_gb300 as hsr
     from hsrq3in_gb300 import _lib
     lib = hsr.load()
     Hp = [torch.from_numpy(np.asfortranarray(H).ravel(order="F")).pin_memory() for H, _ in base]
     total = sum(len(wr) for _, _, wr, _ in reqs)
-    outs = torch.empty(sum(n * len(wr) for _, n, wr, _ in reqs), dtype=torch.float64).pin_memory()
+    shared = len(reqs) > SHARED_OUTPUT_ABOVE
+    if shared:
+        outs_j = [torch.empty(H.shape[0] * H.shape[0], dtype=torch.float64).pin_memory() for H, _ in base]
+    else:
+        outs = torch.empty(sum(n * len(wr) for _, n, wr, _ in reqs), dtype=torch.float64).pin_memory()
     wrs = torch.empty(total, dtype=torch.float64).pin_memory()
     arr = (_lib.Request * len(reqs))()
     o = w = 0
     for i, (j, n, wr, t) in enumerate(reqs):
         wrs.numpy()[w:w + len(wr)] = wr
-        arr[i] = _lib.Request(n, Hp[j].data_ptr(), n, len(wr), wrs.data_ptr() + 8 * w, outs.data_ptr() + 8 * o,
-                              n, t)
+        optr = outs_j[j].data_ptr() if shared else outs.data_ptr() + 8 * o
+        arr[i] = _lib.Request(n, Hp[j].data_ptr(), n, len(wr), wrs.data_ptr() + 8 * w, optr, n, t)
         o += n * len(wr)
         w += len(wr)
     srv = hsr.Server(hbm_budget_bytes=budget_gb * 1e9, tlsz=tl)
@@ -539,12 +566,77 @@ def run_served(args):
             "saturated": {"server": r_burst, "plain_per_request": p_burst,
                           "speedup_server_over_plain": r_burst["eigenvectors_per_s"] / p_burst["eigenvectors_per_s"]},
             "config": "%d requests, n log-uniform [64,4096] from %d distinct generated matrices, shift fraction "
-                      "U[0.1,1], HBM budget %.0f GB, tlsz %d" % (args.requests, len(base), args.budget_gb, tl),
+                      "U[0.1,1], HBM budget %.0f GB, tlsz %d%s" % (
+                          args.requests, len(base), args.budget_gb, tl,
+                          "; outputs on one matrix share a host buffer" if args.requests > SHARED_OUTPUT_ABOVE
+                          else ""),
+            "clocks": clk.summary()}
+
+
+def run_stress(args):
+    """Config 3: the robustness-stress problem (n = 5000, 50 clusters of width
+    1e-13, strictly-upper columns scaled by 10^U[0,150], shifts equal to the
+    eigenvalues), device-resident, all n shifts: eigenvectors/s, and the
+    checks -- finiteness, device residuals of every column, perturbation and
+    scaling statistics from the extended entry point."""
+    import torch
+    import hsrq3in_gb300 as hsr
+    from hsrq3in_gb300 import _lib
+    n = args.stress_order
+    H, lam = stress_workload(n, args.seed)
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    ld = n + (n & 1)
+    dHt = torch.zeros((n, ld), dtype=torch.float64, device=dev)
+    dHt[:, :n] = torch.from_numpy(np.ascontiguousarray(H.T)).to(dev)
+    dwr0 = torch.from_numpy(np.ascontiguousarray(lam)).to(dev)
+    dwr = dwr0.clone()
+    dX = torch.empty((n, ld), dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            dwr.copy_(dwr0)
+            hsr.inverse_iteration_device(dHt, dwr, dX, args.tlsz, stream=stream)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with ClockSampler(0) as clk:
+            e0.record(stream)
+            rcs = []
+            for _ in range(args.steps):
+                dwr.copy_(dwr0)
+                rcs.append(hsr.inverse_iteration_device(dHt, dwr, dX, args.tlsz, stream=stream))
+            e1.record(stream)
+            torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    res = hsr.residuals_device(dHt, dwr, dX).cpu().numpy()
+    finite = bool(torch.isfinite(dX[:, :n]).all().item())
+    info = hsr.inverse_iteration(H, lam, args.tlsz, args.rhs_tlsz)
+    scale = info["scale"]
+    return {"value": n / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+            "whole_tflops_2n2S": 2.0 * n * n * n / (ms / 1e3) / 1e12,
+            "check": {"finite": finite, "max_residual_all_columns": float(np.max(res)),
+                      "residual_bound_10n_eps": 10 * n * 2.0 ** -52, "rc": rcs[-1] if rcs else None,
+                      "perturbed_columns": int(np.sum(info["perturbed"])),
+                      "rescaled_columns": int(np.sum(scale != 0.0)),
+                      "min_scale_exponent": float(np.min(scale)),
+                      "converged_columns": int(np.sum(info["status"]))},
+            "config": {"workload": "stress: n=%d, 50 clusters of width 1e-13, strictly-upper columns scaled by "
+                                   "10^U[0,150], shifts = eigenvalues, tlsz=%d" % (n, args.tlsz),
+                       "n": n, "nrhs": n, "tlsz": args.tlsz, "seed": args.seed},
             "clocks": clk.summary()}
 
 
 def main():
     args = parse()
+    if args.workload == "stress":
+        st = run_stress(args)
+        line = {"metric": "FP64 eigenvectors/s, robustness stress", "value": st["value"], "unit": UNIT,
+                "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": st["ms_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded generator)", "config": st["config"], "stress": st}
+        print(json.dumps(line), flush=True)
+        return
     if args.workload == "batched":
         print(json.dumps(run_batched(args)), flush=True)
         return
@@ -611,6 +703,7 @@ def main():
         line["batched"]["config"] = b["config"]
         sv = run_served(args)
         line["served"] = sv
+        line["stress"] = run_stress(args)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, t, c = cpu_sample(H, wr, args.tlsz, args.rhs_tlsz, sample, 1, 0)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": c, "kind": "port",

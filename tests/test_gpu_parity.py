@@ -64,6 +64,26 @@ def test_stress_finite_and_bitwise(gpu_lib, scaling, intscale):
     assert O.residuals(H, dev["wr"], dev["vr"]).max() <= 10 * n * EPS
 
 
+def test_stress_config_n5000(gpu_lib):
+    """The robustness-stress configuration at its full order (n = 5000,
+    clustered spectrum of width 1e-13, columns scaled by up to 1e150, shifts
+    equal to the eigenvalues), on 128 of its shifts: finite, within the
+    residual bound, and bit-identical to the oracle in vectors, perturbation
+    flags, reconciled scales and convergence."""
+    n = 5000
+    H, lam = G.stress(n, 3)
+    wr = lam[np.linspace(0, n - 1, 128).astype(int)]
+    dev = _device(H, wr, 200)
+    orc = O.oracle_inverse_iteration(H, wr, 200, 16, intscale=1, variant="fma")
+    assert np.all(np.isfinite(dev["vr"]))
+    assert np.array_equal(dev["wr"], orc["wr"])
+    assert np.array_equal(dev["vr"], orc["vr"])
+    assert np.array_equal(dev["perturbed"], orc["perturbed"])
+    assert np.array_equal(dev["scale"], orc["colscale"])
+    assert np.array_equal(dev["status"], orc["status"])
+    assert O.residuals(H, dev["wr"], dev["vr"]).max() <= 10 * n * EPS
+
+
 @pytest.mark.parametrize("kind", ["reduced", "reduced_sub", "block_scaled"])
 def test_protection_branches_pow2(gpu_lib, kind):
     """Nearly reduced and block-scaled inputs fire the division, diagonal,
