@@ -64,7 +64,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0, help="shifts in the CPU sample (0 = 64 per core)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "served", "stress"],
+    ap.add_argument("--workload", default="plain",
+                    choices=["plain", "batched", "served", "stress", "hessenberg"],
                     help="plain: n=10k solve (default); batched: 4096 mixed problems in one graph; "
                          "served: a Poisson request trace through the request loop")
     ap.add_argument("--problems", type=int, default=4096, help="batched: number of problems")
@@ -627,8 +628,59 @@ def run_stress(args):
             "clocks": clk.summary()}
 
 
+def run_hessenberg(args):
+    """The input step on the GPU: reduction of a dense n x n matrix to
+    upper-Hessenberg form (hsr_hessenberg_device), 10/3 n^3 flops, against
+    LAPACK dgehrd (scipy's OpenBLAS, its default of all host cores) at
+    min(n, 4096)."""
+    import torch
+    import hsrq3in_gb300 as hsr
+    n = args.order
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(args.seed)
+    A0 = torch.randn((n, n), dtype=torch.float64, device=dev, generator=g)
+    dA = torch.empty_like(A0)
+    stream = torch.cuda.Stream(device=dev)
+    times = []
+    with torch.cuda.stream(stream):
+        for it in range(args.warmup + args.steps):
+            dA.copy_(A0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            tau = hsr.hessenberg_device(dA, stream=stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if it >= args.warmup:
+                times.append(e0.elapsed_time(e1))
+    ms = float(np.mean(times))
+    flops = 10.0 / 3.0 * n ** 3
+    finite = bool(torch.isfinite(dA).all().item())
+    from scipy.linalg import lapack
+    nh = min(n, 4096)
+    Ah = np.asfortranarray(np.random.default_rng(args.seed).standard_normal((nh, nh)))
+    t0 = time.perf_counter()
+    lapack.dgehrd(Ah)
+    th = time.perf_counter() - t0
+    return {"n": n, "ms": ms, "tflops": flops / (ms / 1e3) / 1e12, "finite": finite,
+            "host_dgehrd": {"n": nh, "s": th, "gflops": 10.0 / 3.0 * nh ** 3 / th / 1e9,
+                            "cores": os.cpu_count(), "library": "scipy LAPACK dgehrd (OpenBLAS)"},
+            "tau_sample": float(tau[0].item())}
+
+
 def main():
     args = parse()
+    if args.workload == "hessenberg":
+        hh = run_hessenberg(args)
+        line = {"metric": "Hessenberg reduction time (dense n x n, FP64)", "value": hh["ms"], "unit": "ms",
+                "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": hh["ms"],
+                "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded N(0,1) matrix)", "config": {"workload": "hessenberg: n=%d" % hh["n"]},
+                "hessenberg": hh}
+        print(json.dumps(line), flush=True)
+        return
     if args.workload == "stress":
         st = run_stress(args)
         line = {"metric": "FP64 eigenvectors/s, robustness stress", "value": st["value"], "unit": UNIT,

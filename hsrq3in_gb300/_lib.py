@@ -27,6 +27,7 @@ EXPORTS = [
     "hsr_last_launch_count", "hsr_set_kernel_timing", "hsr_last_kernel_times",
     "hsr_release_workspace", "hsr_probe_fp64_peak", "hsr_version",
     "hsr_inverse_iteration_noalloc", "hsr_residuals_device",
+    "hsr_hessenberg_device", "hsr_hessenberg_apply_q_device",
     "hsr_batch_plan_create", "hsr_batch_plan_execute", "hsr_batch_plan_info", "hsr_batch_plan_destroy",
     "hsr_autotune_tlsz", "hsr_autotune_batch",
     "hsr_server_create", "hsr_server_replay", "hsr_server_destroy",
@@ -107,6 +108,11 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     lib.hsr_residuals_device.restype = C.c_int
     lib.hsr_residuals_device.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                          C.c_void_p, C.c_void_p]
+    lib.hsr_hessenberg_device.restype = C.c_int
+    lib.hsr_hessenberg_device.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    lib.hsr_hessenberg_apply_q_device.restype = C.c_int
+    lib.hsr_hessenberg_apply_q_device.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                                  C.c_int, C.c_void_p]
     lib.hsr_last_launch_count.restype = C.c_long
     lib.hsr_set_kernel_timing.restype = None
     lib.hsr_set_kernel_timing.argtypes = [C.c_int]

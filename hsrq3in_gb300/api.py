@@ -124,6 +124,32 @@ def residuals_device(dH, dwr, dvr, stream=None):
     return res
 
 
+def hessenberg_device(dA, stream=None):
+    """Reduce the dense matrix in dA (tensor (n, lda), rows = columns) to
+    upper-Hessenberg form in place, LAPACK layout (H on and above the
+    subdiagonal, reflectors below).  Returns the device tensor of tau."""
+    import torch
+    lib = _lib.load()
+    n = dA.shape[0]
+    tau = torch.empty(n, dtype=torch.float64, device=dA.device)
+    st = None if stream is None else C.c_void_p(stream.cuda_stream)
+    rc = lib.hsr_hessenberg_device(n, dA.data_ptr(), dA.stride(0), tau.data_ptr(), st)
+    if rc < 0:
+        raise HsrError(rc)
+    return tau
+
+
+def hessenberg_apply_q_device(dA, dtau, dX, stream=None):
+    """X <- Q X in place for the reduction stored in dA, dtau (dX: tensor
+    (ncols, ldx), rows = columns)."""
+    lib = _lib.load()
+    st = None if stream is None else C.c_void_p(stream.cuda_stream)
+    rc = lib.hsr_hessenberg_apply_q_device(dA.shape[0], dA.data_ptr(), dA.stride(0), dtau.data_ptr(),
+                                           dX.shape[0], dX.data_ptr(), dX.stride(0), st)
+    if rc < 0:
+        raise HsrError(rc)
+
+
 def fp64_peak(ms_target: float = 50.0):
     """(DFMA GFLOP/s, DMMA GFLOP/s) measured on the current GPU."""
     lib = _lib.load()

@@ -123,6 +123,22 @@ int hsr_last_kernel_times(double *ms, long *launches, double *gemm_fma);
 /* Release cached device workspaces of this thread. */
 void hsr_release_workspace(void);
 
+/* ------------------------------------------ Hessenberg reduction (device) */
+/* The input step of the solver, on the GPU: replaces the LAPACK dgehrd call
+ * of the reference's problem generator (problemgenerator.c:344) for dense
+ * inputs.  In place, with LAPACK's layout and reflector convention (dgehd2,
+ * dlarfg): on exit the upper-Hessenberg part of dA holds H, column k below
+ * the subdiagonal holds v_k(k+2 .. n-1) (v_k(k+1) = 1 implied), dtau[n] the
+ * factors, and A = Q H Q^T with Q = H_0 ... H_{n-3}, H_k = I - tau_k v_k v_k^T.
+ * Enqueued on `stream`; all pointers are device pointers.  No reference
+ * counterpart in the solver itself. */
+int hsr_hessenberg_device(int n, double *dA, int lda, double *dtau, void *stream);
+/* X <- Q X for the Q of hsr_hessenberg_device (LAPACK dormhr 'L','N'):
+ * back-transforms eigenvectors of H to eigenvectors of A, or forms Q from
+ * X = I.  dX is n x ncols, leading dimension ldx. */
+int hsr_hessenberg_apply_q_device(int n, const double *dA, int lda, const double *dtau,
+                                  int ncols, double *dX, int ldx, void *stream);
+
 /* ------------------------------------------------- residuals on the device */
 /* Replaces the residual check of validate_real_eigenvectors
  * (validation.c:145-166) for device-resident results: d_res[k] =
