@@ -17,6 +17,11 @@ instead follow the published benchmark configuration:
   upper columns scaled by 10^k, k ~ U[0, 150].
 * ``well_conditioned(n, seed)`` -- the same construction with strictly-upper
   entries scaled by 1/n, so eigenvector angles are meaningful for parity.
+* ``complex_spectrum(n, seed)`` -- T quasi-upper triangular with 2x2 blocks
+  [[a, b r], [-b / r, a]] (eigenvalues a +- i b, a on a jittered grid in
+  [-1, 1], b in [0.1, 1], r in [0.5, 2]) and N(0,1) entries above the
+  blocks, reduced to Hessenberg form the same way; the shifts of the
+  complex-shift path are the eigenvalues with positive imaginary part.
 * shift helpers: all eigenvalues with relative 1e-12 N(0,1) noise, or a
   random subset.
 
@@ -89,6 +94,37 @@ def stress(n: int, seed: int, clusters: int = 50, width: float = 1e-13,
     T = np.triu(rng.standard_normal((n, n)) * (10.0 ** k)[None, :], 1)
     T[np.diag_indices(n)] = lam
     return _hessenberg_similarity(T, rng), lam
+
+
+def complex_spectrum(n: int, seed: int, upper_scale: float = 1.0, n_real: int = 0):
+    """(H, pairs, lam_real): H of order n with (n - n_real) // 2 complex
+    conjugate pairs, returned as the eigenvalues with positive imaginary part
+    (complex array), and n_real (+1 when n - n_real is odd) real eigenvalues."""
+    rng = np.random.default_rng(seed)
+    npairs = (n - n_real) // 2
+    nreal = n - 2 * npairs
+    a = jittered_eigenvalues(npairs, rng) if npairs else np.zeros(0)
+    b = rng.uniform(0.1, 1.0, npairs)
+    r = np.exp(rng.uniform(np.log(0.5), np.log(2.0), npairs))
+    lam_r = jittered_eigenvalues(nreal, rng, min_gap=1e-6) if nreal else np.zeros(0)
+    # Diagonal blocks in random order: 2 = a pair, 1 = a real eigenvalue.
+    kinds = np.array([2] * npairs + [1] * nreal)
+    order = rng.permutation(kinds.size)
+    T = np.triu(rng.standard_normal((n, n)) * upper_scale, 1)
+    pos = 0
+    ip = ir = 0
+    for o in order:
+        if kinds[o] == 2:
+            T[pos, pos] = T[pos + 1, pos + 1] = a[ip]
+            T[pos, pos + 1] = b[ip] * r[ip]
+            T[pos + 1, pos] = -b[ip] / r[ip]
+            ip += 1
+            pos += 2
+        else:
+            T[pos, pos] = lam_r[ir]
+            ir += 1
+            pos += 1
+    return _hessenberg_similarity(T, rng), a + 1j * b, lam_r
 
 
 def block_scaled(n: int, b: int, seed: int, far: float = 1e250, diag: float = 1e-200,

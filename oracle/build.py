@@ -77,6 +77,7 @@ def build_oracle(force: bool = False) -> dict[str, str]:
     os.makedirs(BUILD_DIR, exist_ok=True)
     src = os.path.join(HERE, "hsro.c")
     hdr = os.path.join(HERE, "hsro.h")
+    inc = os.path.join(HERE, "hsro_cplx.c")     # included by hsro.c
     blas = find_openblas()
     link: list[str] = []
     defs: list[str] = []
@@ -92,7 +93,7 @@ def build_oracle(force: bool = False) -> dict[str, str]:
     out: dict[str, str] = {}
     for name, flags in variants.items():
         so = os.path.join(BUILD_DIR, "libhsro_%s.so" % name)
-        if force or _stale(so, [src, hdr, __file__]):
+        if force or _stale(so, [src, hdr, inc, __file__]):
             cmd = (["gcc", "-std=gnu11", "-fopenmp", "-fPIC", "-shared", "-Wall",
                     "-Wno-unused-function"] + flags + defs + [src, "-o", so] + link + ["-lm"])
             _run(cmd)

@@ -1088,3 +1088,7 @@ int hsro_solve_rhs(int n, const double *H, int ldH, int nrhs, const double *wr,
     free(vrnorms); free(fr); free((void *)P.Hn);
     return rc;
 }
+
+/* Complex-conjugate shifts: same translation unit, so that the extension
+ * shares the scalar kernels and helpers above. */
+#include "hsro_cplx.c"

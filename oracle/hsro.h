@@ -76,6 +76,28 @@ double hsro_protect_update(double t, double x, double y, int intscale);
 int    hsro_solve_1x1(double smin, double t, double lambda, double *x,
                       double *scale, int intscale);
 
+/* ---- Complex-conjugate shifts (hsro_cplx.c) ---------------------------- */
+/* Eigenvectors for npairs complex shifts mu_k = wr[k] + i*wi[k].  vr is
+ * n x 2*npairs (ldvr): pair k's vector has its real part in column 2k and its
+ * imaginary part in column 2k+1 (the LAPACK dhsein layout), unit 2-norm.
+ * Pairs that do not converge are solved again in place, up to max_restarts
+ * rounds (< 0: n).  perturbed/colscale/status are per pair.                 */
+int hsro_inverse_iteration_cplx(int n, const double *H, int ldH, int npairs,
+                                const double *wr, const double *wi, int tlsz,
+                                int rhs_tlsz, double *vr, int ldvr, int intscale,
+                                int max_restarts, unsigned char *perturbed,
+                                double *colscale, int *status, hsro_stats *stats);
+/* Complex Givens rotation of (f_re + i f_im, g): c, sigma = sr + i si with
+ * sigma f + c g = 0.                                                        */
+void hsro_cgivens(double fr, double fi, double g, double *c, double *sr, double *si);
+/* robust_cmplx_div (robust.c:639-675) restated. */
+int hsro_robust_cmplx_div(double smin, double a, double b, double c, double d,
+                          double *xr, double *xi, double *scale, int intscale);
+/* x := (scale x) / (t - l), complex t and l (solve_1x1_cmplx_system,
+ * robust.c:677-773, for t real).                                            */
+int hsro_csolve_1x1(double smin, double tr, double ti, double lr, double li,
+                    double *xr, double *xi, double *scale, int intscale);
+
 /* Number of OpenMP threads the oracle may use (0 = runtime default).        */
 void hsro_set_threads(int nthreads);
 /* Which arithmetic mode this build implements: 0 ref, 1 fma.                */

@@ -49,6 +49,13 @@ def _lib(variant: str) -> C.CDLL:
         lib.hsro_dlartg.restype = None
         lib.hsro_dlartg.argtypes = [C.c_double, C.c_double] + [C.POINTER(C.c_double)] * 3
         lib.hsro_set_threads.argtypes = [C.c_int]
+        lib.hsro_inverse_iteration_cplx.restype = C.c_int
+        lib.hsro_cgivens.restype = None
+        lib.hsro_cgivens.argtypes = [C.c_double] * 3 + [C.POINTER(C.c_double)] * 3
+        lib.hsro_robust_cmplx_div.restype = C.c_int
+        lib.hsro_robust_cmplx_div.argtypes = [C.c_double] * 5 + [C.POINTER(C.c_double)] * 3 + [C.c_int]
+        lib.hsro_csolve_1x1.restype = C.c_int
+        lib.hsro_csolve_1x1.argtypes = [C.c_double] * 5 + [C.POINTER(C.c_double)] * 3 + [C.c_int]
         _LIBS[variant] = lib
     return _LIBS[variant]
 
@@ -96,6 +103,54 @@ def oracle_dlartg(f: float, g: float):
     c, s, r = C.c_double(), C.c_double(), C.c_double()
     lib.hsro_dlartg(f, g, C.byref(c), C.byref(s), C.byref(r))
     return c.value, s.value, r.value
+
+
+def oracle_inverse_iteration_cplx(H, wr, wi, tlsz, rhs_tlsz, intscale=0, max_restarts=-1,
+                                  variant="fma"):
+    """Complex-conjugate shifts (oracle/hsro_cplx.c): one pair per (wr[k], wi[k]);
+    returns vr (n x 2*npairs, Re/Im column pairs), the complex vectors X
+    (n x npairs), and per-pair flags."""
+    lib = _lib(variant)
+    H = np.asfortranarray(H, dtype=np.float64)
+    n = H.shape[0]
+    wr = np.ascontiguousarray(wr, dtype=np.float64)
+    wi = np.ascontiguousarray(wi, dtype=np.float64)
+    npairs = wr.shape[0]
+    vr = np.zeros((n, 2 * npairs), dtype=np.float64, order="F")
+    pert = np.zeros(max(npairs, 1), dtype=np.uint8)
+    colscale = np.zeros(max(npairs, 1), dtype=np.float64)
+    status = np.zeros(max(npairs, 1), dtype=np.int32)
+    st = Stats()
+    rc = lib.hsro_inverse_iteration_cplx(
+        C.c_int(n), H.ctypes.data_as(C.c_void_p), C.c_int(n), C.c_int(npairs),
+        wr.ctypes.data_as(C.c_void_p), wi.ctypes.data_as(C.c_void_p), C.c_int(tlsz),
+        C.c_int(rhs_tlsz), vr.ctypes.data_as(C.c_void_p), C.c_int(n), C.c_int(intscale),
+        C.c_int(max_restarts), pert.ctypes.data_as(C.c_void_p),
+        colscale.ctypes.data_as(C.c_void_p), status.ctypes.data_as(C.c_void_p), C.byref(st))
+    if rc != 0:
+        raise RuntimeError("hsro_inverse_iteration_cplx failed with %d" % rc)
+    return dict(vr=vr, X=vr[:, 0::2] + 1j * vr[:, 1::2], perturbed=pert[:npairs].astype(bool),
+                colscale=colscale[:npairs], status=status[:npairs], stats=st.as_dict())
+
+
+def oracle_cgivens(fr: float, fi: float, g: float):
+    c, sr, si = C.c_double(), C.c_double(), C.c_double()
+    _lib("fma").hsro_cgivens(fr, fi, g, C.byref(c), C.byref(sr), C.byref(si))
+    return c.value, sr.value, si.value
+
+
+def oracle_robust_cmplx_div(smin, a, b, c, d, intscale=0):
+    xr, xi, sc = C.c_double(), C.c_double(), C.c_double()
+    info = _lib("fma").hsro_robust_cmplx_div(smin, a, b, c, d, C.byref(xr), C.byref(xi),
+                                             C.byref(sc), intscale)
+    return info, xr.value, xi.value, sc.value
+
+
+def oracle_csolve_1x1(smin, tr, ti, lr, li, xr, xi, intscale=0):
+    pr, pi, sc = C.c_double(xr), C.c_double(xi), C.c_double()
+    info = _lib("fma").hsro_csolve_1x1(smin, tr, ti, lr, li, C.byref(pr), C.byref(pi),
+                                       C.byref(sc), intscale)
+    return info, pr.value, pi.value, sc.value
 
 
 # ---------------------------------------------------------------- reference
@@ -197,6 +252,25 @@ def eigvec_angles(X: np.ndarray, Y: np.ndarray) -> np.ndarray:
     return np.where(c < 0.9, np.arccos(np.clip(c, 0, 1)), 2 * np.arcsin(np.clip(s / 2, 0, 1)))
 
 
+def phase_angles(X: np.ndarray, Y: np.ndarray) -> np.ndarray:
+    """Angle between corresponding columns of complex X and Y, invariant to a
+    unit-modulus phase: atan2(||x - y p||, |p|) with p = y^H x for unit x, y
+    (accurate for small angles, where arccos loses half the digits)."""
+    x = X / scaled_fro(X, axis=0)
+    y = Y / scaled_fro(Y, axis=0)
+    p = np.sum(np.conj(y) * x, axis=0)
+    r = scaled_fro(x - y * p[None, :], axis=0)
+    return np.arctan2(r, np.abs(p))
+
+
+def eig_vectors_for(H: np.ndarray, mu: np.ndarray) -> np.ndarray:
+    """Right eigenvectors from LAPACK dgeev (numpy) for the eigenvalues
+    nearest each shift in mu (complex), one column per shift."""
+    w, V = np.linalg.eig(np.asarray(H))
+    idx = [int(np.argmin(np.abs(w - m))) for m in np.atleast_1d(mu)]
+    return V[:, idx]
+
+
 def eigen_sensitivity(H: np.ndarray, wr: np.ndarray) -> np.ndarray:
     """Estimated eigenvector sensitivity eps*||H||_F*kappa_i/gap_i for each
     shift (nearest eigenvalue), from LAPACK dgeev left/right vectors."""
@@ -212,3 +286,27 @@ def eigen_sensitivity(H: np.ndarray, wr: np.ndarray) -> np.ndarray:
         gap = np.min(np.abs(others - w[i])) if others.size else 1.0
         out[k] = eps * hf / (s * gap) if s > 0 and gap > 0 else np.inf
     return out
+
+
+def reference_robust_cmplx_div(smin, a, b, c, d, intscale=0):
+    """robust_cmplx_div (robust.c:639-675) of the compiled reference."""
+    lib = _ref_lib(intscale)
+    fn = lib.robust_cmplx_div
+    fn.restype = C.c_int
+    xr, xi = C.c_double(), C.c_double()
+    sc = C.c_int() if intscale else C.c_double()
+    info = fn(C.c_double(smin), C.c_double(a), C.c_double(b), C.c_double(c), C.c_double(d),
+              C.byref(xr), C.byref(xi), C.byref(sc))
+    return info, xr.value, xi.value, float(sc.value)
+
+
+def reference_solve_1x1_cmplx(smin, t, lam_re, lam_im, xr, xi, intscale=0):
+    """solve_1x1_cmplx_system (robust.c:677-773) of the compiled reference."""
+    lib = _ref_lib(intscale)
+    fn = lib.solve_1x1_cmplx_system
+    fn.restype = C.c_int
+    pr, pi = C.c_double(xr), C.c_double(xi)
+    sc = C.c_int() if intscale else C.c_double()
+    info = fn(C.c_double(smin), C.c_double(t), C.c_double(lam_re), C.c_double(lam_im),
+              C.byref(pr), C.byref(pi), C.byref(sc))
+    return info, pr.value, pi.value, float(sc.value)
