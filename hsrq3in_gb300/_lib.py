@@ -31,6 +31,7 @@ EXPORTS = [
     "hsr_batch_plan_create", "hsr_batch_plan_execute", "hsr_batch_plan_info", "hsr_batch_plan_destroy",
     "hsr_autotune_tlsz", "hsr_autotune_batch",
     "hsr_server_create", "hsr_server_replay", "hsr_server_destroy",
+    "hsr_inverse_iteration_cplx_ex", "hsr_inverse_iteration_cplx_device",
 ]
 NOALLOC_MAX_N = 256
 NOALLOC_MAX_NRHS = 256
@@ -105,6 +106,14 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     lib.hsr_inverse_iteration_device.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
                                                  C.c_int, C.c_void_p, C.c_int, C.POINTER(Options),
                                                  C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.hsr_inverse_iteration_cplx_ex.restype = C.c_int
+    lib.hsr_inverse_iteration_cplx_ex.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                                  C.c_int, C.c_int, C.c_void_p, C.c_int,
+                                                  C.POINTER(Options), C.POINTER(ColumnInfo)]
+    lib.hsr_inverse_iteration_cplx_device.restype = C.c_int
+    lib.hsr_inverse_iteration_cplx_device.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                                      C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                                      C.POINTER(Options), C.c_void_p, C.c_void_p, C.c_void_p]
     lib.hsr_residuals_device.restype = C.c_int
     lib.hsr_residuals_device.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                          C.c_void_p, C.c_void_p]

@@ -107,6 +107,59 @@ def inverse_iteration_device(dH, dwr, dvr, tlsz: int, stream=None, scaling: str 
     return rc
 
 
+def inverse_iteration_cplx(H: np.ndarray, mu: np.ndarray, tlsz: int, rhs_tlsz: int = 64,
+                           scaling: str = "pow2", max_restarts: int = -1,
+                           hbm_budget_bytes: float = 0.0):
+    """Complex-conjugate shifts: one complex shift per pair (mu, complex array;
+    the vector of conj(mu) is the conjugate).  Returns a dict with vr
+    (n x 2*npairs, real part in column 2k, imaginary part in 2k+1), X (the
+    complex vectors, n x npairs), per-pair status, perturbed, scale, norm and
+    the library status code.  Shifts keep their order."""
+    lib = _lib.load()
+    H = np.asfortranarray(H, dtype=np.float64)
+    n = H.shape[0]
+    mu = np.asarray(mu, dtype=np.complex128)
+    wr = np.ascontiguousarray(mu.real)
+    wi = np.ascontiguousarray(mu.imag)
+    npairs = mu.shape[0]
+    vr = np.zeros((n, 2 * npairs), dtype=np.float64, order="F")
+    status = np.zeros(max(npairs, 1), dtype=np.int32)
+    pert = np.zeros(max(npairs, 1), dtype=np.uint8)
+    scale = np.zeros(max(npairs, 1), dtype=np.float64)
+    norm = np.zeros(max(npairs, 1), dtype=np.float64)
+    opt = _lib.Options(_scaling(scaling), 0, int(max_restarts), float(hbm_budget_bytes))
+    info = _lib.ColumnInfo(_ptr(status, C.c_int), _ptr(pert, C.c_ubyte), _ptr(scale, C.c_double),
+                           None, _ptr(norm, C.c_double))
+    rc = lib.hsr_inverse_iteration_cplx_ex(n, H.ctypes.data, H.shape[0], npairs, wr.ctypes.data, wi.ctypes.data,
+                                           int(tlsz), int(rhs_tlsz), vr.ctypes.data, vr.shape[0], C.byref(opt),
+                                           C.byref(info))
+    if rc < 0:
+        raise HsrError(rc)
+    return dict(vr=vr, X=vr[:, 0::2] + 1j * vr[:, 1::2], status=status[:npairs],
+                perturbed=pert[:npairs].astype(bool), scale=scale[:npairs], norm=norm[:npairs], rc=rc,
+                launches=lib.hsr_last_launch_count())
+
+
+def inverse_iteration_cplx_device(dH, dwr, dwi, dvr, tlsz: int, stream=None, scaling: str = "pow2",
+                                  d_status=None, d_scale=None) -> int:
+    """Device-resident complex-shift call on torch tensors: dH (n, ldh) as in
+    inverse_iteration_device, dwr/dwi (npairs,), dvr (2*npairs, ldvr) whose
+    rows 2k and 2k+1 receive the real and imaginary parts.  Returns the status
+    code; raises on errors."""
+    lib = _lib.load()
+    n = dH.shape[0]
+    opt = _lib.Options(_scaling(scaling), 0, -1, 0.0)
+    st = None if stream is None else C.c_void_p(stream.cuda_stream)
+    rc = lib.hsr_inverse_iteration_cplx_device(n, dH.data_ptr(), dH.stride(0), dwr.shape[0], dwr.data_ptr(),
+                                               dwi.data_ptr(), int(tlsz), dvr.data_ptr(), dvr.stride(0),
+                                               C.byref(opt), st,
+                                               None if d_status is None else d_status.data_ptr(),
+                                               None if d_scale is None else d_scale.data_ptr())
+    if rc < 0:
+        raise HsrError(rc)
+    return rc
+
+
 def residuals_device(dH, dwr, dvr, stream=None):
     """||H x_k - wr_k x_k|| / (||H||_F ||x_k||) per column, on the device.
     Tensors as for inverse_iteration_device: dH (n, ldh), dvr (ncols, ldvr)

@@ -211,6 +211,189 @@ struct Nrm3 {
     }
 };
 
+// ------------------------------------------------ complex-shift helpers
+// Complex values as (re, im) pairs; every product and update has one fixed
+// fma shape, the same one the oracle spells, so results match bit for bit.
+struct dcplx {
+    double re, im;
+};
+__device__ __forceinline__ dcplx cmk(double re, double im) { return dcplx{re, im}; }
+// LAPACK's CABS1: |Re z| + |Im z|, an upper bound of |z| and of each part.
+__device__ __forceinline__ double cabs1(dcplx z) { return fabs(z.re) + fabs(z.im); }
+__device__ __forceinline__ dcplx cmul(dcplx a, dcplx b) {           // a b
+    return cmk(fma(a.re, b.re, -(a.im * b.im)), fma(a.re, b.im, a.im * b.re));
+}
+__device__ __forceinline__ dcplx cmulc(dcplx a, dcplx b) {          // conj(a) b
+    return cmk(fma(a.re, b.re, a.im * b.im), fma(a.re, b.im, -(a.im * b.re)));
+}
+__device__ __forceinline__ dcplx cfma(dcplx a, dcplx b, dcplx y) {  // y + a b
+    return cmk(fma(a.re, b.re, fma(-a.im, b.im, y.re)), fma(a.re, b.im, fma(a.im, b.re, y.im)));
+}
+__device__ __forceinline__ dcplx cfnma(dcplx a, dcplx b, dcplx y) { // y - a b
+    return cmk(fma(-a.re, b.re, fma(a.im, b.im, y.re)), fma(-a.re, b.im, fma(-a.im, b.re, y.im)));
+}
+__device__ __forceinline__ dcplx cfmar(dcplx a, double h, dcplx y) { // y + a h, h real
+    return cmk(fma(a.re, h, y.re), fma(a.im, h, y.im));
+}
+__device__ __forceinline__ dcplx cscal(double c, dcplx a) { return cmk(c * a.re, c * a.im); }
+// Rotation pair of the back-transform and of Ytilde2:
+//   out = c t1 - conj(s) t2,   next = c t2 + s t1.
+__device__ __forceinline__ dcplx crot_out(double c, dcplx s, dcplx t1, dcplx t2) {
+    const dcplx q = cmulc(s, t2);
+    return cmk(fma(c, t1.re, -q.re), fma(c, t1.im, -q.im));
+}
+__device__ __forceinline__ dcplx crot_next(double c, dcplx s, dcplx t1, dcplx t2) {
+    const dcplx p = cmul(s, t1);
+    return cmk(fma(c, t2.re, p.re), fma(c, t2.im, p.im));
+}
+
+// protect_mul (robust.c:194-212): alpha with t (alpha x) safe.  Shortcut:
+// |t|, |x| < 2^497 give |t||x| < 2^994 < Omega and |t| < Omega / |x|.
+__device__ __forceinline__ double protect_mul(double tnorm, double xnorm) {
+    if (mag(tnorm) < pow2_bits(497) && mag(xnorm) < pow2_bits(497)) return 1.0;
+    double scale = 1.0;
+    if (fabs(xnorm) <= 1.0) {
+        if (fabs(tnorm) * fabs(xnorm) > kOmega) scale = 0.5;
+    } else {
+        if (fabs(tnorm) > kOmega / fabs(xnorm)) scale = 0.5 / fabs(xnorm);
+    }
+    return scale;
+}
+
+// Robust complex division in real arithmetic (robust.c:486-637): dladiv2,
+// dladiv1, dladiv, every intermediate protected by protect_sum,
+// protect_mul and protect_real_division.
+__device__ __forceinline__ void c_dladiv2(double a, double b, double c, double d, double r, double t,
+                                          double &ret, double &scale) {
+    double res, alpha = 1.0;
+    if (r != 0.0) {
+        const double br = b * r;
+        if (br != 0.0) {
+            // (a + b r) t
+            double s = protect_sum(a, br);
+            res = (s * a) + (s * br);
+            alpha = s * alpha;
+            s = protect_mul(fabs(t), fabs(res));
+            res = (s * res) * t;
+            alpha = s * alpha;
+        } else {
+            // a t + (b t) r
+            const double s1 = protect_mul(fabs(t), fabs(a));
+            double tmp1 = (s1 * a) * t;
+            const double s2 = protect_mul(fabs(t), fabs(b));
+            double tmp2 = (s2 * b) * t;
+            tmp2 = tmp2 * r;
+            const double smin = fmin(s1, s2);
+            tmp1 = tmp1 * (s1 / smin);
+            tmp2 = tmp2 * (s2 / smin);
+            alpha = smin * alpha;
+            const double s = protect_sum(tmp1, tmp2);
+            res = (s * tmp1) + (s * tmp2);
+            alpha = s * alpha;
+        }
+    } else {
+        // (a + d (b / c)) t
+        const double s1 = protect_real_division(b, c);
+        alpha = s1 * alpha;
+        double tmp = (s1 * b) / c;
+        const double s2 = protect_mul(fabs(d), fabs(tmp));
+        alpha = s2 * alpha;
+        tmp = d * (s2 * tmp);
+        a = (s1 * s2) * a;
+        double s = protect_sum(a, tmp);
+        alpha = s * alpha;
+        tmp = (s * a) + (s * tmp);
+        s = protect_mul(fabs(tmp), fabs(t));
+        alpha = s * alpha;
+        res = (s * tmp) * t;
+    }
+    scale = alpha;
+    ret = res;
+}
+__device__ __forceinline__ void c_dladiv1(double a, double b, double c, double d, double &p, double &q,
+                                          double &scale) {
+    const double r = d / c;
+    const double dr = d * r;
+    const double s1 = protect_sum(c, dr);
+    const double sum = (s1 * c) + (s1 * dr);
+    const double s2 = protect_real_division(1.0, sum);
+    const double t = 1.0 / (s2 * sum);
+    const double alpha = 1.0 / (s1 * s2);
+    double beta1 = 1.0, beta2 = 1.0;
+    c_dladiv2(a, b, c, d, r, t, p, beta1);
+    c_dladiv2(b, -a, c, d, r, t, q, beta2);
+    double beta = 1.0;
+    if (!((beta1 > 1.0 && beta2 < 1.0) || (beta1 < 1.0 && beta2 > 1.0))) {
+        beta = fmin(beta1, beta2);
+        p = p * (beta / beta1);
+        q = q * (beta / beta2);
+    }
+    scale = alpha * beta;
+}
+__device__ __forceinline__ void c_dladiv(double a, double b, double c, double d, double &xr, double &xi,
+                                         double &scale) {
+    if (fabs(d) < fabs(c)) {
+        c_dladiv1(a, b, c, d, xr, xi, scale);
+    } else {
+        c_dladiv1(b, a, d, c, xr, xi, scale);
+        xi = -xi;
+    }
+}
+// Complex 1x1 solve x := (scale x) / (t - l) (solve_1x1_cmplx_system,
+// robust.c:677-773, with a complex t); returns 1 if |t - l| was lifted to smin.
+__device__ __forceinline__ int csolve_1x1(double smin, double tr, double ti, double lr, double li, dcplx &x,
+                                          double &scale, bool is) {
+    int info = 0;
+    const double s = fmin(protect_sum(tr, -lr), protect_sum(ti, -li));
+    double csr = (s * tr) - (s * lr);
+    double csi = (s * ti) - (s * li);
+    if (fabs(csr) + fabs(csi) < smin) {
+        csr = smin;
+        csi = 0.0;
+        info = 1;
+    }
+    double alpha = 1.0;
+    c_dladiv(x.re, x.im, csr, csi, x.re, x.im, alpha);
+    scale = is ? (double)ilogb((1.0 / s) * alpha) : (1.0 / s) * alpha;
+    return info;
+}
+
+// Complex Givens rotation of (f, g), f complex, g real: c real >= 0 and
+// sigma with sigma f + c g = 0.  Exact power-of-two scaling: the phase of f
+// from f scaled by its own exponent, |f| and g on the exponent of the larger
+// (E. Anderson, "Algorithm 978: Safe scaling in the Level 1 BLAS", 2017);
+// c = 0 when |f| < 2^-600 |g|.
+__device__ __forceinline__ int exp_clamped(double m) {
+    int e = (int)((ubits(m) >> 52) & 0x7ff) - 1023;
+    return e > 1000 ? 1000 : (e < -1000 ? -1000 : e);
+}
+__device__ __forceinline__ double pow2d(int e) { return __longlong_as_double((long long)pow2_bits(e)); }
+__device__ __forceinline__ void cgivens(dcplx f, double g, double &c, dcplx &sg) {
+    if (is_zero(g)) {
+        c = 1.0;
+        sg = cmk(0.0, 0.0);
+        return;
+    }
+    if (is_zero(f.re) && is_zero(f.im)) {
+        c = 0.0;
+        sg = cmk(-copysign(1.0, g), 0.0);
+        return;
+    }
+    const int ef = exp_clamped(fmax(fabs(f.re), fabs(f.im)));
+    const int eg = exp_clamped(fabs(g));
+    const int e = ef > eg ? ef : eg;
+    const double uf = pow2d(-ef);
+    const double fsr = f.re * uf, fsi = f.im * uf;
+    const double af1 = sqrt(fma(fsr, fsr, fsi * fsi));
+    const double pr = fsr / af1, pi = fsi / af1;
+    const double af = (ef - e < -600) ? 0.0 : af1 * pow2d(ef - e);
+    const double gs = g * pow2d(-e);
+    const double d = sqrt(fma(af, af, gs * gs));
+    c = af / d;
+    const double t = gs / d;
+    sg = cmk(-(t * pr), t * pi);
+}
+
 // ------------------------------------------------ mbarrier + TMA (PTX)
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);

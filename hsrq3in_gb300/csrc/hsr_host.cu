@@ -584,6 +584,336 @@ int host_call(int n, const double *H, int ldH, int nrhs, double *wr, int tlsz, i
     return rc;
 }
 
+
+// ------------------------------------------------------- complex shifts
+// Pair p of a complex solve owns columns 2p (real part) and 2p+1 (imaginary
+// part) of X and of every per-column workspace; the shifts are interleaved
+// the same way.  A pass runs the same stage schedule as run_pass, with the
+// complex kernels (hsr_cplx.cu) and the complex epilogue of the GEMM; off and
+// cnt count columns and are even.
+int run_pass_c(Solver &s, int mode, int its, int off, int cnt) {
+    Workspace &w = *s.w;
+    HSR_CK(w.ensure_side());
+    cudaStream_t M = s.st, D = w.side;
+    bool gvy = false;
+    diag_c_smem_bytes(s.tlsz, &gvy);
+    double *gs = gvy ? w.gscratch.as<double>() : nullptr;
+    for (int c0 = 0; c0 < cnt; c0 += s.Scap) {
+        const int cc = std::min(s.Scap, cnt - c0);
+        DevProblem P0 = problem_for(s, off + c0, cc, 0);
+        HSR_LAUNCH_C(kcSetup, M, launch_init_c(P0, mode, s.eps3_dev, its, M));
+        {
+            const int J = s.T - 1;
+            DevProblem P = problem_for(s, off + c0, cc, J & 1);
+            HSR_LAUNCH_C(kcDiag, M, launch_diag_c(P, J, s.fr[J + 1] - s.fr[J], gs, M));
+        }
+        for (int J = s.T - 1; J >= 1; --J) {
+            const int bj = s.fr[J + 1] - s.fr[J];
+            DevProblem P = problem_for(s, off + c0, cc, J & 1);
+            DevProblem Pn = problem_for(s, off + c0, cc, (J - 1) & 1);
+            HSR_LAUNCH_C(kcPart1, M, launch_part1_c(P, J, M));
+            HSR_CK(cudaEventRecord(w.ev_top, M));
+            HSR_CK(cudaStreamWaitEvent(D, w.ev_top, 0));
+            HSR_LAUNCH_C(kcGemmTop, D,
+                         launch_gemm_c(P, J, s.fr[J - 1], s.fr[J], s.tmH, s.tmW[J & 1], s.tmZ[J & 1], D));
+            HSR_LAUNCH_C(kcDiag, D, launch_diag_c(Pn, J - 1, s.fr[J] - s.fr[J - 1], gs, D));
+            HSR_CK(cudaEventRecord(w.ev_diag, D));
+            if (s.fr[J - 1] > 0)
+                HSR_LAUNCH_C(kcGemm, M,
+                             launch_gemm_c(P, J, 0, s.fr[J - 1], s.tmH, s.tmW[J & 1], s.tmZ[J & 1], M));
+            HSR_CK(cudaStreamWaitEvent(M, w.ev_diag, 0));
+            if (g_timing.enabled) g_timing.gemm_fma[0] += (double)s.fr[J - 1] * (2.0 * bj - 1.0) * cc;
+        }
+        DevProblem P = problem_for(s, off + c0, cc, 0);
+        HSR_LAUNCH_C(kcFinal, M, launch_finalize_c(P, s.d_colnorm + off + c0, s.d_status + off + c0,
+                                                   s.d_scale ? s.d_scale + (off + c0) / 2 : nullptr, M));
+        HSR_LAUNCH_C(kcFinal, M, launch_normalize(P, s.d_colnorm + off + c0, s.d_status + off + c0, M));
+    }
+    return HSR_OK;
+}
+
+// Complex solve on device data: H (ldh even, aligned), dwc [2*np] interleaved
+// shifts (a workspace copy: permuted during restarts and restored before
+// return), X n x 2np.  Pairs that do not converge are solved again with the
+// restart vectors of successive rounds; their positions are unchanged on
+// return.  Host outputs are per pair.
+int solve_device_cplx(int n, const double *dH, long long ldh, int np, double *dwc, int tlsz, double *dX,
+                      long long ldx, const hsr_options *opt, cudaStream_t st, int *d_status_pairs,
+                      double *d_scale_pairs, std::vector<int> *h_status, std::vector<unsigned char> *h_pert,
+                      std::vector<double> *h_scale, std::vector<double> *h_norm) {
+    Workspace &w = ws();
+    hsr_options o{};
+    if (opt) o = *opt;
+    Solver s{};
+    s.n = n;
+    s.tlsz = tlsz;
+    s.T = (n + tlsz - 1) / tlsz;
+    s.is = o.scaling == HSR_SCALING_DOUBLE ? 0 : 1;
+    partition(n, s.T, tlsz, s.fr);
+    s.H = dH;
+    s.ldh = ldh;
+    s.X = dX;
+    s.ldx = ldx;
+    s.wr = dwc;
+    const int S = 2 * np;
+    s.S = S;
+    s.st = st;
+    s.w = &w;
+    {
+        const double eps = DBL_EPSILON / 2;
+        s.smlnum = std::fmax(2 * DBL_MIN, DBL_MIN * ((double)n / eps));
+    }
+    const int T = s.T;
+    {
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        double budget = o.hbm_budget_bytes > 0 ? o.hbm_budget_bytes : 0.6 * (double)free_b;
+        const double per_col = 8.0 * (4.0 * round_up(n, 4) + 4.0 * tlsz + 2.0 * T + 16) + T + 2.0 * tlsz * 8;
+        long long cap = (long long)(budget / per_col);
+        cap = std::max<long long>(64, std::min<long long>(cap, S));
+        cap = std::min<long long>(cap, 65534);
+        s.Scap = (int)(cap & ~1LL);
+    }
+    s.Spad = (int)round_up(s.Scap, 64);
+    const size_t Sp = (size_t)s.Spad;
+    const size_t ldr = (size_t)round_up(n, 4);
+    HSR_CK(w.R.ensure(ldr * Sp * 8));
+    HSR_CK(w.Cr.ensure((size_t)n * Sp * 8));
+    HSR_CK(w.Sr.ensure((size_t)n * Sp * 8));
+    HSR_CK(w.beta.ensure((size_t)T * Sp * 8));
+    HSR_CK(w.ynorm.ensure((size_t)T * Sp * 8));
+    HSR_CK(w.W.ensure(2 * (size_t)tlsz * Sp * 8));
+    HSR_CK(w.Zs.ensure(2 * (size_t)tlsz * Sp * 8));
+    HSR_CK(w.vecs.ensure(2 * 4 * Sp * 8));
+    HSR_CK(w.Zslow.ensure((size_t)T * tlsz * Sp * 8));
+    HSR_CK(w.slow.ensure((size_t)T * Sp));
+    HSR_CK(w.fr.ensure((size_t)(T + 1) * sizeof(int)));
+    HSR_CK(w.bits.ensure((2 * (size_t)T * T + 2) * 8));
+    HSR_CK(w.err.ensure(16));
+    HSR_CK(w.colnorm.ensure((size_t)S * 8));
+    HSR_CK(w.status.ensure((size_t)S * sizeof(int)));
+    HSR_CK(w.pert.ensure((size_t)S));
+    HSR_CK(w.scale.ensure((size_t)np * 8));
+    {
+        bool gvy = false;
+        diag_c_smem_bytes(tlsz, &gvy);
+        if (gvy) HSR_CK(w.gscratch.ensure((size_t)((Sp / 2 + 31) / 32) * 4 * 32 * tlsz * 8));
+    }
+    HSR_CK(cudaMemsetAsync(w.W.p, 0, 2 * (size_t)tlsz * Sp * 8, st));
+    HSR_CK(cudaMemsetAsync(w.Zs.p, 0, 2 * (size_t)tlsz * Sp * 8, st));
+    HSR_CK(cudaMemsetAsync(w.err.p, 0, 16, st));
+    HSR_CK(cudaMemcpyAsync(w.fr.p, s.fr.data(), (T + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+    s.d_status = w.status.as<int>();
+    s.d_colnorm = w.colnorm.as<double>();
+    s.d_scale = w.scale.as<double>();
+    s.d_pert = w.pert.as<unsigned char>();
+
+    if (!make_map(&s.tmH, dH, (unsigned long long)n, (unsigned long long)n, (unsigned long long)ldh, kGemmBM,
+                  kGemmKC) ||
+        !make_map(&s.tmW[0], w.W.as<double>(), Sp, (unsigned long long)tlsz, Sp, kGemmBN, kGemmKC) ||
+        !make_map(&s.tmW[1], w.W.as<double>() + (size_t)tlsz * Sp, Sp, (unsigned long long)tlsz, Sp, kGemmBN,
+                  kGemmKC) ||
+        !make_map(&s.tmZ[0], w.Zs.as<double>(), Sp, (unsigned long long)tlsz, Sp, kGemmBN, kGemmKC) ||
+        !make_map(&s.tmZ[1], w.Zs.as<double>() + (size_t)tlsz * Sp, Sp, (unsigned long long)tlsz, Sp, kGemmBN,
+                  kGemmKC))
+        return HSR_ERR_CUDA;
+
+    unsigned long long *bits = w.bits.as<unsigned long long>();
+    HSR_CK(cudaMemsetAsync(bits, 0, (2 * (size_t)T * T + 2) * 8, st));
+    {
+        DevProblem P0 = problem_for(s, 0, std::min(S, s.Scap));
+        HSR_LAUNCH_C(kcSetup, st, launch_norms(P0, bits, bits + (size_t)T * T, bits + 2 * (size_t)T * T,
+                                               w.err.as<int>() + 1, st));
+        ++g_launches;
+    }
+    double hinf = 0.0;
+    HSR_CK(cudaMemcpyAsync(&hinf, bits + 2 * (size_t)T * T, 8, cudaMemcpyDeviceToHost, st));
+    int nanflag[2] = {0, 0};
+    HSR_CK(cudaMemcpyAsync(nanflag, w.err.as<int>(), 8, cudaMemcpyDeviceToHost, st));
+    HSR_CK(cudaStreamSynchronize(st));
+    if (nanflag[1] & 1) hinf = NAN;
+    const double eps3 = hinf * (DBL_EPSILON / 2);
+    s.eps3_dev = reinterpret_cast<double *>(bits + 2 * (size_t)T * T + 1);
+    HSR_CK(cudaMemcpyAsync(s.eps3_dev, &eps3, 8, cudaMemcpyHostToDevice, st));
+
+    int rc = run_pass_c(s, 0, 0, 0, S);
+    if (rc) return rc;
+
+    // Restarts: stable partition of the pairs (converged first), tracked in
+    // `order` so that the original positions are restored at the end.
+    std::vector<int> order(np), st_h(S);
+    for (int p = 0; p < np; ++p) order[p] = p;
+    bool permuted = false;
+    auto apply_perm = [&](int front, const std::vector<int> &perm) -> int {
+        const int m = (int)perm.size();
+        std::vector<int> cperm(2 * m);
+        for (int q = 0; q < m; ++q) {
+            cperm[2 * q] = 2 * perm[q];
+            cperm[2 * q + 1] = 2 * perm[q] + 1;
+        }
+        HSR_CK(w.tmpX.ensure((size_t)n * 2 * m * 8));
+        HSR_CK(w.perm.ensure((size_t)2 * m * sizeof(int)));
+        HSR_CK(cudaMemcpyAsync(w.perm.p, cperm.data(), 2 * m * sizeof(int), cudaMemcpyHostToDevice, st));
+        HSR_LAUNCH_C(kcOther, st, launch_gather_cols(w.tmpX.as<double>(), n, dX + (size_t)2 * front * ldx, ldx,
+                                                     n, w.perm.as<int>(), 2 * m, st));
+        HSR_CK(cudaMemcpy2DAsync(dX + (size_t)2 * front * ldx, ldx * 8, w.tmpX.p, (size_t)n * 8, (size_t)n * 8,
+                                 2 * m, cudaMemcpyDeviceToDevice, st));
+        auto permute = [&](void *dptr, size_t elem) -> int {
+            std::vector<unsigned char> a((size_t)m * elem), b((size_t)m * elem);
+            unsigned char *base = reinterpret_cast<unsigned char *>(dptr) + (size_t)front * elem;
+            HSR_CK(cudaMemcpyAsync(a.data(), base, (size_t)m * elem, cudaMemcpyDeviceToHost, st));
+            HSR_CK(cudaStreamSynchronize(st));
+            for (int j = 0; j < m; ++j) memcpy(&b[(size_t)j * elem], &a[(size_t)perm[j] * elem], elem);
+            HSR_CK(cudaMemcpyAsync(base, b.data(), (size_t)m * elem, cudaMemcpyHostToDevice, st));
+            HSR_CK(cudaStreamSynchronize(st));
+            return HSR_OK;
+        };
+        int r;
+        if ((r = permute(dwc, 16))) return r;
+        if ((r = permute(s.d_scale, 8))) return r;
+        if ((r = permute(s.d_pert, 2))) return r;
+        if ((r = permute(s.d_status, 2 * sizeof(int)))) return r;
+        if ((r = permute(s.d_colnorm, 16))) return r;
+        std::vector<int> no(order.begin() + front, order.begin() + front + m);
+        for (int q = 0; q < m; ++q) order[front + q] = no[perm[q]];
+        return HSR_OK;
+    };
+    int front = 0, its = 0;
+    const int max_its = o.max_restarts < 0 ? n : std::min(o.max_restarts, n);
+    while (np > 0) {
+        HSR_CK(cudaMemcpyAsync(st_h.data() + 2 * front, s.d_status + 2 * front, (size_t)(S - 2 * front) * sizeof(int),
+                               cudaMemcpyDeviceToHost, st));
+        HSR_CK(cudaStreamSynchronize(st));
+        int all = 1;
+        for (int p = front; p < np; ++p)
+            if (!st_h[2 * p]) all = 0;
+        if (all || its >= max_its) break;
+        const int m = np - front;
+        std::vector<int> perm;
+        perm.reserve(m);
+        for (int q = 0; q < m; ++q)
+            if (st_h[2 * (front + q)]) perm.push_back(q);
+        const int nc = (int)perm.size();
+        for (int q = 0; q < m; ++q)
+            if (!st_h[2 * (front + q)]) perm.push_back(q);
+        if ((rc = apply_perm(front, perm))) return rc;
+        permuted = true;
+        for (int q = 0; q < nc; ++q) st_h[2 * (front + q)] = st_h[2 * (front + q) + 1] = 1;
+        front += nc;
+        rc = run_pass_c(s, 1, its, 2 * front, 2 * (np - front));
+        if (rc) return rc;
+        ++its;
+    }
+    if (permuted) {
+        HSR_CK(cudaMemcpyAsync(st_h.data(), s.d_status, (size_t)S * sizeof(int), cudaMemcpyDeviceToHost, st));
+        HSR_CK(cudaStreamSynchronize(st));
+        std::vector<int> inv(np);
+        for (int q = 0; q < np; ++q) inv[order[q]] = q;
+        std::vector<int> st2(S);
+        for (int p = 0; p < np; ++p) st2[2 * p] = st2[2 * p + 1] = st_h[2 * inv[p]];
+        if ((rc = apply_perm(0, inv))) return rc;
+        st_h.swap(st2);
+    }
+    int nonconv = 0;
+    for (int p = 0; p < np; ++p) nonconv += !st_h[2 * p];
+
+    int errw = 0;
+    HSR_CK(cudaMemcpyAsync(&errw, w.err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    HSR_CK(cudaStreamSynchronize(st));
+    g_timing.resolve();
+    if (errw) return HSR_ERR_DEVICE;
+    if (d_status_pairs)
+        HSR_CK(cudaMemcpy2DAsync(d_status_pairs, sizeof(int), s.d_status, 2 * sizeof(int), sizeof(int), np,
+                                 cudaMemcpyDeviceToDevice, st));
+    if (d_scale_pairs)
+        HSR_CK(cudaMemcpyAsync(d_scale_pairs, s.d_scale, (size_t)np * 8, cudaMemcpyDeviceToDevice, st));
+    if (h_status) {
+        h_status->resize(np);
+        for (int p = 0; p < np; ++p) (*h_status)[p] = st_h[2 * p];
+    }
+    if (h_pert) {
+        std::vector<unsigned char> t(S);
+        HSR_CK(cudaMemcpy(t.data(), s.d_pert, S, cudaMemcpyDeviceToHost));
+        h_pert->resize(np);
+        for (int p = 0; p < np; ++p) (*h_pert)[p] = t[2 * p];
+    }
+    if (h_scale) {
+        h_scale->resize(np);
+        HSR_CK(cudaMemcpy(h_scale->data(), s.d_scale, (size_t)np * 8, cudaMemcpyDeviceToHost));
+    }
+    if (h_norm) {
+        std::vector<double> t(S);
+        HSR_CK(cudaMemcpy(t.data(), s.d_colnorm, (size_t)S * 8, cudaMemcpyDeviceToHost));
+        h_norm->resize(np);
+        for (int p = 0; p < np; ++p) (*h_norm)[p] = t[2 * p];
+    }
+    if (d_status_pairs || d_scale_pairs) HSR_CK(cudaStreamSynchronize(st));
+    return nonconv ? HSR_ERR_NOT_CONVERGED : HSR_OK;
+}
+
+int check_args_c(int n, int ldH, int np, int tlsz, int ldvr, const void *H, const void *wr, const void *wi,
+                 const void *vr) {
+    if (n <= 0 || ldH < n || np < 0 || tlsz <= 0 || (tlsz % 4) != 0 || ldvr < n || !H) return HSR_ERR_ARG;
+    if (np > 0 && (!wr || !wi || !vr)) return HSR_ERR_ARG;
+    return HSR_OK;
+}
+
+int host_call_c(int n, const double *H, int ldH, int np, const double *wr, const double *wi, int tlsz,
+                int rhs_tlsz, double *vr, int ldvr, const hsr_options *opt, hsr_column_info *info) {
+    g_launches = 0;
+    g_timing.reset();
+    int rc = check_args_c(n, ldH, np, tlsz, ldvr, H, wr, wi, vr);
+    if (rc) return rc;
+    if (rhs_tlsz <= 0) return HSR_ERR_ARG;
+    if (opt && opt->user_rhs) return HSR_ERR_ARG;
+    if (np == 0) return HSR_OK;
+    Workspace &w = ws();
+    if (!w.stream) HSR_CK(cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking));
+    cudaStream_t st = w.stream;
+    const long long ldh = (ldH % 2 == 0) ? ldH : round_up(n, 32);
+    const long long ldx = ldvr;
+    HSR_CK(w.H.ensure((size_t)ldh * n * 8));
+    HSR_CK(w.X.ensure((size_t)ldx * 2 * np * 8));
+    HSR_CK(w.wr.ensure((size_t)2 * np * 8));
+    std::vector<double> wc(2 * (size_t)np);
+    for (int p = 0; p < np; ++p) {
+        wc[2 * p] = wr[p];
+        wc[2 * p + 1] = wi[p];
+    }
+    g_timing.begin(kcH2D, st);
+    if (ldh == ldH)
+        HSR_CK(cudaMemcpyAsync(w.H.p, H, ((size_t)ldH * (n - 1) + n) * 8, cudaMemcpyHostToDevice, st));
+    else
+        HSR_CK(cudaMemcpy2DAsync(w.H.p, ldh * 8, H, (size_t)ldH * 8, (size_t)n * 8, n, cudaMemcpyHostToDevice, st));
+    HSR_CK(cudaMemcpyAsync(w.wr.p, wc.data(), (size_t)2 * np * 8, cudaMemcpyHostToDevice, st));
+    g_timing.end(st);
+    std::vector<int> hs;
+    std::vector<unsigned char> hp;
+    std::vector<double> hsc, hn;
+    const bool want = info != nullptr;
+    rc = solve_device_cplx(n, w.H.as<double>(), ldh, np, w.wr.as<double>(), tlsz, w.X.as<double>(), ldx, opt, st,
+                           nullptr, nullptr, want && info->status ? &hs : nullptr,
+                           want && info->perturbed ? &hp : nullptr, want && info->scale ? &hsc : nullptr,
+                           want && info->norm ? &hn : nullptr);
+    if (rc < 0) return rc;
+    g_timing.begin(kcD2H, st);
+    if (ldvr == n)
+        HSR_CK(cudaMemcpyAsync(vr, w.X.p, (size_t)n * 2 * np * 8, cudaMemcpyDeviceToHost, st));
+    else
+        HSR_CK(cudaMemcpy2DAsync(vr, (size_t)ldvr * 8, w.X.p, ldx * 8, (size_t)n * 8, 2 * np,
+                                 cudaMemcpyDeviceToHost, st));
+    g_timing.end(st);
+    HSR_CK(cudaStreamSynchronize(st));
+    g_timing.resolve();
+    if (want) {
+        if (info->status) memcpy(info->status, hs.data(), (size_t)np * sizeof(int));
+        if (info->perturbed) memcpy(info->perturbed, hp.data(), (size_t)np);
+        if (info->scale) memcpy(info->scale, hsc.data(), (size_t)np * 8);
+        if (info->norm) memcpy(info->norm, hn.data(), (size_t)np * 8);
+    }
+    return rc;
+}
+
 }  // namespace
 }  // namespace hsr
 
@@ -641,6 +971,49 @@ int hsr_inverse_iteration_device(int n, const double *dH, int lddH, int nrhs, do
     }
     rc = solve_device(n, Huse, ldh, nrhs, dwr, tlsz, dvr, lddvr, opt, st, d_scale, d_status, nullptr, nullptr,
                       nullptr, nullptr, nullptr);
+    return g_last_status = rc;
+}
+
+int hsr_inverse_iteration_cplx_ex(int n, const double *H, int ldH, int npairs, const double *wr, const double *wi,
+                                  int tlsz, int rhs_tlsz, double *vr, int ldvr, const hsr_options *opt,
+                                  hsr_column_info *info) {
+    g_last_status = host_call_c(n, H, ldH, npairs, wr, wi, tlsz, rhs_tlsz, vr, ldvr, opt, info);
+    return g_last_status;
+}
+
+int hsr_inverse_iteration_cplx_device(int n, const double *dH, int lddH, int npairs, const double *dwr,
+                                      const double *dwi, int tlsz, double *dvr, int lddvr, const hsr_options *opt,
+                                      void *stream, int *d_status, double *d_scale) {
+    g_launches = 0;
+    g_timing.reset();
+    int rc = check_args_c(n, lddH, npairs, tlsz, lddvr, dH, dwr, dwi, dvr);
+    if (rc) return g_last_status = rc;
+    if (opt && opt->user_rhs) return g_last_status = HSR_ERR_ARG;
+    if (npairs == 0) return g_last_status = HSR_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    Workspace &w = ws();
+    const double *Huse = dH;
+    long long ldh = lddH;
+    cudaError_t e = cudaSuccess;
+    if ((lddH & 1) || (reinterpret_cast<uintptr_t>(dH) & 15)) {
+        ldh = round_up(n, 32);
+        e = w.H.ensure((size_t)ldh * n * 8);
+        if (e == cudaSuccess)
+            e = cudaMemcpy2DAsync(w.H.p, ldh * 8, dH, (size_t)lddH * 8, (size_t)n * 8, n, cudaMemcpyDeviceToDevice, st);
+        Huse = w.H.as<double>();
+    }
+    // Interleave the shifts (re, im) into the workspace copy.
+    if (e == cudaSuccess) e = w.wr.ensure((size_t)2 * npairs * 8);
+    if (e == cudaSuccess)
+        e = cudaMemcpy2DAsync(w.wr.p, 16, dwr, 8, 8, npairs, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpy2DAsync(w.wr.as<double>() + 1, 16, dwi, 8, 8, npairs, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) {
+        last_cuda_error() = e;
+        return g_last_status = HSR_ERR_CUDA;
+    }
+    rc = solve_device_cplx(n, Huse, ldh, npairs, w.wr.as<double>(), tlsz, dvr, lddvr, opt, st, d_status, d_scale,
+                           nullptr, nullptr, nullptr, nullptr);
     return g_last_status = rc;
 }
 

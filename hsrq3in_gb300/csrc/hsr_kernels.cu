@@ -730,6 +730,80 @@ struct GemmSmem {
 
 size_t gemm_smem_bytes() { return sizeof(GemmSmem) + 128; }
 
+// Complex-shift epilogue: columns (2p, 2p+1) hold the real and imaginary
+// parts of pair p, the same thread owns both, and every scalar of the real
+// epilogue becomes its complex counterpart (crossover coefficient pi, Part-1
+// ytilde, shift mu, zlast, the old crossover column); the bound folded into
+// ynorm is the largest cabs1 of the pair's rows, kept at column 2p.
+__device__ __forceinline__ void gemm_epilogue_cplx(const DevProblem &P, int J, int row_lo, int row_hi, int row0,
+                                                   int col0, const double *eaw, const double *eaz, int kEpiLd) {
+    const int tid = threadIdx.x;
+    const int l = P.fr[J], b = P.fr[J + 1] - l;
+    const size_t Spad = (size_t)P.Spad;
+    unsigned long long *ynb = reinterpret_cast<unsigned long long *>(P.ynorm);
+    const int lane = tid & 31;
+    const int er = tid & (kGemmBM - 1), cg = tid >> 6;
+    const int row = row0 + er;
+    const bool rowok = row >= row_lo && row < row_hi;
+    int I = P.T - 1 - (P.n - 1 - row) / P.tlsz;
+    if (I < 0) I = 0;
+    const int key = rowok ? I : -1;
+    const double hl1 = rowok ? P.H[row + (size_t)(l - 1) * P.ldh] : 0.0;
+    for (int j = 0; j < kGemmBN / 4; j += 2) {
+        const int cc = cg * (kGemmBN / 4) + j;
+        const int col = col0 + cc;
+        if (col >= P.S) break;
+        const dcplx pik = cmk(P.pi[col], P.pi[col + 1]);
+        const dcplx w0 = cmk(P.W[col], P.W[col + 1]);
+        const dcplx zl = cmk(P.zlast[col], P.zlast[col + 1]);
+        const dcplx mu = cmk(P.wr[col], P.wr[col + 1]);
+        const dcplx yt = cmk(P.ytil[col], P.ytil[col + 1]);
+        unsigned long long m = 0;
+        if (rowok) {
+            const size_t ir = row + (size_t)col * P.ldr;
+            const size_t ix = row + (size_t)col * P.ldx;
+            const dcplx rold = cmk(P.R[ir], P.R[ir + P.ldr]);
+            dcplx rnew = cfma(pik, rold, cmk(eaw[cc * kEpiLd + er], eaw[(cc + 1) * kEpiLd + er]));
+            if (row == l - 1) rnew = cfnma(mu, w0, rnew);
+            P.R[ir] = rnew.re;
+            P.R[ir + P.ldr] = rnew.im;
+            dcplx yv = cmk(P.X[ix], P.X[ix + P.ldx]);
+            const unsigned char fl = P.slow[(size_t)I * Spad + col];
+            if (fl & 2) {
+                yv = cmk(fma(-hl1, yt.re, yv.re), fma(-hl1, yt.im, yv.im));
+                if (row == l - 1) yv = cfma(mu, yt, yv);
+            }
+            if (fl & 1) {
+                const double *zs = P.Zslow + (size_t)I * P.tlsz * Spad + col;
+                const double *hr = P.H + row + (size_t)l * P.ldh;
+                double ar = 0.0, ai = 0.0;
+                for (int q = 0; q < b - 1; ++q) {
+                    const double h = hr[(size_t)q * P.ldh];
+                    ar = fma(h, zs[(size_t)q * Spad], ar);
+                    ai = fma(h, zs[(size_t)q * Spad + 1], ai);
+                }
+                yv = cmk(yv.re - ar, yv.im - ai);
+                yv = cfnma(rold, cmk(zs[(size_t)(b - 1) * Spad], zs[(size_t)(b - 1) * Spad + 1]), yv);
+            } else {
+                yv = cmk(yv.re - eaz[cc * kEpiLd + er], yv.im - eaz[(cc + 1) * kEpiLd + er]);
+                yv = cfnma(rold, zl, yv);
+            }
+            P.X[ix] = yv.re;
+            P.X[ix + P.ldx] = yv.im;
+            m = abs_bits(cabs1(yv));
+        }
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned long long mo = __shfl_up_sync(0xffffffffu, m, d);
+            const int ko = __shfl_up_sync(0xffffffffu, key, d);
+            if (lane >= d && ko == key) m = umax64(m, mo);
+        }
+        const int kn = __shfl_down_sync(0xffffffffu, key, 1);
+        if (rowok && (lane == 31 || kn != key)) atomicMax(&ynb[(size_t)I * Spad + col], m);
+    }
+}
+
+template <bool kCplx>
 __device__ __forceinline__ void gemm_body(const DevProblem &P, int J, int row_lo, int row_hi, int bx, int by,
                                           const CUtensorMap *tmH, const CUtensorMap *tmW,
                                           const CUtensorMap *tmZ) {
@@ -833,6 +907,10 @@ __device__ __forceinline__ void gemm_body(const DevProblem &P, int J, int row_lo
             }
     }
     __syncthreads();
+    if constexpr (kCplx) {
+        gemm_epilogue_cplx(P, J, row_lo, row_hi, row0, col0, eaw, eaz, kEpiLd);
+        return;
+    }
 
     const size_t Spad = (size_t)P.Spad;
     unsigned long long *ynb = reinterpret_cast<unsigned long long *>(P.ynorm);
@@ -895,7 +973,13 @@ __device__ __forceinline__ void gemm_body(const DevProblem &P, int J, int row_lo
 __global__ void __launch_bounds__(256, 2)
 k_gemm(DevProblem P, int J, int row_lo, int row_hi, const __grid_constant__ CUtensorMap tmH,
        const __grid_constant__ CUtensorMap tmW, const __grid_constant__ CUtensorMap tmZ) {
-    gemm_body(P, J, row_lo, row_hi, blockIdx.x, blockIdx.y, &tmH, &tmW, &tmZ);
+    gemm_body<false>(P, J, row_lo, row_hi, blockIdx.x, blockIdx.y, &tmH, &tmW, &tmZ);
+}
+
+__global__ void __launch_bounds__(256, 2)
+k_gemm_c(DevProblem P, int J, int row_lo, int row_hi, const __grid_constant__ CUtensorMap tmH,
+         const __grid_constant__ CUtensorMap tmW, const __grid_constant__ CUtensorMap tmZ) {
+    gemm_body<true>(P, J, row_lo, row_hi, blockIdx.x, blockIdx.y, &tmH, &tmW, &tmZ);
 }
 
 cudaError_t launch_gemm(const DevProblem &P, int J, int row_lo, int row_hi, const CUtensorMap &tmH,
@@ -911,6 +995,22 @@ cudaError_t launch_gemm(const DevProblem &P, int J, int row_lo, int row_hi, cons
     const int span = row_hi - (row_lo & ~7);
     dim3 g((span + kGemmBM - 1) / kGemmBM, (P.S + kGemmBN - 1) / kGemmBN);
     k_gemm<<<g, 256, smem, st>>>(P, J, row_lo, row_hi, tmH, tmW, tmZ);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gemm_c(const DevProblem &P, int J, int row_lo, int row_hi, const CUtensorMap &tmH,
+                          const CUtensorMap &tmW, const CUtensorMap &tmZ, cudaStream_t st) {
+    static bool configured = false;
+    const size_t smem = gemm_smem_bytes();
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    if (row_hi <= row_lo) return cudaSuccess;
+    const int span = row_hi - (row_lo & ~7);
+    dim3 g((span + kGemmBM - 1) / kGemmBM, (P.S + kGemmBN - 1) / kGemmBN);
+    k_gemm_c<<<g, 256, smem, st>>>(P, J, row_lo, row_hi, tmH, tmW, tmZ);
     return cudaGetLastError();
 }
 
@@ -1125,7 +1225,7 @@ __global__ void __launch_bounds__(256, 2) k_gemm_b(const DevProblem *__restrict_
     const int J = it.y;
     const bool top = (it.z & kGemmTopFlag) != 0;
     const int lo = top ? P.fr[J - 1] : 0, hi = top ? P.fr[J] : P.fr[J - 1];
-    gemm_body(P, J, lo, hi, it.z & ~kGemmTopFlag, it.w, m, m + 1, m + 2);
+    gemm_body<false>(P, J, lo, hi, it.z & ~kGemmTopFlag, it.w, m, m + 1, m + 2);
 }
 
 __global__ void __launch_bounds__(32) k_finalize_b(const DevProblem *probs, const BatchItem *items) {

@@ -100,6 +100,21 @@ constexpr int kNormRows = 128;        // rows per norms item
 constexpr int kNormalizeCols = 8;     // columns per normalize item
 constexpr int kPart1Shifts = 256;     // shifts per part-1 block (a lane per shift)
 
+// Complex-conjugate shifts (hsr_cplx.cu).  The problem's S counts real
+// columns: pair p owns columns 2p (real part) and 2p+1 (imaginary part), and
+// P.wr holds the shifts interleaved the same way.
+cudaError_t launch_init_c(const DevProblem &P, int mode, const double *eps3_dev, int its, cudaStream_t st);
+// Shared memory of k_diag_c for tile height b; *global_vy tells whether v/y
+// need the global scratch region of 4*32*b doubles per 32 pairs instead.
+size_t diag_c_smem_bytes(int b, bool *global_vy);
+cudaError_t launch_diag_c(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st);
+cudaError_t launch_part1_c(const DevProblem &P, int J, cudaStream_t st);
+cudaError_t launch_gemm_c(const DevProblem &P, int J, int row_lo, int row_hi, const CUtensorMap &tmH,
+                          const CUtensorMap &tmW, const CUtensorMap &tmZ, cudaStream_t st);
+// colnorm/status per column (both columns of a pair), scale_out per pair.
+cudaError_t launch_finalize_c(const DevProblem &P, double *colnorm, int *status, double *scale_out,
+                              cudaStream_t st);
+
 // FP64 throughput probe kernels.
 cudaError_t launch_probe_dfma(double *out, int blocks, int iters, cudaStream_t st);
 cudaError_t launch_probe_dmma(double *out, int blocks, int iters, cudaStream_t st);

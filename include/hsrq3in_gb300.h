@@ -107,6 +107,33 @@ int hsr_inverse_iteration_device(int n, const double *dH, int lddH, int nrhs,
                                  const hsr_options *opt, void *stream,
                                  int *d_status, double *d_scale);
 
+/* ------------------------------------------ complex-conjugate shifts */
+/* Extends tiled_inverse_iteration (inverse_iteration.h:19-22) to complex
+ * shifts mu_k = wr[k] + i*wi[k], one per conjugate pair, which the reference
+ * declares (problemgenerator.h:12-19 returns wi; main.c:95-97 stops at
+ * "only real eigenvalues are supported") and provides the robust kernels for
+ * (robust.c:370-773) without a driver.  Same tiled Givens RQ of H - mu I and
+ * robust back-substitution, in complex arithmetic, on the current device.
+ *   vr   n x 2*npairs output (ldvr >= n), the LAPACK dhsein layout: column 2k
+ *        holds the real part and column 2k+1 the imaginary part of the
+ *        unit-2-norm eigenvector for mu_k (the conjugate vector belongs to
+ *        conj(mu_k))
+ *   wr, wi  [npairs], not modified: pairs that need a restart are solved
+ *        again in place (opt->max_restarts rounds), so column order is kept
+ *   info  per pair (status, perturbed, scale, norm; tile_scales unused)
+ * One scaling factor per pair (robust.c:370-417); magnitude bounds use
+ * |Re| + |Im|.  opt->user_rhs is not supported (HSR_ERR_ARG).            */
+int hsr_inverse_iteration_cplx_ex(int n, const double *H, int ldH, int npairs,
+                                  const double *wr, const double *wi, int tlsz,
+                                  int rhs_tlsz, double *vr, int ldvr,
+                                  const hsr_options *opt, hsr_column_info *info);
+/* Device-pointer form: dwr, dwi [npairs], dvr n x 2*npairs, enqueued on
+ * `stream`; d_status (int) and d_scale (double) are per pair and optional. */
+int hsr_inverse_iteration_cplx_device(int n, const double *dH, int lddH, int npairs,
+                                      const double *dwr, const double *dwi, int tlsz,
+                                      double *dvr, int lddvr, const hsr_options *opt,
+                                      void *stream, int *d_status, double *d_scale);
+
 /* Number of kernel launches the last call on this thread enqueued. */
 long hsr_last_launch_count(void);
 
