@@ -65,9 +65,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="plain",
-                    choices=["plain", "batched", "served", "stress", "hessenberg"],
+                    choices=["plain", "batched", "served", "stress", "hessenberg", "complex"],
                     help="plain: n=10k solve (default); batched: 4096 mixed problems in one graph; "
-                         "served: a Poisson request trace through the request loop")
+                         "served: a Poisson request trace through the request loop; complex: n=10k with "
+                         "n/2 complex-conjugate shifts")
     ap.add_argument("--problems", type=int, default=4096, help="batched: number of problems")
     ap.add_argument("--requests", type=int, default=800, help="served: number of requests")
     ap.add_argument("--rate", type=float, default=120.0, help="served: arrivals per second")
@@ -628,6 +629,160 @@ def run_stress(args):
             "clocks": clk.summary()}
 
 
+def complex_workload(n: int, seed: int):
+    """Complex-spectrum problem (H, eigenvalues with positive imaginary part),
+    cached like workload()."""
+    from hsrq3in_gb300 import generators as G
+    d = os.path.join(tempfile.gettempdir(), "hsrq3in_bench")
+    os.makedirs(d, exist_ok=True)
+    f = os.path.join(d, "cplx_n%d_s%d_v1.npz" % (n, seed))
+    if os.path.exists(f):
+        z = np.load(f)
+        return np.asfortranarray(z["H"]), z["pairs"]
+    H, pairs, _ = G.complex_spectrum(n, seed)
+    tmp = f + ".%d.tmp.npz" % os.getpid()
+    np.savez(tmp, H=H, pairs=pairs)
+    os.replace(tmp, f)
+    return H, pairs
+
+
+def run_complex(args):
+    """Complex-conjugate shifts: H of order n with n/2 conjugate pairs (2x2
+    blocks a +- ib, a on a jittered grid in [-1,1], b in [0.1,1], N(0,1) above
+    the blocks), every pair's eigenvalue with positive imaginary part as a
+    shift.  Each pair gives two eigenvectors (mu and its conjugate), stored as
+    two real columns, so eigenvectors/s counts columns.  value: device-resident
+    (hsr_inverse_iteration_cplx_device); e2e: hsr_inverse_iteration_cplx_ex with
+    pinned host buffers; roofline of the complex GEMM launches; residuals of
+    128 sampled pairs; the oracle port's complex path on the host cores."""
+    import torch
+    import hsrq3in_gb300 as hsr
+    from hsrq3in_gb300 import _lib
+    lib = hsr.load(build_if_missing=True)
+    n = args.order
+    H, pairs = complex_workload(n, args.seed)
+    npairs = pairs.size
+    S = 2 * npairs
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    ld = n + (n & 1)
+    dHt = torch.zeros((n, ld), dtype=torch.float64, device=dev)
+    dHt[:, :n] = torch.from_numpy(np.ascontiguousarray(H.T)).to(dev)
+    dwr = torch.from_numpy(np.ascontiguousarray(pairs.real)).to(dev)
+    dwi = torch.from_numpy(np.ascontiguousarray(pairs.imag)).to(dev)
+    dX = torch.empty((S, ld), dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    opt = _lib.Options(0, 0, -1, 0.0)
+
+    def step():
+        rc = lib.hsr_inverse_iteration_cplx_device(n, dHt.data_ptr(), ld, npairs, dwr.data_ptr(), dwi.data_ptr(),
+                                                   args.tlsz, dX.data_ptr(), ld, C.byref(opt),
+                                                   C.c_void_p(stream.cuda_stream), None, None)
+        if rc < 0:
+            raise RuntimeError("complex device call failed: %d" % rc)
+        return rc
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    torch.cuda.synchronize()
+    dfma, _ = hsr.fp64_peak(200.0)
+    lib.hsr_set_kernel_timing(1)
+    ncls = len(_lib.KERNEL_CLASSES)
+    kms = np.zeros(ncls)
+    kl = np.zeros(ncls, dtype=np.int64)
+    gemm_fma = 0.0
+    launches = 0
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    rcs = []
+    with ClockSampler(0) as clk:
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(args.steps):
+                rcs.append(step())
+                ms = (C.c_double * ncls)()
+                ln = (C.c_long * ncls)()
+                fm = C.c_double()
+                lib.hsr_last_kernel_times(ms, ln, C.byref(fm))
+                kms += np.array(ms[:])
+                kl += np.array(ln[:])
+                gemm_fma += fm.value
+                launches += lib.hsr_last_launch_count()
+            e1.record(stream)
+        torch.cuda.synchronize()
+    lib.hsr_set_kernel_timing(0)
+    ms_step = e0.elapsed_time(e1) / args.steps
+    finite = bool(torch.isfinite(dX[:, :n]).all().item())
+    # residuals ||H x - mu x|| / (||H||_F ||x||) of 128 sampled pairs (torch, FP64)
+    idx = np.linspace(0, npairs - 1, 128).astype(np.int64)
+    Xr = dX[2 * idx, :n].T
+    Xi = dX[2 * idx + 1, :n].T
+    Hm = dHt[:, :n].T
+    a = dwr[idx][None, :]
+    b = dwi[idx][None, :]
+    Rr = Hm @ Xr - (a * Xr - b * Xi)
+    Ri = Hm @ Xi - (a * Xi + b * Xr)
+    num = torch.sqrt((Rr * Rr + Ri * Ri).sum(0))
+    den = torch.linalg.norm(Hm) * torch.sqrt((Xr * Xr + Xi * Xi).sum(0))
+    res = (num / den).cpu().numpy()
+    gemm_ms = kms[3]
+    achieved = 2.0 * gemm_fma / (gemm_ms * 1e-3) / 1e12 if gemm_ms > 0 else None
+    peak = dfma / 1e3
+    out = {"value": S / (ms_step / 1e3), "unit": UNIT, "ms_per_step": ms_step,
+           "pairs_per_s": npairs / (ms_step / 1e3),
+           "whole_tflops_2n2S": 2.0 * n * n * S / (ms_step / 1e3) / 1e12,
+           "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                        "frac": (achieved / peak) if achieved else None,
+                        "kernel": "k_gemm_c (the real GEMM over H with the complex epilogue; launches over the "
+                                  "rows above the next diagonal tile)",
+                        "peak_source": "FP64 DFMA stream measured in this run",
+                        "avg_launch_ms": gemm_ms / max(kl[3], 1)},
+           "kernel_ms_per_step": {k: float(v) / args.steps for k, v in zip(_lib.KERNEL_CLASSES, kms)},
+           "gpu_launches": int(launches), "clocks": clk.summary(),
+           "check": {"finite": finite, "max_residual_128_pairs": float(np.max(res)),
+                     "residual_bound_10n_eps": 10 * n * 2.0 ** -52, "rc": rcs[-1] if rcs else None},
+           "config": {"workload": "complex: n=%d, %d conjugate pairs (2 eigenvectors each), tlsz=%d"
+                                  % (n, npairs, args.tlsz),
+                      "n": n, "pairs": npairs, "tlsz": args.tlsz, "seed": args.seed,
+                      "generator": "T quasi-triangular, 2x2 blocks a+-ib (a jittered grid in [-1,1], b in "
+                                   "[0.1,1]), N(0,1) above the blocks; H = hess(Q T Q^T)",
+                      "l2": "inputs larger than L2 (H is %.0f MB); no flush" % (8 * n * n / 1e6)}}
+    if not args.no_e2e:
+        Hp = torch.from_numpy(np.asfortranarray(H).ravel(order="F")).pin_memory()
+        Xp = torch.empty(n * S, dtype=torch.float64).pin_memory()
+        wrh = np.ascontiguousarray(pairs.real)
+        wih = np.ascontiguousarray(pairs.imag)
+
+        def e2e_step():
+            rc = lib.hsr_inverse_iteration_cplx_ex(n, Hp.data_ptr(), n, npairs, wrh.ctypes.data, wih.ctypes.data,
+                                                   args.tlsz, args.rhs_tlsz, Xp.data_ptr(), n, C.byref(opt), None)
+            if rc < 0:
+                raise RuntimeError("complex host call failed: %d" % rc)
+        e2e_step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        te = (time.perf_counter() - t0) / args.steps
+        out["e2e"] = {"value": S / te, "unit": UNIT, "ms_per_step": te * 1e3,
+                      "h2d_bytes_per_step": 8 * (n * n + 2 * npairs), "d2h_bytes_per_step": 8 * n * S,
+                      "api": "hsr_inverse_iteration_cplx_ex (C ABI, pinned host buffers)"}
+    if not args.no_cpu_baseline:
+        from oracle import pyoracle as O
+        cores = os.cpu_count() or 1
+        O.set_threads(cores, variant="ref_fast")
+        sample = min(npairs, args.cpu_sample or 32 * cores)
+        t0 = time.perf_counter()
+        O.oracle_inverse_iteration_cplx(H, pairs.real[:sample], pairs.imag[:sample], args.tlsz, args.rhs_tlsz,
+                                        variant="ref_fast")
+        tc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 2 * sample / tc, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": "n=%d, first %d of %d pairs, one solve (%.1f s), tlsz=%d; the oracle's "
+                                         "complex path (the reference has no complex driver)"
+                                         % (n, sample, npairs, tc, args.tlsz)}
+    return out
+
+
 def run_hessenberg(args):
     """The input step on the GPU: reduction of a dense n x n matrix to
     upper-Hessenberg form (hsr_hessenberg_device), 10/3 n^3 flops, against
@@ -691,6 +846,18 @@ def main():
         return
     if args.workload == "batched":
         print(json.dumps(run_batched(args)), flush=True)
+        return
+    if args.workload == "complex":
+        cx = run_complex(args)
+        line = {"metric": "FP64 eigenvectors/s, complex-conjugate shifts", "value": cx["value"], "unit": UNIT,
+                "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": cx["ms_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded generator)", "config": cx["config"]}
+        for k in ("e2e", "roofline", "clocks", "gpu_launches", "cpu_baseline", "check"):
+            if k in cx:
+                line[k] = cx[k]
+        line["complex"] = {k: cx[k] for k in ("pairs_per_s", "whole_tflops_2n2S", "kernel_ms_per_step")}
+        print(json.dumps(line), flush=True)
         return
     if args.workload == "served":
         sv = run_served(args)
