@@ -432,18 +432,42 @@ __global__ void __launch_bounds__(32 * kDiagWarpsC) k_diag_c(DevProblem P, int J
 #undef BC
 }
 
-cudaError_t launch_diag_c(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st) {
-    bool gvy = false;
-    const size_t smem = diag_c_smem_bytes(b, &gvy);
-    if (gvy && !gscratch) return cudaErrorInvalidValue;
+// The dynamic shared-memory limit of k_diag_c only ever grows.
+cudaError_t diag_c_smem_attr(size_t smem) {
     static size_t configured = 0;
     if (smem > configured) {
         cudaError_t e = cudaFuncSetAttribute(k_diag_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
+    return cudaSuccess;
+}
+
+cudaError_t launch_diag_c(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st) {
+    bool gvy = false;
+    size_t smem = diag_c_smem_bytes(b, &gvy);
+    if (gvy && !gscratch) return cudaErrorInvalidValue;
+    if (gscratch) {
+        gvy = true;
+        smem = diagc_small_bytes(b);
+    }
+    {
+        cudaError_t e = diag_c_smem_attr(smem);
+        if (e != cudaSuccess) return e;
+    }
     k_diag_c<<<(P.S / 2 + 31) / 32, 32 * kDiagWarpsC, smem, st>>>(P, J, gvy ? gscratch : nullptr);
     return cudaGetLastError();
+}
+
+int diag_c_ctas_per_sm(int b) {
+    bool gvy = false;
+    const size_t smem = diag_c_smem_bytes(b, &gvy);
+    if (gvy) return 0;
+    if (diag_c_smem_attr(smem) != cudaSuccess) return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_diag_c, 32 * kDiagWarpsC, smem) != cudaSuccess)
+        return 0;
+    return nb;
 }
 
 // --------------------------------------------------------------- Part 1

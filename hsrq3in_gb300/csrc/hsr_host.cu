@@ -13,6 +13,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -203,6 +204,22 @@ Workspace &ws() {
     return w;
 }
 
+// Where the diagonal kernels keep v and y for a pass of `ctas` CTAs: in
+// shared memory when all CTAs are resident in one wave, else in global
+// scratch.  Beyond one wave the shared-memory form would run a second wave
+// of the latency-bound diagonal solve, and its large CTAs would keep the
+// concurrent GEMM's CTAs off their SMs; with v/y in global scratch a CTA
+// needs ~10 KB and shares each SM with two GEMM CTAs (measured at n = 10^4:
+// 1800 -> 1784 ms real, 1980 -> 1877 ms complex; at n <= 6144, where one
+// wave suffices, shared memory is faster).
+bool diag_vy_global(int ctas, int per_sm) {
+    if (per_sm <= 0) return true;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return ctas > per_sm * sms;
+}
+
 // One solve over a column range: the sweep J = T-1 .. 0, finalize, normalize.
 struct Solver {
     int n, T, tlsz, is;
@@ -286,7 +303,8 @@ int run_pass(Solver &s, int mode, int its, int off, int cnt) {
         HSR_LAUNCH_C(kcSetup, M, launch_init(P0, mode, s.eps3_dev, its, M));
         if (mode == 2) ++g_launches;
         const int b = s.tlsz;
-        const bool big = diag_smem_bytes(b) < (size_t)64 * b * sizeof(double);
+        const bool big = diag_smem_bytes(b) < (size_t)64 * b * sizeof(double) ||
+                         diag_vy_global((cc + 31) / 32, diag_ctas_per_sm(b));
         double *gs = big ? w.gscratch.as<double>() : nullptr;
         {
             const int J = s.T - 1;
@@ -383,7 +401,8 @@ int solve_device(int n, const double *dH, long long ldh, int S, double *dwr, int
     HSR_CK(w.status.ensure((size_t)S * sizeof(int)));
     HSR_CK(w.pert.ensure((size_t)S));
     if (!d_scale_user && (h_scale || h_tile_scales)) HSR_CK(w.scale.ensure((size_t)S * 8));
-    if (diag_smem_bytes(tlsz) < (size_t)64 * tlsz * sizeof(double))
+    if (diag_smem_bytes(tlsz) < (size_t)64 * tlsz * sizeof(double) ||
+        diag_vy_global((s.Scap + 31) / 32, diag_ctas_per_sm(tlsz)))
         HSR_CK(w.gscratch.ensure((size_t)((Sp + 31) / 32) * 64 * tlsz * 8));
     HSR_CK(cudaMemsetAsync(w.W.p, 0, 2 * (size_t)tlsz * Sp * 8, st));
     HSR_CK(cudaMemsetAsync(w.Zs.p, 0, 2 * (size_t)tlsz * Sp * 8, st));
@@ -595,11 +614,10 @@ int run_pass_c(Solver &s, int mode, int its, int off, int cnt) {
     Workspace &w = *s.w;
     HSR_CK(w.ensure_side());
     cudaStream_t M = s.st, D = w.side;
-    bool gvy = false;
-    diag_c_smem_bytes(s.tlsz, &gvy);
-    double *gs = gvy ? w.gscratch.as<double>() : nullptr;
     for (int c0 = 0; c0 < cnt; c0 += s.Scap) {
         const int cc = std::min(s.Scap, cnt - c0);
+        const bool gvy = diag_vy_global((cc / 2 + 31) / 32, diag_c_ctas_per_sm(s.tlsz));
+        double *gs = gvy ? w.gscratch.as<double>() : nullptr;
         DevProblem P0 = problem_for(s, off + c0, cc, 0);
         HSR_LAUNCH_C(kcSetup, M, launch_init_c(P0, mode, s.eps3_dev, its, M));
         {
@@ -695,9 +713,7 @@ int solve_device_cplx(int n, const double *dH, long long ldh, int np, double *dw
     HSR_CK(w.pert.ensure((size_t)S));
     HSR_CK(w.scale.ensure((size_t)np * 8));
     {
-        bool gvy = false;
-        diag_c_smem_bytes(tlsz, &gvy);
-        if (gvy) HSR_CK(w.gscratch.ensure((size_t)((Sp / 2 + 31) / 32) * 4 * 32 * tlsz * 8));
+        if (diag_vy_global((s.Scap / 2 + 31) / 32, diag_c_ctas_per_sm(tlsz))) HSR_CK(w.gscratch.ensure((size_t)((Sp / 2 + 31) / 32) * 4 * 32 * tlsz * 8));
     }
     HSR_CK(cudaMemsetAsync(w.W.p, 0, 2 * (size_t)tlsz * Sp * 8, st));
     HSR_CK(cudaMemsetAsync(w.Zs.p, 0, 2 * (size_t)tlsz * Sp * 8, st));

@@ -506,17 +506,36 @@ __global__ void __launch_bounds__(32 * kDiagWarps) k_diag(DevProblem P, int J, d
     diag_body<kDiagWarps>(P, J, blockIdx.x, gscratch ? gscratch + (size_t)blockIdx.x * 64 * b : nullptr);
 }
 
-cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st) {
-    const size_t small = diag_small_bytes(b, kDiagWarps);
-    const size_t smem = gscratch ? small : diag_smem_bytes(b);
+// The dynamic shared-memory limit of k_diag only ever grows: a launch must
+// never find it lowered below what an earlier launch configured.
+cudaError_t diag_smem_attr(size_t smem) {
     static size_t configured = 0;
     if (smem > configured) {
         cudaError_t e = cudaFuncSetAttribute(k_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
+    return cudaSuccess;
+}
+
+cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st) {
+    const size_t small = diag_small_bytes(b, kDiagWarps);
+    const size_t smem = gscratch ? small : diag_smem_bytes(b);
+    {
+        cudaError_t e = diag_smem_attr(smem);
+        if (e != cudaSuccess) return e;
+    }
     k_diag<<<(P.S + 31) / 32, 32 * kDiagWarps, smem, st>>>(P, J, gscratch);
     return cudaGetLastError();
+}
+
+// CTAs of k_diag that one SM holds with v/y in shared memory (tile height b).
+int diag_ctas_per_sm(int b) {
+    const size_t smem = diag_smem_bytes(b);
+    if (diag_smem_attr(smem) != cudaSuccess) return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_diag, 32 * kDiagWarps, smem) != cudaSuccess) return 0;
+    return nb;
 }
 
 // --------------------------------------------------------------- Part 1

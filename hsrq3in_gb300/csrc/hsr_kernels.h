@@ -62,6 +62,10 @@ cudaError_t launch_init(const DevProblem &P, int mode, const double *eps3_dev,
                         int its, cudaStream_t st);
 cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st);
 size_t diag_smem_bytes(int b);
+// CTAs per SM of the diagonal kernels with v/y in shared memory (0: v/y do
+// not fit).  More CTAs than one resident wave -> v/y go to global scratch.
+int diag_ctas_per_sm(int b);
+int diag_c_ctas_per_sm(int b);
 cudaError_t launch_part1(const DevProblem &P, int J, cudaStream_t st);
 // Crossover/update GEMM of stage J over rows [row_lo, row_hi) (row_hi <= fr[J]).
 cudaError_t launch_gemm(const DevProblem &P, int J, int row_lo, int row_hi, const CUtensorMap &tmH,
