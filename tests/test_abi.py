@@ -68,5 +68,32 @@ def test_argument_errors_without_gpu(lib):
                                         C.cast(vr, C.c_void_p), 4, C.byref(opt), None) == _lib.HSR_ERR_ARG
 
 
+def test_complex_argument_errors_without_gpu(lib):
+    """The complex-shift entry points reject bad arguments before any CUDA
+    call: n, ldH, tlsz (a positive multiple of 4), ldvr, missing shifts, and
+    caller right-hand sides (not supported for complex shifts)."""
+    from hsrq3in_gb300 import _lib
+    wr = (C.c_double * 4)()
+    wi = (C.c_double * 4)()
+    vr = (C.c_double * 32)()
+    H = (C.c_double * 16)()
+    opt = _lib.Options(0, 0, -1, 0.0)
+    cases = [(0, 4, 4, 4), (4, 3, 4, 4), (4, 4, 6, 4), (4, 4, 4, 3)]   # n, ldH, tlsz, ldvr
+    for n, ldH, tlsz, ldvr in cases:
+        rc = lib.hsr_inverse_iteration_cplx_ex(n, C.cast(H, C.c_void_p), ldH, 2, C.cast(wr, C.c_void_p),
+                                               C.cast(wi, C.c_void_p), tlsz, 4, C.cast(vr, C.c_void_p), ldvr,
+                                               C.byref(opt), None)
+        assert rc == _lib.HSR_ERR_ARG and lib.hsr_last_status() == _lib.HSR_ERR_ARG
+    assert lib.hsr_inverse_iteration_cplx_ex(4, C.cast(H, C.c_void_p), 4, 2, C.cast(wr, C.c_void_p), None, 4, 4,
+                                             C.cast(vr, C.c_void_p), 4, C.byref(opt), None) == _lib.HSR_ERR_ARG
+    rhs = _lib.Options(0, 1, -1, 0.0)
+    assert lib.hsr_inverse_iteration_cplx_ex(4, C.cast(H, C.c_void_p), 4, 2, C.cast(wr, C.c_void_p),
+                                             C.cast(wi, C.c_void_p), 4, 4, C.cast(vr, C.c_void_p), 4,
+                                             C.byref(rhs), None) == _lib.HSR_ERR_ARG
+    assert lib.hsr_inverse_iteration_cplx_device(4, C.cast(H, C.c_void_p), 4, 2, C.cast(wr, C.c_void_p),
+                                                 C.cast(wi, C.c_void_p), 6, C.cast(vr, C.c_void_p), 4,
+                                                 C.byref(opt), None, None, None) == _lib.HSR_ERR_ARG
+
+
 def test_version_string(lib):
     assert b"sm_103a" in lib.hsr_version()
