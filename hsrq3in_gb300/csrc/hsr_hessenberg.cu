@@ -72,7 +72,7 @@ __device__ __forceinline__ double vk(const double *A, long long lda, int k, int 
 
 constexpr int kHbNb = 64;         // reflectors per panel
 constexpr int kHbRows = 256;      // rows per CTA of the row-parallel kernels
-constexpr int kHbChunk = 256;     // columns per CTA of the panel GEMV
+constexpr int kHbChunk = 64;      // columns per CTA of the panel GEMV
 constexpr int kHbMaxSplit = 8;    // split-K factor of the thin left-update GEMM
 
 // Device state of one reduction.  Y, V: n x kHbNb (leading dimension n);
@@ -135,6 +135,33 @@ __device__ __forceinline__ double dot4(const double *x, long long stride, const 
     return (s0 + s1) + (s2 + s3);
 }
 
+// The same with eight chains, for the panel GEMV: eight independent loads in
+// flight per thread.
+__device__ __forceinline__ double dot8(const double *x, long long stride, const double *w, int m) {
+    double s[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    int q = 0;
+    for (; q + 7 < m; q += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s[u] = fma(x[(size_t)(q + u) * stride], w[q + u], s[u]);
+    }
+    for (; q < m; ++q) s[0] = fma(x[(size_t)q * stride], w[q], s[0]);
+    return ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
+}
+
+// Sum of m partials p[ch * stride], four chains in a fixed order.
+__device__ __forceinline__ double sum4(const double *p, long long stride, int m) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int q = 0;
+    for (; q + 3 < m; q += 4) {
+        s0 += p[(size_t)q * stride];
+        s1 += p[(size_t)(q + 1) * stride];
+        s2 += p[(size_t)(q + 2) * stride];
+        s3 += p[(size_t)(q + 3) * stride];
+    }
+    for (; q < m; ++q) s0 += p[(size_t)q * stride];
+    return (s0 + s1) + (s2 + s3);
+}
+
 // T(0:ip, ip) = -tau T(0:ip, 0:ip) vv, T(ip, ip) = tau, by one block.
 __device__ __forceinline__ void hb_tcol(const HbState &S, int ip, double t, const double *vv) {
     for (int p = threadIdx.x; p < ip; p += blockDim.x) {
@@ -165,8 +192,7 @@ __global__ void __launch_bounds__(kHbRows) k_hb_step(HbState S, int k0, int ip, 
         __syncthreads();
         const double t = S.sc[kHbNb + 1], rs = S.sc[kHbNb];
         if (r < n) {
-            double av = 0.0;
-            for (int ch = 0; ch < nchp; ++ch) av += S.gpart[(size_t)ch * n + r];
+            const double av = sum4(S.gpart + r, n, nchp);
             const double y = av - dot4(S.Y + r, n, vv, ip);
             S.Y[r + (size_t)ip * n] = t * y;
             if (r >= jp + 1) {
@@ -289,7 +315,7 @@ __global__ void __launch_bounds__(kHbRows) k_hb_gemv(HbState S, int k0, int i, i
     for (int t = tid; t < c1 - c0; t += blockDim.x) vs[t] = hb_v(S, j, rs, c0 + t);
     __syncthreads();
     const int r0 = blockIdx.x * kHbRows, r = r0 + tid;
-    if (r < n) S.gpart[(size_t)blockIdx.y * n + r] = dot4(S.A + r + (size_t)c0 * S.lda, S.lda, vs, c1 - c0);
+    if (r < n) S.gpart[(size_t)blockIdx.y * n + r] = dot8(S.A + r + (size_t)c0 * S.lda, S.lda, vs, c1 - c0);
     if (blockIdx.y != 0 || i == 0) return;
     cs[tid] = r < n ? hb_v(S, j, rs, r) : 0.0;
     __syncthreads();
