@@ -65,10 +65,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="plain",
-                    choices=["plain", "batched", "served", "stress", "hessenberg", "complex"],
+                    choices=["plain", "batched", "served", "stress", "hessenberg", "complex", "dense"],
                     help="plain: n=10k solve (default); batched: 4096 mixed problems in one graph; "
                          "served: a Poisson request trace through the request loop; complex: n=10k with "
-                         "n/2 complex-conjugate shifts")
+                         "n/2 complex-conjugate shifts; dense: reduce + solve + back-transform of a dense matrix")
     ap.add_argument("--problems", type=int, default=4096, help="batched: number of problems")
     ap.add_argument("--requests", type=int, default=800, help="served: number of requests")
     ap.add_argument("--rate", type=float, default=120.0, help="served: arrivals per second")
@@ -783,6 +783,77 @@ def run_complex(args):
     return out
 
 
+def run_dense(args):
+    """Dense input end to end on the device: A = P H0 P (P a random
+    Householder reflector, so A is dense with H0's known spectrum), reduced to
+    Hessenberg form (hsr_hessenberg_device), all n eigenvectors of H computed
+    (hsr_inverse_iteration_device, shifts = eigenvalues with rel. 1e-12
+    noise), and back-transformed to eigenvectors of A (hsr_hessenberg_apply_q_
+    device).  Each phase timed with CUDA events on the launching stream;
+    residuals ||A x - lambda x|| / (||A||_F ||x||) of 64 sampled columns."""
+    import torch
+    import hsrq3in_gb300 as hsr
+    n = args.order
+    H0, wr = workload(n, args.seed)
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    ld = n + (n & 1)
+    g = torch.Generator(device=dev)
+    g.manual_seed(args.seed + 5)
+    w = torch.randn(n, dtype=torch.float64, device=dev, generator=g)
+    w /= torch.linalg.norm(w)
+    Ht = torch.from_numpy(np.ascontiguousarray(H0.T)).to(dev)       # Ht[c, r] = H0[r, c]
+    # A = P H0 P with P = I - 2 w w^T; At = A^T in the same row-per-column layout
+    Hw = Ht.T @ w
+    wH = Ht @ w                                                      # (w^T H0)^T
+    c = torch.dot(w, Hw)
+    A = Ht.T - 2.0 * torch.outer(w, wH) - 2.0 * torch.outer(Hw, w) + 4.0 * c * torch.outer(w, w)
+    A0 = torch.zeros((n, ld), dtype=torch.float64, device=dev)
+    A0[:, :n] = A.T
+    del A, Hw, wH
+    dA = torch.empty_like(A0)
+    dH = torch.zeros((n, ld), dtype=torch.float64, device=dev)
+    dwr0 = torch.from_numpy(np.ascontiguousarray(wr)).to(dev)
+    dwr = dwr0.clone()
+    dX = torch.empty((n, ld), dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    keep = torch.tril(torch.ones((n, n), dtype=torch.bool, device=dev), diagonal=1)   # rows r <= c+1 of column c
+    phases = {"reduce": [], "solve": [], "back_transform": [], "total": []}
+    with torch.cuda.stream(stream):
+        for it in range(args.warmup + args.steps):
+            dA.copy_(A0)
+            dwr.copy_(dwr0)
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            ev[0].record(stream)
+            tau = hsr.hessenberg_device(dA, stream=stream)
+            ev[1].record(stream)
+            dH[:, :n] = torch.where(keep, dA[:, :n], torch.zeros((), dtype=torch.float64, device=dev))
+            hsr.inverse_iteration_device(dH, dwr, dX, args.tlsz, stream=stream)
+            ev[2].record(stream)
+            hsr.hessenberg_apply_q_device(dA, tau, dX, stream=stream)
+            ev[3].record(stream)
+            torch.cuda.synchronize()
+            if it >= args.warmup:
+                phases["reduce"].append(ev[0].elapsed_time(ev[1]))
+                phases["solve"].append(ev[1].elapsed_time(ev[2]))
+                phases["back_transform"].append(ev[2].elapsed_time(ev[3]))
+                phases["total"].append(ev[0].elapsed_time(ev[3]))
+    ms = {k: float(np.mean(v)) for k, v in phases.items()}
+    idx = torch.from_numpy(np.linspace(0, n - 1, 64).astype(np.int64)).to(dev)
+    X = dX[idx, :n].T
+    lam = dwr[idx]
+    Am = A0[:, :n].T
+    res = (torch.linalg.norm(Am @ X - X * lam[None, :], dim=0) /
+           (torch.linalg.norm(Am) * torch.linalg.norm(X, dim=0))).cpu().numpy()
+    return {"value": n / (ms["total"] / 1e3), "unit": UNIT, "ms_per_step": ms["total"], "phase_ms": ms,
+            "tflops_reduce": 10.0 / 3.0 * n ** 3 / (ms["reduce"] / 1e3) / 1e12,
+            "tflops_back_transform": 2.0 * n ** 3 / (ms["back_transform"] / 1e3) / 1e12,
+            "check": {"max_residual_64_cols": float(np.max(res)), "residual_bound_10n_eps": 10 * n * 2.0 ** -52,
+                      "finite": bool(torch.isfinite(dX[:, :n]).all().item())},
+            "config": {"workload": "dense: n=%d, A = P H P (P a random Householder reflector), all %d eigenvectors, "
+                                   "tlsz=%d" % (n, n, args.tlsz), "n": n, "tlsz": args.tlsz, "seed": args.seed}}
+
+
 def run_hessenberg(args):
     """The input step on the GPU: reduction of a dense n x n matrix to
     upper-Hessenberg form (hsr_hessenberg_device), 10/3 n^3 flops, against
@@ -846,6 +917,14 @@ def main():
         return
     if args.workload == "batched":
         print(json.dumps(run_batched(args)), flush=True)
+        return
+    if args.workload == "dense":
+        de = run_dense(args)
+        line = {"metric": "FP64 eigenvectors/s of a dense matrix (reduce + solve + back-transform)",
+                "value": de["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": de["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic (seeded generator)", "config": de["config"], "dense": de}
+        print(json.dumps(line), flush=True)
         return
     if args.workload == "complex":
         cx = run_complex(args)

@@ -41,7 +41,6 @@
 namespace hsr {
 namespace {
 
-constexpr int kHhThreads = 256;
 
 __device__ __forceinline__ double block_sum3(double v, double *red) {
     for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -65,10 +64,6 @@ __device__ __forceinline__ double lapy2(double x, double y) {
     return w * sqrt(1.0 + q * q);
 }
 
-// v(i) of reflector k for i >= k+1 (1 at k+1, stored entries below).
-__device__ __forceinline__ double vk(const double *A, long long lda, int k, int i) {
-    return i == k + 1 ? 1.0 : A[i + (size_t)k * lda];
-}
 
 constexpr int kHbNb = 64;         // reflectors per panel
 constexpr int kHbRows = 256;      // rows per CTA of the row-parallel kernels
@@ -421,16 +416,30 @@ cudaError_t hb_gemm(int M, int N, int K, double alpha, const double *A, long lon
     return cudaGetLastError();
 }
 
-// X(k+1 :, c) = H_k X(k+1 :, c) for every column c of X.
-__global__ void __launch_bounds__(kHhThreads) k_hh_apply(int n, const double *A, long long lda, int k,
-                                                        const double *tau, double *X, long long ldx) {
-    __shared__ double red[32];
-    double *x = X + (size_t)blockIdx.x * ldx;
-    double d = 0.0;
-    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) d = fma(vk(A, lda, k, i), x[i], d);
-    d = block_sum3(d, red);
-    const double td = -tau[k] * d;
-    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) x[i] = fma(vk(A, lda, k, i), td, x[i]);
+// Back-transform Q X, blocked like LAPACK dormhr ('L', 'N'): the panels of
+// the reduction in reverse order, X(k0+1:, :) -= V (T (V^T X(k0+1:, :))), with
+// V rebuilt from the reflectors stored in A and T from V and tau (dlarft:
+// T(0:i, i) = -tau_i T(0:i, 0:i) (V^T V)(0:i, i), T(i, i) = tau_i).
+__global__ void k_hq_vpanel(int n, const double *A, long long lda, int k0, double *V) {
+    const int i = blockIdx.y, j = k0 + i;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+        V[r + (size_t)i * n] = r == j + 1 ? 1.0 : (r >= j + 2 ? A[r + (size_t)j * lda] : 0.0);
+}
+
+__global__ void k_hq_tfactor(int ib, const double *tau, const double *G, double *T) {
+    for (int i = 0; i < ib; ++i) {
+        const double t = tau[i];
+        for (int p = threadIdx.x; p < i; p += blockDim.x) {
+            double s = 0.0;
+            for (int q = p; q < i; ++q) s = fma(T[p + (size_t)q * kHbNb], G[q + (size_t)i * kHbNb], s);
+            T[p + (size_t)i * kHbNb] = -t * s;
+        }
+        if (threadIdx.x == 0) {
+            T[i + (size_t)i * kHbNb] = t;
+            for (int p = i + 1; p < kHbNb; ++p) T[p + (size_t)i * kHbNb] = 0.0;
+        }
+        __syncthreads();
+    }
 }
 
 struct HhScratch {
@@ -550,6 +559,50 @@ extern "C" int hsr_hessenberg_apply_q_device(int n, const double *dA, int lda, c
     if (n <= 0 || lda < n || ncols < 0 || ldx < n || !dA || !dtau || (ncols > 0 && !dX)) return HSR_ERR_ARG;
     if (ncols == 0 || n <= 2) return HSR_OK;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    for (int k = n - 3; k >= 0; --k) k_hh_apply<<<ncols, kHhThreads, 0, st>>>(n, dA, lda, k, dtau, dX, ldx);
+    static thread_local HhScratch sc;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return HSR_ERR_CUDA;
+    const size_t nb = kHbNb;
+    const size_t need = (size_t)n * nb + 2 * nb * nb + (size_t)kHbMaxSplit * nb * nb +
+                        (size_t)(kHbMaxSplit + 2) * nb * ncols;
+    if (sc.ensure(need * sizeof(double), dev) != cudaSuccess) return HSR_ERR_NOMEM;
+    double *V = sc.p, *G = V + (size_t)n * nb, *T = G + nb * nb, *Gp = T + nb * nb;
+    double *Wp = Gp + (size_t)kHbMaxSplit * nb * nb, *W = Wp + (size_t)kHbMaxSplit * nb * ncols,
+           *W2 = W + nb * (size_t)ncols;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    auto split_for = [&](int tiles, int kr) {
+        int sp = (2 * sms + tiles - 1) / tiles;
+        return std::max(1, std::min(sp, std::min(kHbMaxSplit, (kr + kHbTk - 1) / kHbTk)));
+    };
+    auto sum_parts = [&](int M, int N, int kr, int sp, const double *parts, double *out) {
+        const int kc = (((kr + sp - 1) / sp) + kHbTk - 1) / kHbTk * kHbTk;
+        const int nz = (kr + kc - 1) / kc;
+        k_hb_sumk<<<(M * N + 255) / 256, 256, 0, st>>>(M, N, nz, parts, nb, nb * (long long)N, out);
+    };
+    const int last = ((n - 3) / kHbNb) * kHbNb;
+    for (int k0 = last; k0 >= 0; k0 -= kHbNb) {
+        const int ib = std::min(kHbNb, n - 2 - k0);
+        const int kr = n - k0 - 1;
+        k_hq_vpanel<<<dim3((n + 255) / 256 < 64 ? (n + 255) / 256 : 64, ib), 256, 0, st>>>(n, dA, lda, k0, V);
+        // G = V^T V over rows k0+1 .., then T (dlarft, forward, columnwise).
+        const int sg = split_for(1, kr);
+        if (hb_gemm(ib, ib, kr, 1.0, V + (k0 + 1), n, 1, V + (k0 + 1), 1, n, 0.0, Gp, nb, sg, nb * (long long)ib,
+                    st) != cudaSuccess)
+            return HSR_ERR_CUDA;
+        sum_parts(ib, ib, kr, sg, Gp, G);
+        k_hq_tfactor<<<1, 64, 0, st>>>(ib, dtau + k0, G, T);
+        // X(k0+1:, :) -= V (T (V^T X(k0+1:, :)))
+        const int tiles = (ncols + kHbTm - 1) / kHbTm;
+        const int sp = split_for(tiles, kr);
+        if (hb_gemm(ib, ncols, kr, 1.0, V + (k0 + 1), n, 1, dX + (k0 + 1), 1, ldx, 0.0, Wp, nb, sp,
+                    nb * (long long)ncols, st) != cudaSuccess)
+            return HSR_ERR_CUDA;
+        sum_parts(ib, ncols, kr, sp, Wp, W);
+        if (hb_gemm(ib, ncols, ib, 1.0, T, 1, nb, W, 1, nb, 0.0, W2, nb, 1, 0, st) != cudaSuccess ||
+            hb_gemm(kr, ncols, ib, -1.0, V + (k0 + 1), 1, n, W2, 1, nb, 1.0, dX + (k0 + 1), ldx, 1, 0, st) !=
+                cudaSuccess)
+            return HSR_ERR_CUDA;
+    }
     return cudaGetLastError() == cudaSuccess ? HSR_OK : HSR_ERR_CUDA;
 }
