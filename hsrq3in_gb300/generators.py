@@ -61,9 +61,7 @@ def _hessenberg_similarity(T: np.ndarray, rng: np.random.Generator) -> np.ndarra
         A -= 2.0 * np.outer(w, w @ A)
         A -= 2.0 * np.outer(A @ w, w)
     H = sl.hessenberg(A, overwrite_a=True, check_finite=False)
-    H = np.asfortranarray(H)
-    H[np.tril_indices(n, -2)] = 0.0
-    return H
+    return np.asfortranarray(np.triu(H, -1))
 
 
 def real_spectrum(n: int, seed: int, upper_scale: float = 1.0):

@@ -452,11 +452,13 @@ static void offdiag_reduce(const prob_t *P, int I, int J, double mu,
         w[k] = c[k] * pk;
         pk = pk * s[k];
     }
-    for (int i = 0; i < m; i++) {
-        double acc = 0.0;
-        for (int k = 0; k < nc; k++) acc = fma(HIJ(i, k), w[k], acc);
-        r[i] = fma(pk, r[i], acc);
-    }
+    /* Per row the sum over k runs in k order; the loop nest walks H by
+     * columns so that the accesses are contiguous. */
+    double acc[m];
+    for (int i = 0; i < m; i++) acc[i] = 0.0;
+    for (int k = 0; k < nc; k++)
+        for (int i = 0; i < m; i++) acc[i] = fma(HIJ(i, k), w[k], acc[i]);
+    for (int i = 0; i < m; i++) r[i] = fma(pk, r[i], acc[i]);
     if (applyShift) r[m - 1] = fma(-mu, w[0], r[m - 1]);
 #else
     for (int k = nc - 1; k >= 4; k -= 4) {
@@ -594,14 +596,18 @@ static void tile_update(const prob_t *P, int I, int J, int ns, const double *wr,
     /* Y -= H(I, J .. J+kb-2) * Ytilde2(0:kb-2) (update-task.c:233). */
     const double *Hs = &HH(r0, P->fr[J]);
 #if HSRO_MODE
-    for (int k = 0; k < ns; k++) {
-        const double *z = work + (size_t)k * kb;
-        double *y = Y + (size_t)k * ldY;
-        for (int i = 0; i < m; i++) {
-            double acc = 0.0;
-            for (int q = 0; q < kb - 1; q++)
-                acc = fma(Hs[(size_t)i + (size_t)q * P->ldH], z[q], acc);
-            y[i] = y[i] - acc;
+    {
+        /* Per row the sum over q runs in q order; columns of H outermost. */
+        double acc[m];
+        for (int k = 0; k < ns; k++) {
+            const double *z = work + (size_t)k * kb;
+            double *y = Y + (size_t)k * ldY;
+            for (int i = 0; i < m; i++) acc[i] = 0.0;
+            for (int q = 0; q < kb - 1; q++) {
+                const double *hq = Hs + (size_t)q * P->ldH;
+                for (int i = 0; i < m; i++) acc[i] = fma(hq[i], z[q], acc[i]);
+            }
+            for (int i = 0; i < m; i++) y[i] = y[i] - acc[i];
         }
     }
 #else

@@ -424,14 +424,17 @@ static void coffdiag_reduce(const prob_t *P, int I, int J, hcplx mu, const doubl
         wim[k] = w.im;
         pk = cmul(pk, cmk(sr[k], si[k]));
     }
-    for (int i = 0; i < m; i++) {
-        double ar = 0.0, ai = 0.0;
-        for (int k = 0; k < nc; k++) {
+    /* Per row the sums over k run in k order; columns of H outermost. */
+    double ar[m], ai[m];
+    for (int i = 0; i < m; i++) ar[i] = ai[i] = 0.0;
+    for (int k = 0; k < nc; k++)
+        for (int i = 0; i < m; i++) {
             const double h = HH(r0 + i, c0 + k);
-            ar = fma(h, wre[k], ar);
-            ai = fma(h, wim[k], ai);
+            ar[i] = fma(h, wre[k], ar[i]);
+            ai[i] = fma(h, wim[k], ai[i]);
         }
-        const hcplx r = cfma(pk, cmk(rre[i], rim[i]), cmk(ar, ai));
+    for (int i = 0; i < m; i++) {
+        const hcplx r = cfma(pk, cmk(rre[i], rim[i]), cmk(ar[i], ai[i]));
         rre[i] = r.re;
         rim[i] = r.im;
     }
@@ -557,19 +560,23 @@ static void ctile_update(const prob_t *P, int I, int J, int ns, const double *wr
     /* Y -= H(I, J .. J+kb-2) Ytilde2(0:kb-2), then the rank-1 term with the
      * crossover column (update-task.c:233-243). */
     const double *Hs = &HH(r0, P->fr[J]);
+    double ar[m], ai[m];
     for (int k = 0; k < ns; k++) {
         const double *wr_ = zr + (size_t)k * kb, *wi_ = zi + (size_t)k * kb;
         const double *rtr = Rtr + (size_t)k * m, *rti = Rti + (size_t)k * m;
         double *yr = YR(k), *yi = YI(k);
         const hcplx zl = cmk(wr_[kb - 1], wi_[kb - 1]);
-        for (int i = 0; i < m; i++) {
-            double ar = 0.0, ai = 0.0;
-            for (int q = 0; q < kb - 1; q++) {
-                const double hv = Hs[(size_t)i + (size_t)q * P->ldH];
-                ar = fma(hv, wr_[q], ar);
-                ai = fma(hv, wi_[q], ai);
+        /* Per row the sums over q run in q order; columns of H outermost. */
+        for (int i = 0; i < m; i++) ar[i] = ai[i] = 0.0;
+        for (int q = 0; q < kb - 1; q++) {
+            const double *hq = Hs + (size_t)q * P->ldH;
+            for (int i = 0; i < m; i++) {
+                ar[i] = fma(hq[i], wr_[q], ar[i]);
+                ai[i] = fma(hq[i], wi_[q], ai[i]);
             }
-            hcplx t = cmk(yr[i] - ar, yi[i] - ai);
+        }
+        for (int i = 0; i < m; i++) {
+            hcplx t = cmk(yr[i] - ar[i], yi[i] - ai[i]);
             t = cfnma(cmk(rtr[i], rti[i]), zl, t);
             yr[i] = t.re;
             yi[i] = t.im;
