@@ -31,7 +31,7 @@ EXPORTS = [
     "hsr_batch_plan_create", "hsr_batch_plan_execute", "hsr_batch_plan_info", "hsr_batch_plan_destroy",
     "hsr_autotune_tlsz", "hsr_autotune_batch",
     "hsr_server_create", "hsr_server_replay", "hsr_server_destroy",
-    "hsr_inverse_iteration_cplx_ex", "hsr_inverse_iteration_cplx_device",
+    "hsr_inverse_iteration_cplx_ex", "hsr_inverse_iteration_cplx_device", "hsr_inverse_iteration_mixed",
 ]
 NOALLOC_MAX_N = 256
 NOALLOC_MAX_NRHS = 256
@@ -114,6 +114,10 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     lib.hsr_inverse_iteration_cplx_device.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
                                                       C.c_void_p, C.c_int, C.c_void_p, C.c_int,
                                                       C.POINTER(Options), C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.hsr_inverse_iteration_mixed.restype = C.c_int
+    lib.hsr_inverse_iteration_mixed.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                                C.c_int, C.c_int, C.c_void_p, C.c_int, C.POINTER(Options),
+                                                C.c_void_p]
     lib.hsr_residuals_device.restype = C.c_int
     lib.hsr_residuals_device.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                          C.c_void_p, C.c_void_p]

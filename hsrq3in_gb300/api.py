@@ -140,6 +140,30 @@ def inverse_iteration_cplx(H: np.ndarray, mu: np.ndarray, tlsz: int, rhs_tlsz: i
                 launches=lib.hsr_last_launch_count())
 
 
+def inverse_iteration_mixed(H: np.ndarray, wr: np.ndarray, wi: np.ndarray, tlsz: int, rhs_tlsz: int = 64,
+                            scaling: str = "pow2", max_restarts: int = -1):
+    """Real eigenvalues and conjugate pairs in one call (LAPACK dhsein layout:
+    a pair is two consecutive entries (a, b), (a, -b) with b > 0).  Returns a
+    dict with vr (n x m: column k for a real shift; columns k, k+1 the real and
+    imaginary parts for a pair), wr (real shifts possibly reordered among the
+    real positions), wi, per-column status and the library status code."""
+    lib = _lib.load()
+    H = np.asfortranarray(H, dtype=np.float64)
+    n = H.shape[0]
+    wr = np.array(wr, dtype=np.float64, copy=True)
+    wi = np.array(wi, dtype=np.float64, copy=True)
+    m = wr.shape[0]
+    vr = np.zeros((n, m), dtype=np.float64, order="F")
+    status = np.zeros(max(m, 1), dtype=np.int32)
+    opt = _lib.Options(_scaling(scaling), 0, int(max_restarts), 0.0)
+    rc = lib.hsr_inverse_iteration_mixed(n, H.ctypes.data, H.shape[0], m, wr.ctypes.data, wi.ctypes.data, int(tlsz),
+                                         int(rhs_tlsz), vr.ctypes.data, vr.shape[0], C.byref(opt),
+                                         status.ctypes.data)
+    if rc < 0:
+        raise HsrError(rc)
+    return dict(vr=vr, wr=wr, wi=wi, status=status[:m], rc=rc)
+
+
 def inverse_iteration_cplx_device(dH, dwr, dwi, dvr, tlsz: int, stream=None, scaling: str = "pow2",
                                   d_status=None, d_scale=None) -> int:
     """Device-resident complex-shift call on torch tensors: dH (n, ldh) as in

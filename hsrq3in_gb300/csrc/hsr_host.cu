@@ -1033,6 +1033,66 @@ int hsr_inverse_iteration_cplx_device(int n, const double *dH, int lddH, int npa
     return g_last_status = rc;
 }
 
+int hsr_inverse_iteration_mixed(int n, const double *H, int ldH, int m, double *wr, double *wi, int tlsz,
+                                int rhs_tlsz, double *vr, int ldvr, const hsr_options *opt, int *status) {
+    // Validate the layout: a conjugate pair is two consecutive entries
+    // (wr, +wi), (wr, -wi) with wi > 0.
+    if (n <= 0 || ldH < n || m < 0 || ldvr < n || !H || (m > 0 && (!wr || !wi || !vr)) || tlsz <= 0 ||
+        tlsz % 4 != 0 || rhs_tlsz <= 0 || (opt && opt->user_rhs))
+        return g_last_status = HSR_ERR_ARG;
+    std::vector<int> real_pos, pair_pos;
+    for (int k = 0; k < m;) {
+        if (wi[k] == 0.0) {
+            real_pos.push_back(k);
+            k += 1;
+        } else {
+            if (!(wi[k] > 0.0) || k + 1 >= m || wr[k + 1] != wr[k] || wi[k + 1] != -wi[k])
+                return g_last_status = HSR_ERR_ARG;
+            pair_pos.push_back(k);
+            k += 2;
+        }
+    }
+    const int nr = (int)real_pos.size(), np = (int)pair_pos.size();
+    int rc_r = HSR_OK, rc_c = HSR_OK;
+    if (nr > 0) {
+        std::vector<double> w(nr), x((size_t)n * nr);
+        std::vector<int> st(nr);
+        for (int q = 0; q < nr; ++q) w[q] = wr[real_pos[q]];
+        hsr_column_info info{};
+        info.status = st.data();
+        rc_r = host_call(n, H, ldH, nr, w.data(), tlsz, rhs_tlsz, x.data(), n, opt, &info);
+        if (rc_r < 0) return g_last_status = rc_r;
+        // The real path may reorder its shifts (converged first); they stay
+        // in the real positions, each with its own column.
+        for (int q = 0; q < nr; ++q) {
+            const int k = real_pos[q];
+            wr[k] = w[q];
+            memcpy(vr + (size_t)k * ldvr, x.data() + (size_t)q * n, (size_t)n * 8);
+            if (status) status[k] = st[q];
+        }
+    }
+    if (np > 0) {
+        std::vector<double> a(np), b(np), x((size_t)n * 2 * np);
+        std::vector<int> st(np);
+        for (int q = 0; q < np; ++q) {
+            a[q] = wr[pair_pos[q]];
+            b[q] = wi[pair_pos[q]];
+        }
+        hsr_column_info info{};
+        info.status = st.data();
+        rc_c = host_call_c(n, H, ldH, np, a.data(), b.data(), tlsz, rhs_tlsz, x.data(), n, opt, &info);
+        if (rc_c < 0) return g_last_status = rc_c;
+        for (int q = 0; q < np; ++q) {
+            const int k = pair_pos[q];
+            memcpy(vr + (size_t)k * ldvr, x.data() + (size_t)(2 * q) * n, (size_t)n * 8);
+            memcpy(vr + (size_t)(k + 1) * ldvr, x.data() + (size_t)(2 * q + 1) * n, (size_t)n * 8);
+            if (status) status[k] = status[k + 1] = st[q];
+        }
+    }
+    return g_last_status = (rc_r == HSR_ERR_NOT_CONVERGED || rc_c == HSR_ERR_NOT_CONVERGED) ? HSR_ERR_NOT_CONVERGED
+                                                                                              : HSR_OK;
+}
+
 long hsr_last_launch_count(void) { return g_launches; }
 
 void hsr_set_kernel_timing(int enable) { g_timing.enabled = enable != 0; }

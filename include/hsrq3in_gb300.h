@@ -134,6 +134,22 @@ int hsr_inverse_iteration_cplx_device(int n, const double *dH, int lddH, int npa
                                       double *dvr, int lddvr, const hsr_options *opt,
                                       void *stream, int *d_status, double *d_scale);
 
+/* Mixed real and complex shifts in one call, as LAPACK dhsein takes them
+ * from a real Schur spectrum: m entries (wr[k], wi[k]); a real shift has
+ * wi[k] == 0 and gets column k of vr; a conjugate pair occupies entries k,
+ * k+1 with wi[k] > 0, wr[k+1] == wr[k], wi[k+1] == -wi[k], and columns k and
+ * k+1 receive the real and imaginary parts of the vector for wr[k] + i wi[k].
+ * Real shifts run through tiled_inverse_iteration's path and may be
+ * reordered among the real positions when a restart was needed (wr updated,
+ * columns follow); pairs run through hsr_inverse_iteration_cplx_ex and keep
+ * their positions.  status (optional, [m]) is per column.  A malformed pair
+ * returns HSR_ERR_ARG.  Extends inverse_iteration.h:19-22 to the wi that
+ * problemgenerator.h:12-19 produces. */
+int hsr_inverse_iteration_mixed(int n, const double *H, int ldH, int m,
+                                double *wr, double *wi, int tlsz, int rhs_tlsz,
+                                double *vr, int ldvr, const hsr_options *opt,
+                                int *status);
+
 /* Number of kernel launches the last call on this thread enqueued. */
 long hsr_last_launch_count(void);
 

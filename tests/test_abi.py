@@ -95,5 +95,21 @@ def test_complex_argument_errors_without_gpu(lib):
                                                  C.byref(opt), None, None, None) == _lib.HSR_ERR_ARG
 
 
+def test_mixed_layout_errors_without_gpu(lib):
+    """Malformed conjugate pairs are rejected before any CUDA call."""
+    from hsrq3in_gb300 import _lib
+    H = (C.c_double * 16)()
+    vr = (C.c_double * 16)()
+    opt = _lib.Options(0, 0, -1, 0.0)
+    for wr_, wi_ in ([0.1, 0.1], [0.5, 0.5]), ([0.1, 0.1], [-0.5, 0.5]), ([0.1, 0.2], [0.5, -0.5]), \
+            ([0.0, 0.1], [0.0, 0.5]):
+        wr = (C.c_double * 2)(*wr_)
+        wi = (C.c_double * 2)(*wi_)
+        rc = lib.hsr_inverse_iteration_mixed(4, C.cast(H, C.c_void_p), 4, 2, C.cast(wr, C.c_void_p),
+                                             C.cast(wi, C.c_void_p), 4, 4, C.cast(vr, C.c_void_p), 4,
+                                             C.byref(opt), None)
+        assert rc == _lib.HSR_ERR_ARG, (wr_, wi_)
+
+
 def test_version_string(lib):
     assert b"sm_103a" in lib.hsr_version()

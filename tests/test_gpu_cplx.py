@@ -131,3 +131,39 @@ def test_cplx_device_entry(gpu_lib):
     assert np.array_equal(dvr.cpu().numpy().T, host["vr"])
     assert np.array_equal(d_status.cpu().numpy(), host["status"])
     assert np.array_equal(d_scale.cpu().numpy(), host["scale"])
+
+
+def test_mixed_real_and_pairs(gpu_lib):
+    """hsr_inverse_iteration_mixed on a spectrum with real eigenvalues and
+    conjugate pairs interleaved (the LAPACK dhsein layout) equals the real and
+    the complex entry points called separately, column for column, bit for
+    bit; every eigenpair meets the residual bound."""
+    import hsrq3in_gb300 as hsr
+    n, tlsz = 160, 32
+    H, pairs, lam_r = G.complex_spectrum(n, 31, n_real=40)
+    rng = np.random.default_rng(5)
+    items = [("r", x) for x in lam_r[:12]] + [("c", z) for z in pairs[:14]]
+    rng.shuffle(items)
+    wr, wi = [], []
+    for kind, v in items:
+        if kind == "r":
+            wr.append(v)
+            wi.append(0.0)
+        else:
+            wr += [v.real, v.real]
+            wi += [v.imag, -v.imag]
+    wr, wi = np.array(wr), np.array(wi)
+    out = hsr.inverse_iteration_mixed(H, wr, wi, tlsz, 16)
+    assert out["rc"] == 0 and out["status"].all()
+    rpos = np.where(wi == 0.0)[0]
+    cpos = np.where(wi > 0.0)[0]
+    sep_r = hsr.inverse_iteration(H, wr[rpos], tlsz, 16)
+    sep_c = hsr.inverse_iteration_cplx(H, wr[cpos] + 1j * wi[cpos], tlsz, 16)
+    assert np.array_equal(out["vr"][:, rpos], sep_r["vr"])
+    assert np.array_equal(out["vr"][:, cpos], sep_c["vr"][:, 0::2])
+    assert np.array_equal(out["vr"][:, cpos + 1], sep_c["vr"][:, 1::2])
+    X = out["vr"].astype(complex)
+    X[:, cpos] = out["vr"][:, cpos] + 1j * out["vr"][:, cpos + 1]
+    X[:, cpos + 1] = np.conj(X[:, cpos])
+    mu = out["wr"] + 1j * out["wi"]
+    assert O.residuals(H, mu, X).max() <= 10 * n * EPS
