@@ -58,7 +58,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--order", type=int, default=10000, help="n, the order of H")
     ap.add_argument("--nrhs", type=int, default=0, help="0 = all n eigenvalues")
-    ap.add_argument("--tlsz", type=int, default=200)
+    ap.add_argument("--tlsz", type=int, default=160,
+                    help="row tile size (160: fastest of 128..320 on GB300 at n=10k)")
     ap.add_argument("--rhs-tlsz", type=int, default=64)
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--cpu-sample", type=int, default=0, help="shifts in the CPU sample (0 = 64 per core)")

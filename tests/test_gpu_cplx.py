@@ -167,3 +167,13 @@ def test_mixed_real_and_pairs(gpu_lib):
     X[:, cpos + 1] = np.conj(X[:, cpos])
     mu = out["wr"] + 1j * out["wi"]
     assert O.residuals(H, mu, X).max() <= 10 * n * EPS
+
+
+def test_cplx_passes_by_hbm_budget(gpu_lib):
+    """Complex shifts in passes of 32 pairs (a 400 KB workspace budget) give
+    the one-pass result bit for bit."""
+    n, tlsz = 300, 40
+    H, pairs, _ = G.complex_spectrum(n, 43)
+    one = _device(H, pairs[:90], tlsz)
+    split = _device(H, pairs[:90], tlsz, hbm_budget_bytes=4e5)
+    _same(dict(split, colscale=split["scale"]), dict(one, colscale=one["scale"]))

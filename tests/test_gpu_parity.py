@@ -146,3 +146,16 @@ def test_user_rhs(gpu_lib):
     dev = _device(H, wr, 20, rhs=rhs)
     orc = O.oracle_solve_rhs(H, wr, rhs, 20, 16, intscale=1, variant="fma")
     assert np.array_equal(dev["vr"], orc["vr"])
+
+
+def test_passes_by_hbm_budget(gpu_lib):
+    """A workspace budget that holds only 32 columns splits the shifts into
+    passes; every column is the same bit for bit as in one pass."""
+    n, tlsz = 300, 40
+    H, lam = G.real_spectrum(n, 41)
+    wr = G.perturbed_shifts(lam, 42)[:100]
+    one = _device(H, wr, tlsz)
+    split = _device(H, wr, tlsz, hbm_budget_bytes=4e5)
+    assert np.array_equal(one["vr"], split["vr"])
+    assert np.array_equal(one["scale"], split["scale"])
+    assert np.array_equal(one["status"], split["status"])
