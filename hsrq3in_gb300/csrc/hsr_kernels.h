@@ -17,6 +17,11 @@ namespace hsr {
 //          rotated solved tile (row 0 of Zs is zero)
 //   Zslow  rescaled copies of Ytilde2 for columns needing overflow
 //          protection, [(T*tlsz)][Spad] indexed by (I*tlsz + q)
+// For complex shifts (hsr_cplx.cu) S counts real columns: pair p occupies
+// columns 2p (real part) and 2p+1 (imaginary part) of every array above and
+// of the per-column scalars; wr holds (Re mu_p, Im mu_p) at 2p, 2p+1; the
+// cosine of a rotation is Cr[.][2p] and its complex sine Sr[.][2p] +
+// i Sr[.][2p+1]; beta, ynorm, slow and pert of pair p sit at column 2p.
 struct DevProblem {
     int n, T, S, Spad, tlsz;
     const int *fr;             // first row of each tile, [T+1]
