@@ -435,12 +435,7 @@ __global__ void __launch_bounds__(32 * kDiagWarpsC) k_diag_c(DevProblem P, int J
 // The dynamic shared-memory limit of k_diag_c only ever grows.
 cudaError_t diag_c_smem_attr(size_t smem) {
     static size_t configured = 0;
-    if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_diag_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = smem;
-    }
-    return cudaSuccess;
+    return raise_smem_limit((const void *)k_diag_c, &configured, smem);
 }
 
 cudaError_t launch_diag_c(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st) {

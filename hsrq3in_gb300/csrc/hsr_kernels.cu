@@ -25,8 +25,21 @@
 #include "hsr_kernels.h"
 
 #include <cfloat>
+#include <mutex>
 
 namespace hsr {
+
+// Raise a kernel's dynamic shared-memory limit to at least `smem`.  The
+// limit only grows, under one lock, so a host thread never lowers it below
+// what another thread's launch already relies on.
+cudaError_t raise_smem_limit(const void *func, size_t *configured, size_t smem) {
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    if (smem <= *configured) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) *configured = smem;
+    return e;
+}
 
 // --------------------------------------------------------------- norms
 // Row sums of |H| accumulated column by column in order, as LAPACK dlange
@@ -510,12 +523,7 @@ __global__ void __launch_bounds__(32 * kDiagWarps) k_diag(DevProblem P, int J, d
 // never find it lowered below what an earlier launch configured.
 cudaError_t diag_smem_attr(size_t smem) {
     static size_t configured = 0;
-    if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = smem;
-    }
-    return cudaSuccess;
+    return raise_smem_limit((const void *)k_diag, &configured, smem);
 }
 
 cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st) {
@@ -1003,12 +1011,11 @@ k_gemm_c(DevProblem P, int J, int row_lo, int row_hi, const __grid_constant__ CU
 
 cudaError_t launch_gemm(const DevProblem &P, int J, int row_lo, int row_hi, const CUtensorMap &tmH,
                         const CUtensorMap &tmW, const CUtensorMap &tmZ, cudaStream_t st) {
-    static bool configured = false;
+    static size_t configured = 0;
     const size_t smem = gemm_smem_bytes();
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    {
+        const cudaError_t e = raise_smem_limit((const void *)k_gemm, &configured, smem);
         if (e != cudaSuccess) return e;
-        configured = true;
     }
     if (row_hi <= row_lo) return cudaSuccess;
     const int span = row_hi - (row_lo & ~7);
@@ -1019,12 +1026,11 @@ cudaError_t launch_gemm(const DevProblem &P, int J, int row_lo, int row_hi, cons
 
 cudaError_t launch_gemm_c(const DevProblem &P, int J, int row_lo, int row_hi, const CUtensorMap &tmH,
                           const CUtensorMap &tmW, const CUtensorMap &tmZ, cudaStream_t st) {
-    static bool configured = false;
+    static size_t configured = 0;
     const size_t smem = gemm_smem_bytes();
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_gemm_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    {
+        const cudaError_t e = raise_smem_limit((const void *)k_gemm_c, &configured, smem);
         if (e != cudaSuccess) return e;
-        configured = true;
     }
     if (row_hi <= row_lo) return cudaSuccess;
     const int span = row_hi - (row_lo & ~7);
@@ -1278,10 +1284,9 @@ cudaError_t launch_diag_b(const DevProblem *probs, const BatchItem *items, int n
     const size_t smem = diag_smem_bytes_nw(bmax, kDiagWarpsB);
     if (smem < (size_t)64 * bmax * sizeof(double)) return cudaErrorInvalidValue;   // must fit shared memory
     static size_t configured = 0;
-    if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_diag_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    {
+        const cudaError_t e = raise_smem_limit((const void *)k_diag_b, &configured, smem);
         if (e != cudaSuccess) return e;
-        configured = smem;
     }
     if (n_items <= 0) return cudaSuccess;
     k_diag_b<<<n_items, 32 * kDiagWarpsB, smem, st>>>(probs, items);
@@ -1294,12 +1299,11 @@ cudaError_t launch_part1_b(const DevProblem *probs, const BatchItem *items, int 
 }
 cudaError_t launch_gemm_b(const DevProblem *probs, const BatchItem *items, int n_items, const CUtensorMap *maps,
                           cudaStream_t st) {
-    static bool configured = false;
+    static size_t configured = 0;
     const size_t smem = gemm_smem_bytes();
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_gemm_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    {
+        const cudaError_t e = raise_smem_limit((const void *)k_gemm_b, &configured, smem);
         if (e != cudaSuccess) return e;
-        configured = true;
     }
     if (n_items <= 0) return cudaSuccess;
     k_gemm_b<<<n_items, 256, smem, st>>>(probs, items, maps);

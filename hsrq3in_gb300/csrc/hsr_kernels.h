@@ -56,6 +56,10 @@ struct DevProblem {
 // z, w = block indices whose meaning depends on the kernel.
 typedef int4 BatchItem;
 
+// Raise a kernel's dynamic shared-memory limit to at least `smem`; the limit
+// only grows (one lock for all kernels).  `configured` is the kernel's cache.
+cudaError_t raise_smem_limit(const void *func, size_t *configured, size_t smem);
+
 // Setup: tile norms, eps3 = ||H||_oo * eps/2.  hnbits/Hnbits/hnorm_bits are
 // zeroed by the caller.
 cudaError_t launch_norms(const DevProblem &P, unsigned long long *Hn_bits,
