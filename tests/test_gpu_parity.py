@@ -159,3 +159,30 @@ def test_passes_by_hbm_budget(gpu_lib):
     assert np.array_equal(one["vr"], split["vr"])
     assert np.array_equal(one["scale"], split["scale"])
     assert np.array_equal(one["status"], split["status"])
+
+
+def test_concurrent_host_threads(gpu_lib):
+    """Calls from different host threads use separate workspaces and streams:
+    two threads solving different problems with different tile sizes (and so
+    different shared-memory footprints) concurrently get the results of the
+    same calls made one after the other."""
+    import threading
+    jobs = []
+    for n, tlsz, seed in ((300, 40, 51), (257, 88, 52), (410, 200, 53)):
+        H, lam = G.real_spectrum(n, seed)
+        jobs.append((H, G.perturbed_shifts(lam, seed + 1)[:120], tlsz))
+    serial = [_device(H, wr, t) for H, wr, t in jobs]
+    out = [None] * len(jobs)
+
+    def work(k):
+        H, wr, t = jobs[k]
+        for _ in range(3):
+            out[k] = _device(H, wr, t)
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(len(jobs))]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    for a, b in zip(serial, out):
+        assert np.array_equal(a["vr"], b["vr"]) and np.array_equal(a["wr"], b["wr"])
