@@ -32,6 +32,7 @@ EXPORTS = [
     "hsr_autotune_tlsz", "hsr_autotune_batch",
     "hsr_server_create", "hsr_server_replay", "hsr_server_destroy",
     "hsr_inverse_iteration_cplx_ex", "hsr_inverse_iteration_cplx_device", "hsr_inverse_iteration_mixed",
+    "hsr_selftest_bounded_wait",
 ]
 NOALLOC_MAX_N = 256
 NOALLOC_MAX_NRHS = 256
@@ -118,6 +119,8 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     lib.hsr_inverse_iteration_mixed.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                                 C.c_int, C.c_int, C.c_void_p, C.c_int, C.POINTER(Options),
                                                 C.c_void_p]
+    lib.hsr_selftest_bounded_wait.restype = C.c_int
+    lib.hsr_selftest_bounded_wait.argtypes = [C.c_void_p]
     lib.hsr_residuals_device.restype = C.c_int
     lib.hsr_residuals_device.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                          C.c_void_p, C.c_void_p]

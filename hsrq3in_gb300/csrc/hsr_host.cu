@@ -6,6 +6,7 @@
 // intended semantics), and copies vr and wr back.  Workspaces are cached per
 // host thread and grow on demand.
 #include "hsr_common.h"
+#include "hsr_device.cuh"
 #include "hsr_kernels.h"
 #include "../../include/hsrq3in_gb300.h"
 
@@ -1155,6 +1156,20 @@ int hsr_probe_fp64_peak(double ms_target, double *dfma_gflops, double *dmma_gflo
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return rc ? HSR_ERR_CUDA : HSR_OK;
+}
+
+int hsr_selftest_bounded_wait(void *stream) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    Workspace &w = ws();
+    HSR_CK(w.err.ensure(16));
+    HSR_CK(cudaMemsetAsync(w.err.p, 0, 16, st));
+    HSR_CK(launch_wait_selftest(w.err.as<int>(), 1L << 14, st));
+    int errw = 0;
+    HSR_CK(cudaMemcpyAsync(&errw, w.err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    HSR_CK(cudaStreamSynchronize(st));
+    HSR_CK(cudaMemsetAsync(w.err.p, 0, 16, st));
+    HSR_CK(cudaStreamSynchronize(st));
+    return g_last_status = (errw & kErrWaitTimeout) ? HSR_ERR_DEVICE : HSR_OK;
 }
 
 const char *hsr_version(void) { return "hsrq3in_gb300 0.1 (sm_103a, FP64 DFMA)"; }

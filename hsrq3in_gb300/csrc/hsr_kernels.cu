@@ -1320,6 +1320,26 @@ cudaError_t launch_normalize_b(const DevProblem *probs, const BatchItem *items, 
     return cudaGetLastError();
 }
 
+// ------------------------------------------------ bounded-wait self-test
+// One thread initialises an mbarrier that expects two arrivals, arrives once
+// and waits with the library's bounded wait: the phase can never complete, so
+// the wait gives up after `limit` polls and records kErrWaitTimeout, exactly
+// as a GEMM wait on a TMA copy that never lands would.  Nothing faults and
+// the kernel returns.
+__global__ void k_wait_selftest(int *err, long limit) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x != 0) return;
+    mbar_init(&bar, 2);
+    mbar_fence_init();
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&bar)) : "memory");
+    mbar_wait(&bar, 0, err, limit);
+}
+
+cudaError_t launch_wait_selftest(int *err, long limit, cudaStream_t st) {
+    k_wait_selftest<<<1, 32, 0, st>>>(err, limit);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------- FP64 peak probe
 // Eight independent FMA chains per thread; a and b are launch arguments so
 // the chains cannot be folded.

@@ -128,6 +128,10 @@ cudaError_t launch_gemm_c(const DevProblem &P, int J, int row_lo, int row_hi, co
 cudaError_t launch_finalize_c(const DevProblem &P, double *colnorm, int *status, double *scale_out,
                               cudaStream_t st);
 
+// Bounded-wait self-test: a wait that cannot complete, given up after
+// `limit` polls with kErrWaitTimeout recorded in *err.
+cudaError_t launch_wait_selftest(int *err, long limit, cudaStream_t st);
+
 // FP64 throughput probe kernels.
 cudaError_t launch_probe_dfma(double *out, int blocks, int iters, cudaStream_t st);
 cudaError_t launch_probe_dmma(double *out, int blocks, int iters, cudaStream_t st);

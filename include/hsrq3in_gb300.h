@@ -318,6 +318,14 @@ int hsr_inverse_iteration_noalloc(int n, const double *dH, int lddH, int nrhs,
 int hsr_probe_fp64_peak(double ms_target, double *dfma_gflops,
                         double *dmma_gflops);
 
+/* Failure-detection self-test: launches one wait on a barrier that can never
+ * complete, through the same bounded wait the GEMM uses on its TMA copies.
+ * The wait gives up after a short poll limit and records its error bit, the
+ * kernel returns, and the call reports HSR_ERR_DEVICE -- the status a real
+ * stalled copy would produce -- while the context stays usable.  Returns
+ * HSR_OK only if the wait did not report.  No reference counterpart. */
+int hsr_selftest_bounded_wait(void *stream);
+
 /* Library version string. */
 const char *hsr_version(void);
 

@@ -186,3 +186,17 @@ def test_concurrent_host_threads(gpu_lib):
         th.join()
     for a, b in zip(serial, out):
         assert np.array_equal(a["vr"], b["vr"]) and np.array_equal(a["wr"], b["wr"])
+
+
+def test_bounded_wait_reports_and_context_survives(gpu_lib):
+    """Failure detection without a fault: a device wait that can never
+    complete gives up after its poll limit, the call reports HSR_ERR_DEVICE,
+    and the context stays usable -- the next solve is bit-exact to the oracle."""
+    from hsrq3in_gb300 import _lib
+    assert gpu_lib.hsr_selftest_bounded_wait(None) == _lib.HSR_ERR_DEVICE
+    n, tlsz = 64, 16
+    H, lam = G.real_spectrum(n, 61)
+    wr = G.perturbed_shifts(lam, 62)
+    dev = _device(H, wr, tlsz)
+    orc = O.oracle_inverse_iteration(H, wr, tlsz, 16, intscale=1, variant="fma")
+    assert dev["rc"] == 0 and np.array_equal(dev["vr"], orc["vr"])
