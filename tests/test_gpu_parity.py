@@ -200,3 +200,42 @@ def test_bounded_wait_reports_and_context_survives(gpu_lib):
     dev = _device(H, wr, tlsz)
     orc = O.oracle_inverse_iteration(H, wr, tlsz, 16, intscale=1, variant="fma")
     assert dev["rc"] == 0 and np.array_equal(dev["vr"], orc["vr"])
+
+
+@pytest.mark.parametrize("extra_h,extra_v", [(1, 3), (3, 0), (0, 5)])
+def test_leading_dimensions_through_c_abi(gpu_lib, extra_h, extra_v):
+    """The drop-in call with ldH = n + extra_h (odd pitches are re-padded for
+    TMA) and ldvr = n + extra_v: the result equals the compact call bit for
+    bit and the caller's padding rows of vr are left untouched; the same for
+    the complex-shift entry."""
+    import ctypes as C
+    from hsrq3in_gb300 import _lib
+    n, tlsz, m = 97, 24, 20
+    H, lam = G.real_spectrum(n, 71)
+    wr = np.ascontiguousarray(G.perturbed_shifts(lam, 72)[:m])
+    ldh, ldv = n + extra_h, n + extra_v
+    Hp = np.full((ldh, n), 7.0, order="F")
+    Hp[:n, :] = H
+    ref = _device(H, wr, tlsz)
+    vr = np.full((ldv, m), -3.25, order="F")
+    w = wr.copy()
+    gpu_lib.tiled_inverse_iteration(n, Hp.ctypes.data, ldh, m, w.ctypes.data, tlsz, 16, vr.ctypes.data, ldv)
+    assert gpu_lib.hsr_last_status() == 0
+    assert np.array_equal(vr[:n], ref["vr"]) and np.array_equal(w, ref["wr"])
+    assert np.all(vr[n:] == -3.25)
+    Hc, pairs, _ = G.complex_spectrum(n, 73)
+    Hcp = np.full((ldh, n), 7.0, order="F")
+    Hcp[:n, :] = Hc
+    cref = hsr_cplx(Hc, pairs[:10], tlsz)
+    vc = np.full((ldv, 20), -3.25, order="F")
+    a, b = np.ascontiguousarray(pairs[:10].real), np.ascontiguousarray(pairs[:10].imag)
+    opt = _lib.Options(0, 0, -1, 0.0)
+    rc = gpu_lib.hsr_inverse_iteration_cplx_ex(n, Hcp.ctypes.data, ldh, 10, a.ctypes.data, b.ctypes.data, tlsz, 16,
+                                               vc.ctypes.data, ldv, C.byref(opt), None)
+    assert rc == 0
+    assert np.array_equal(vc[:n], cref["vr"]) and np.all(vc[n:] == -3.25)
+
+
+def hsr_cplx(H, mu, tlsz):
+    import hsrq3in_gb300 as hsr
+    return hsr.inverse_iteration_cplx(H, mu, tlsz, 16)
