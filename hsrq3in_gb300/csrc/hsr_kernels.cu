@@ -151,24 +151,30 @@ cudaError_t launch_init(const DevProblem &P, int mode, const double *eps3_dev, i
 
 // -------------------------------------------------------------- diagonal
 // 32 shifts per CTA, one per lane, and NW warps per CTA.  The FP64 unit is
-// per SM sub-partition, so with NW = 4 the vector part of each step (the
-// updates of y(0:j-2) and of the running column) is split over the four
-// warps by row (i mod 4) and a lone CTA keeps all four sub-partitions busy,
-// while every warp evaluates the short scalar chain of the step (Givens, 1x1
-// solve, overflow decisions) itself -- identical arithmetic, no broadcast.
-// That replication costs FP64 issue slots, so where many CTAs share the GPU
-// (the batched engine) NW = 1 does the same work with the fewest FP64
-// instructions.  v (running column) and y (solution tile) live in shared
-// memory as [row][lane]; the column of H needed by step j is staged one step
-// ahead with cp.async and read as a broadcast.  Per-warp maxima of |y| and
-// |v| meet in shared memory once per step.  When 2*32*b doubles do not fit,
-// v/y live in a global scratch region instead (same code, generic pointers).
+// per SM sub-partition, so the single-problem kernel (k_diag) runs NW = 4
+// warps and a lone CTA keeps all four sub-partitions busy: warp 0 evaluates
+// the short scalar chain of each step (Givens, 1x1 solve, overflow
+// decisions) and warps 1-3 split the vector part (the updates of y(0:j-2)
+// and of the running column) by row, one step behind the chain
+// (diag_body_pipe).  Where many CTAs share the GPU (the batched engine) one
+// warp per CTA does the same work with the fewest FP64 instructions
+// (diag_body<1>).  v (running column) and y (solution tile) live in shared
+// memory as [row][lane]; columns of H are staged ahead with cp.async and
+// read as broadcasts.  Per-warp maxima of |y| and |v| meet in shared memory
+// once per step.  When 2*32*b doubles do not fit, v/y live in a global
+// scratch region instead (same code, generic pointers).
 constexpr int kDiagWarps = 4;     // single-problem path
 constexpr int kDiagWarpsB = 1;    // batched path
 
 constexpr int kDiagBcast = 8;      // per-lane step results broadcast by warp 0
-constexpr size_t diag_small_bytes(int b, int nw) {
-    return (size_t)(2 * (b + 1)) * sizeof(double) + (size_t)2 * nw * 2 * 32 * 8 +
+// Staging buffers for columns of H: the pipelined multi-warp body keeps three
+// in flight (rows of step j, chain of step j-1, copy for step j-2), the
+// single-warp body two.
+__host__ __device__ constexpr int diag_col_bufs(int nw) { return nw > 1 ? 3 : 2; }
+// Shared memory of everything but v/y: column buffers, per-warp maxima
+// [2][nw][2][32] and, with several warps, the broadcast slots.
+__host__ __device__ constexpr size_t diag_small_bytes(int b, int nw) {
+    return (size_t)(diag_col_bufs(nw) * (b + 1)) * sizeof(double) + (size_t)2 * nw * 2 * 32 * 8 +
            (nw > 1 ? (size_t)kDiagBcast * 32 * 8 : 0);
 }
 size_t diag_smem_bytes_nw(int b, int nw) {
@@ -514,9 +520,385 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
 #undef BC
 }
 
+// The four-warp diagonal kernel, software-pipelined by one step.  Step j's
+// scalar chain (Givens, 1x1 solve, three overflow decisions) runs on warp 0
+// and feeds the row updates of step j, which run on warps 1-3; warp 0 first
+// updates row j-2 itself and then evaluates the first two parts of step
+// j-1's chain -- everything that does not need the new row maxima -- while
+// warps 1-3 are still updating rows 0 .. j-3.  After a barrier warp 0 folds
+// their maxima into the third decision of step j-1 and publishes that step's
+// scalars; a second barrier hands them to warps 1-3.  Every row sees the
+// same operations in the same order as in the unpipelined form (and the
+// oracle), and the maxima cover the same rows, so the result is unchanged
+// bit for bit.  The H column of step j-1 is staged with cp.async two steps
+// ahead (three buffers: the rows of step j, the chain of step j-1, the copy
+// for step j-2).
+__device__ __forceinline__ void diag_body_pipe(const DevProblem &P, int J, int bx, double *vy_scratch) {
+    constexpr int NW = kDiagWarps;
+    extern __shared__ double sm[];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    const int k0 = bx * 32;
+    const int k = k0 + lane;
+    const bool act = k < P.S;
+    const int l = P.fr[J], b = P.fr[J + 1] - l;
+    const bool is = P.is != 0;
+    const size_t Spad = (size_t)P.Spad;
+
+    constexpr int NB = diag_col_bufs(NW);                                     // 3 column buffers
+    double *hc = sm;                                                          // [NB][b+1]
+    unsigned long long *pmax = reinterpret_cast<unsigned long long *>(sm + NB * (b + 1));  // [NW][2][32]
+    double *bc = sm + NB * (b + 1) + 2 * NW * 2 * 32;                         // [kDiagBcast][32]
+    double *v, *y;
+    if (vy_scratch) {
+        v = vy_scratch;
+        y = v + (size_t)32 * b;
+    } else {
+        v = bc + kDiagBcast * 32;
+        y = v + (size_t)32 * b;
+    }
+#define V(i) v[(size_t)(i) * 32 + lane]
+#define Y(i) y[(size_t)(i) * 32 + lane]
+#define PM(w, which) pmax[(((w) * 2) + (which)) * 32 + lane]
+#define BC(q) bc[(q) * 32 + lane]
+#define HCOL(col) (hc + (size_t)((col) % NB) * (b + 1))
+
+    for (int c = wid; c < 32; c += NW) {
+        const int kc = k0 + c;
+        if (kc < P.S) {
+            const double *rc = P.R + l + (size_t)kc * P.ldr;
+            const double *xc = P.X + l + (size_t)kc * P.ldx;
+            for (int i = lane; i < b; i += 32) {
+                v[(size_t)i * 32 + c] = rc[i];
+                y[(size_t)i * 32 + c] = xc[i];
+            }
+        } else {
+            for (int i = lane; i < b; i += 32) {
+                v[(size_t)i * 32 + c] = 1.0;
+                y[(size_t)i * 32 + c] = 0.0;
+            }
+        }
+    }
+
+    const double mu = act ? P.wr[k] : 0.0;
+    const double smin = fmax(DBL_EPSILON / 2 * fabs(mu), P.smlnum);
+    const double Hnorm = P.Hn[J + (size_t)J * P.T];
+    double beta = act ? P.beta[(size_t)J * Spad + k] : sc_one(is);
+    int pert = 0;
+
+    const double *Hd = P.H + l + (size_t)l * P.ldh;                           // H(l, l)
+    auto stage_col = [&](int col) {                                           // H(l : l+col+1, l+col), warp 0
+        int rows = col + 2;
+        if (rows > b) rows = b;
+        const double *src = Hd + (size_t)col * P.ldh;
+        double *dst = HCOL(col);
+        for (int i = lane; i < rows; i += 32) cp_async8(dst + i, src + i);
+        cp_async_commit();
+    };
+    if (wid == 0 && b >= 2) stage_col(b - 2);
+    if (wid == 0 && b >= 3) stage_col(b - 3);
+    if (wid == 0) cp_async_wait_all();
+    __syncthreads();                                                          // tiles and columns loaded
+
+    // Maxima of |y(0:b-3)| and |v(0:b-3)| for the first step, by warps 1-3.
+    {
+        unsigned long long ym = 0, vm = 0;
+        if (wid > 0)
+            for (int i = wid - 1; i < b - 2; i += NW - 1) {
+                ym = umax64(ym, abs_bits(Y(i)));
+                vm = umax64(vm, abs_bits(V(i)));
+            }
+        PM(wid, 0) = ym;
+        PM(wid, 1) = vm;
+    }
+
+    // Chain state of warp 0.
+    double vcar = V(b - 1), ycar = Y(b - 1);
+    double c = 0.0, s = 0.0, yc = 0.0, ys = 0.0, a1 = 1.0, a2 = 1.0, a3 = 1.0, yj = 0.0, yjm1 = 0.0;
+
+    // Parts 1-2 of step jj's chain: Givens, the 1x1 solve and the y(jj-1)
+    // decision and update (solve-task.c:76-90), and the next running column
+    // entry (solve-task.c:105-108).  vjm1, yjm1 enter as row jj-1.
+    auto chain12 = [&](int jj, double vjm1, double yjm1_in) {
+        const double *hcol = HCOL(jj - 1);
+        const double hsub = hcol[jj];
+        const double hdiag = hcol[jj - 1] - mu;
+        const double vj = vcar;
+        yj = ycar;
+        yjm1 = yjm1_in;
+        givens(vj, hsub, c, s);
+        if (act) {
+            P.Cr[(size_t)(l + jj) * Spad + k] = c;
+            P.Sr[(size_t)(l + jj) * Spad + k] = s;
+        }
+        double phi = sc_one(is);
+        pert |= solve_1x1(smin, c * vj, s * hsub, yj, phi, is);
+        beta = sc_combine(beta, phi, is);
+        a1 = sc_value(phi, is);
+        if (!is_one(a1)) yjm1 = a1 * yjm1;
+        phi = protect_double_update(fabs(vjm1), fabs(yj), fabs(hdiag), fabs(yj), fabs(yjm1), is);
+        a2 = sc_value(phi, is);
+        if (!is_one(a2)) {
+            yj = a2 * yj;
+            yjm1 = a2 * yjm1;
+        }
+        beta = sc_combine(beta, phi, is);
+        yc = yj * c;
+        ys = yj * s;
+        yjm1 = fma(ys, hdiag, fma(-yc, vjm1, yjm1));
+        vcar = fma(c, hdiag, s * vjm1);
+    };
+    // Part 3 of step jj's chain: the y(0:jj-2) decision (solve-task.c:92-100)
+    // with the maxima of rows 0 .. jj-2 folded by warps 1-3, then the step's
+    // scalars for the row warps, the solved entry y(jj) and y(jj-1).
+    auto chain3 = [&](int jj) {
+        unsigned long long ymb = 0, vmb = 0;
+#pragma unroll
+        for (int w = 1; w < NW; ++w) {
+            ymb = umax64(ymb, PM(w, 0));
+            vmb = umax64(vmb, PM(w, 1));
+        }
+        double ymax = from_bits(ymb);
+        if (!is_one(a1)) ymax = from_bits(abs_bits(a1 * ymax));
+        if (!is_one(a2)) ymax = from_bits(abs_bits(a2 * ymax));
+        const double phi = protect_double_update(from_bits(vmb), fabs(yj), Hnorm, fabs(yj), ymax, is);
+        a3 = sc_value(phi, is);
+        if (!is_one(a3)) {
+            yj = a3 * yj;
+            yjm1 = a3 * yjm1;
+            yc = yj * c;
+            ys = yj * s;
+        }
+        beta = sc_combine(beta, phi, is);
+        BC(0) = c;
+        BC(1) = s;
+        BC(2) = yc;
+        BC(3) = ys;
+        BC(4) = a1;
+        BC(5) = a2;
+        BC(6) = a3;
+        Y(jj) = yj;
+        ycar = yjm1;
+    };
+
+    if (wid == 0 && b >= 2) {
+        chain12(b - 1, V(b - 2), Y(b - 2));
+        chain3(b - 1);
+    }
+    __syncthreads();                                                          // step b-1's scalars visible
+
+    for (int j = b - 1; j >= 1; --j) {
+        // Step j's scalars: registers on warp 0, shared memory for the rest.
+        double sc_c = c, sc_s = s, sc_yc = yc, sc_ys = ys, s1 = a1, s2 = a2, s3 = a3;
+        if (wid != 0) {
+            sc_c = BC(0);
+            sc_s = BC(1);
+            sc_yc = BC(2);
+            sc_ys = BC(3);
+            s1 = BC(4);
+            s2 = BC(5);
+            s3 = BC(6);
+        }
+        const bool scaled = (!is_one(s1)) || (!is_one(s2)) || (!is_one(s3));
+        const double *hcol = HCOL(j - 1);
+        if (wid == 0) {
+            // Row j-2 first: it enters step j-1's chain.
+            double vn = 0.0, yn = 0.0;
+            if (j >= 2) {
+                const double h = hcol[j - 2];
+                double yi = Y(j - 2);
+                const double vi = V(j - 2);
+                if (scaled) {
+                    if (!is_one(s1)) yi = s1 * yi;
+                    if (!is_one(s2)) yi = s2 * yi;
+                    if (!is_one(s3)) yi = s3 * yi;
+                }
+                yn = fma(sc_ys, h, fma(-sc_yc, vi, yi));
+                vn = fma(sc_c, h, sc_s * vi);
+                Y(j - 2) = yn;
+                V(j - 2) = vn;
+            }
+            if (j >= 2) {
+                cp_async_wait_all();                                          // column j-2, staged last step
+                __syncwarp();                                                 // ... by all lanes of warp 0
+                chain12(j - 1, vn, yn);
+            }
+            if (j >= 3) stage_col(j - 3);                                     // for step j-2's chain
+        } else {
+            if (scaled) {
+                for (int i = j + 1 + ((wid - 1 - (j + 1)) % (NW - 1) + (NW - 1)) % (NW - 1); i < b; i += NW - 1) {
+                    double t = Y(i);
+                    if (!is_one(s1)) t = s1 * t;
+                    if (!is_one(s2)) t = s2 * t;
+                    if (!is_one(s3)) t = s3 * t;
+                    Y(i) = t;
+                }
+            }
+            unsigned long long ymx = 0, vmx = 0;
+            const int lim = j - 2;                                            // rows 0 .. j-3
+            int i = wid - 1;
+            for (; i + 3 * (NW - 1) < lim; i += 4 * (NW - 1)) {
+                double hh[4], yy[4], vv[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    hh[q] = hcol[i + q * (NW - 1)];
+                    yy[q] = Y(i + q * (NW - 1));
+                    vv[q] = V(i + q * (NW - 1));
+                }
+                if (scaled) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        if (!is_one(s1)) yy[q] = s1 * yy[q];
+                        if (!is_one(s2)) yy[q] = s2 * yy[q];
+                        if (!is_one(s3)) yy[q] = s3 * yy[q];
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    yy[q] = fma(sc_ys, hh[q], fma(-sc_yc, vv[q], yy[q]));
+                    vv[q] = fma(sc_c, hh[q], sc_s * vv[q]);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int r = i + q * (NW - 1);
+                    Y(r) = yy[q];
+                    V(r) = vv[q];
+                    ymx = umax64(ymx, abs_bits(yy[q]));
+                    vmx = umax64(vmx, abs_bits(vv[q]));
+                }
+            }
+            for (; i < lim; i += NW - 1) {
+                const double h = hcol[i];
+                double yi = Y(i), vi = V(i);
+                if (scaled) {
+                    if (!is_one(s1)) yi = s1 * yi;
+                    if (!is_one(s2)) yi = s2 * yi;
+                    if (!is_one(s3)) yi = s3 * yi;
+                }
+                yi = fma(sc_ys, h, fma(-sc_yc, vi, yi));
+                vi = fma(sc_c, h, sc_s * vi);
+                Y(i) = yi;
+                V(i) = vi;
+                ymx = umax64(ymx, abs_bits(yi));
+                vmx = umax64(vmx, abs_bits(vi));
+            }
+            PM(wid, 0) = ymx;
+            PM(wid, 1) = vmx;
+        }
+        __syncthreads();                                                      // rows of step j done, maxima in
+        if (wid == 0 && j >= 2) chain3(j - 1);
+        __syncthreads();                                                      // step j-1's scalars visible
+    }
+
+    constexpr bool kBcast = true;
+    double c0 = 0.0, s0 = 0.0;
+    {
+        double y0 = 0.0, a = 1.0;
+        if (!kBcast || wid == 0) {
+            double v0 = b >= 2 ? vcar : V(0);
+            y0 = b >= 2 ? ycar : Y(0);
+            double hleft = 0.0;
+            if (J > 0) {
+                // Final rotation with H(l, l-1) (reduce.c:53-61, solve-task.c:111-118).
+                hleft = P.H[l + (size_t)(l - 1) * P.ldh];
+                if (hleft != 0) {
+                    givens(v0, hleft, c0, s0);
+                } else {
+                    c0 = 1.0;
+                    s0 = 0.0;
+                }
+                if (act && wid == 0) {
+                    P.Cr[(size_t)l * Spad + k] = c0;
+                    P.Sr[(size_t)l * Spad + k] = s0;
+                }
+                v0 = fma(v0, c0, -(hleft * s0));
+            }
+            double phi = sc_one(is);
+            pert |= solve_1x1(smin, v0, 0.0, y0, phi, is);
+            beta = sc_combine(beta, phi, is);
+            a = sc_value(phi, is);
+            if (kBcast) {
+                BC(0) = c0;
+                BC(1) = s0;
+                BC(2) = a;
+            }
+        }
+        __syncthreads();                                       // last step's rows (and the scalars) written
+        if (kBcast && wid != 0) {
+            c0 = BC(0);
+            s0 = BC(1);
+            a = BC(2);
+        }
+        if (!is_one(a))
+            for (int i = 1 + ((wid - 1) % kDiagWarps + kDiagWarps) % kDiagWarps; i < b; i += kDiagWarps)
+                Y(i) = a * Y(i);
+        if (wid == 0) Y(0) = y0;
+    }
+    __syncthreads();
+
+    // Store the solved tile, its scaling factor and the perturbation flag.
+    for (int c = wid; c < 32; c += kDiagWarps) {
+        const int kc = k0 + c;
+        if (kc < P.S) {
+            double *xc = P.X + l + (size_t)kc * P.ldx;
+            for (int i = lane; i < b; i += 32) xc[i] = y[(size_t)i * 32 + c];
+        }
+    }
+    if (act && wid == 0) {
+        P.beta[(size_t)J * Spad + k] = beta;
+        if (pert) P.pert[k] = 1;
+    }
+    if (J == 0 || !act) return;
+
+    if (wid == 0) {
+        // W(q) = c_q * prod_{p<q} s_p, pi = prod s (crossover propagation).
+        double pk = 1.0;
+        for (int q = 0; q < b; ++q) {
+            const double cq = P.Cr[(size_t)(l + q) * Spad + k];
+            const double sq = P.Sr[(size_t)(l + q) * Spad + k];
+            P.W[(size_t)q * Spad + k] = cq * pk;
+            pk = pk * sq;
+        }
+        P.pi[k] = pk;
+    }
+    if (wid == (kDiagWarps > 1 ? 1 : 0)) {
+        // Ytilde2 = G_{b-1}^T ... G_1^T (c_0 x_0, x_1, ...) (update-task.c:193-220);
+        // Zs(q) = Ytilde2(q-1), Zs(0) = 0, zlast = Ytilde2(b-1).
+        unsigned long long zmx = 0;
+        double z = c0 * Y(0);
+        P.Zs[k] = 0.0;
+        for (int q = 1; q < b; ++q) {
+            const double cq = P.Cr[(size_t)(l + q) * Spad + k];
+            const double sq = P.Sr[(size_t)(l + q) * Spad + k];
+            const double t1 = z, t2 = Y(q);
+            const double zo = fma(cq, t1, -(sq * t2));
+            z = fma(sq, t1, cq * t2);
+            P.Zs[(size_t)q * Spad + k] = zo;
+            zmx = umax64(zmx, abs_bits(zo));
+        }
+        zmx = umax64(zmx, abs_bits(z));
+        P.zlast[k] = z;
+        P.z2n[k] = from_bits(zmx);
+        P.ytil[k] = -s0 * Y(0);
+    }
+#undef V
+#undef Y
+#undef PM
+#undef HCOL
+#undef BC
+}
+
+
 __global__ void __launch_bounds__(32 * kDiagWarps) k_diag(DevProblem P, int J, double *gscratch) {
     const int b = P.fr[J + 1] - P.fr[J];
-    diag_body<kDiagWarps>(P, J, blockIdx.x, gscratch ? gscratch + (size_t)blockIdx.x * 64 * b : nullptr);
+    // The layout needs diag_small_bytes (+ v/y unless they are in global
+    // scratch); a launch given less records a shape error and touches nothing.
+    const size_t need = diag_small_bytes(b, kDiagWarps) + (gscratch ? 0 : (size_t)64 * b * sizeof(double));
+    if (need > dynamic_smem_bytes()) {
+        if (threadIdx.x == 0) atomicOr(P.err, kErrShape);
+        return;
+    }
+    diag_body_pipe(P, J, blockIdx.x, gscratch ? gscratch + (size_t)blockIdx.x * 64 * b : nullptr);
 }
 
 // The dynamic shared-memory limit of k_diag only ever grows: a launch must
