@@ -152,10 +152,10 @@ cudaError_t launch_init(const DevProblem &P, int mode, const double *eps3_dev, i
 // -------------------------------------------------------------- diagonal
 // 32 shifts per CTA, one per lane, and NW warps per CTA.  The FP64 unit is
 // per SM sub-partition, so the single-problem kernel (k_diag) runs NW = 4
-// warps and a lone CTA keeps all four sub-partitions busy: warp 0 evaluates
-// the short scalar chain of each step (Givens, 1x1 solve, overflow
-// decisions) and warps 1-3 split the vector part (the updates of y(0:j-2)
-// and of the running column) by row, one step behind the chain
+// or 8 warps and a lone CTA keeps all four sub-partitions busy: warp 0
+// evaluates the short scalar chain of each step (Givens, 1x1 solve, overflow
+// decisions) and warps 1 .. NW-1 split the vector part (the updates of
+// y(0:j-2) and of the running column) by row, one step behind the chain
 // (diag_body_pipe).  Where many CTAs share the GPU (the batched engine) one
 // warp per CTA does the same work with the fewest FP64 instructions
 // (diag_body<1>).  v (running column) and y (solution tile) live in shared
@@ -163,7 +163,8 @@ cudaError_t launch_init(const DevProblem &P, int mode, const double *eps3_dev, i
 // read as broadcasts.  Per-warp maxima of |y| and |v| meet in shared memory
 // once per step.  When 2*32*b doubles do not fit, v/y live in a global
 // scratch region instead (same code, generic pointers).
-constexpr int kDiagWarps = 4;     // single-problem path
+constexpr int kDiagWarps = 4;     // single-problem path, v/y in global scratch
+constexpr int kDiagWarpsSmem = 8; // single-problem path, v/y in shared memory
 constexpr int kDiagWarpsB = 1;    // batched path
 
 constexpr int kDiagBcast = 8;      // per-lane step results broadcast by warp 0
@@ -182,7 +183,7 @@ size_t diag_smem_bytes_nw(int b, int nw) {
     const size_t full = small + (size_t)64 * b * sizeof(double);
     return full <= 200 * 1024 ? full : small;
 }
-size_t diag_smem_bytes(int b) { return diag_smem_bytes_nw(b, kDiagWarps); }
+size_t diag_smem_bytes(int b) { return diag_smem_bytes_nw(b, kDiagWarpsSmem); }
 
 // Body of the diagonal kernel for the 32 shifts of block bx; vy_scratch is
 // this block's global v/y region, or null when v/y fit in shared memory.
@@ -533,8 +534,8 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
 // bit for bit.  The H column of step j-1 is staged with cp.async two steps
 // ahead (three buffers: the rows of step j, the chain of step j-1, the copy
 // for step j-2).
+template <int NW>
 __device__ __forceinline__ void diag_body_pipe(const DevProblem &P, int J, int bx, double *vy_scratch) {
-    constexpr int NW = kDiagWarps;
     extern __shared__ double sm[];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
@@ -830,14 +831,14 @@ __device__ __forceinline__ void diag_body_pipe(const DevProblem &P, int J, int b
             a = BC(2);
         }
         if (!is_one(a))
-            for (int i = 1 + ((wid - 1) % kDiagWarps + kDiagWarps) % kDiagWarps; i < b; i += kDiagWarps)
+            for (int i = 1 + ((wid - 1) % NW + NW) % NW; i < b; i += NW)
                 Y(i) = a * Y(i);
         if (wid == 0) Y(0) = y0;
     }
     __syncthreads();
 
     // Store the solved tile, its scaling factor and the perturbation flag.
-    for (int c = wid; c < 32; c += kDiagWarps) {
+    for (int c = wid; c < 32; c += NW) {
         const int kc = k0 + c;
         if (kc < P.S) {
             double *xc = P.X + l + (size_t)kc * P.ldx;
@@ -861,7 +862,7 @@ __device__ __forceinline__ void diag_body_pipe(const DevProblem &P, int J, int b
         }
         P.pi[k] = pk;
     }
-    if (wid == (kDiagWarps > 1 ? 1 : 0)) {
+    if (wid == (NW > 1 ? 1 : 0)) {
         // Ytilde2 = G_{b-1}^T ... G_1^T (c_0 x_0, x_1, ...) (update-task.c:193-220);
         // Zs(q) = Ytilde2(q-1), Zs(0) = 0, zlast = Ytilde2(b-1).
         unsigned long long zmx = 0;
@@ -889,42 +890,55 @@ __device__ __forceinline__ void diag_body_pipe(const DevProblem &P, int J, int b
 }
 
 
-__global__ void __launch_bounds__(32 * kDiagWarps) k_diag(DevProblem P, int J, double *gscratch) {
+// NW warps: 8 (two per sub-partition, hiding FP64 latency) when v/y sit in
+// shared memory and the CTA has its SM mostly to itself; 4 when v/y are in
+// global scratch, where the CTAs share SMs with the concurrent GEMM's and a
+// smaller register footprint lets them co-reside.
+template <int NW>
+__global__ void __launch_bounds__(32 * NW) k_diag(DevProblem P, int J, double *gscratch) {
     const int b = P.fr[J + 1] - P.fr[J];
     // The layout needs diag_small_bytes (+ v/y unless they are in global
     // scratch); a launch given less records a shape error and touches nothing.
-    const size_t need = diag_small_bytes(b, kDiagWarps) + (gscratch ? 0 : (size_t)64 * b * sizeof(double));
+    const size_t need = diag_small_bytes(b, NW) + (gscratch ? 0 : (size_t)64 * b * sizeof(double));
     if (need > dynamic_smem_bytes()) {
         if (threadIdx.x == 0) atomicOr(P.err, kErrShape);
         return;
     }
-    diag_body_pipe(P, J, blockIdx.x, gscratch ? gscratch + (size_t)blockIdx.x * 64 * b : nullptr);
+    diag_body_pipe<NW>(P, J, blockIdx.x, gscratch ? gscratch + (size_t)blockIdx.x * 64 * b : nullptr);
 }
 
-// The dynamic shared-memory limit of k_diag only ever grows: a launch must
-// never find it lowered below what an earlier launch configured.
+// The dynamic shared-memory limit of each k_diag form only ever grows: a
+// launch must never find it lowered below what an earlier launch configured.
+template <int NW>
 cudaError_t diag_smem_attr(size_t smem) {
     static size_t configured = 0;
-    return raise_smem_limit((const void *)k_diag, &configured, smem);
+    return raise_smem_limit((const void *)k_diag<NW>, &configured, smem);
 }
 
 cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st) {
-    const size_t small = diag_small_bytes(b, kDiagWarps);
-    const size_t smem = gscratch ? small : diag_smem_bytes(b);
-    {
-        cudaError_t e = diag_smem_attr(smem);
+    const int grid = (P.S + 31) / 32;
+    if (gscratch) {
+        const size_t smem = diag_small_bytes(b, kDiagWarps);
+        const cudaError_t e = diag_smem_attr<kDiagWarps>(smem);
         if (e != cudaSuccess) return e;
+        k_diag<kDiagWarps><<<grid, 32 * kDiagWarps, smem, st>>>(P, J, gscratch);
+    } else {
+        const size_t smem = diag_smem_bytes(b);
+        const cudaError_t e = diag_smem_attr<kDiagWarpsSmem>(smem);
+        if (e != cudaSuccess) return e;
+        k_diag<kDiagWarpsSmem><<<grid, 32 * kDiagWarpsSmem, smem, st>>>(P, J, gscratch);
     }
-    k_diag<<<(P.S + 31) / 32, 32 * kDiagWarps, smem, st>>>(P, J, gscratch);
     return cudaGetLastError();
 }
 
 // CTAs of k_diag that one SM holds with v/y in shared memory (tile height b).
 int diag_ctas_per_sm(int b) {
     const size_t smem = diag_smem_bytes(b);
-    if (diag_smem_attr(smem) != cudaSuccess) return 0;
+    if (diag_smem_attr<kDiagWarpsSmem>(smem) != cudaSuccess) return 0;
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_diag, 32 * kDiagWarps, smem) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_diag<kDiagWarpsSmem>, 32 * kDiagWarpsSmem, smem) !=
+        cudaSuccess)
+        return 0;
     return nb;
 }
 
