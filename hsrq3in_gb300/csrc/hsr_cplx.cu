@@ -82,31 +82,42 @@ cudaError_t launch_init_c(const DevProblem &P, int mode, const double *eps3_dev,
 }
 
 // -------------------------------------------------------------- diagonal
-// 32 pairs per CTA, one per lane, on four warps (one per SM sub-partition).
-// Warp 0 evaluates each step's scalar chain -- complex Givens, the robust
-// complex 1x1 solve, the three overflow decisions -- and hands its results
-// to the others through shared memory; all four warps then update the rows
-// i = w, w+4, ... of y and of the running column v.  v and y live in shared
-// memory as [row][lane] (real and imaginary parts in separate arrays); when
-// 4*32*b doubles do not fit, in a global scratch region.  The bound of
-// y(0:j-2) is the largest cabs1 at the start of the step (folded by the four
-// warps during the previous step), times the step's scaling factors.
-constexpr int kDiagWarpsC = 4;
+// 32 pairs per CTA, one per lane, on NW warps (at least one per SM
+// sub-partition).  Warp 0 evaluates each step's scalar chain -- complex
+// Givens, the robust complex 1x1 solve, the three overflow decisions -- and
+// hands its results to the others through shared memory; warps 1 .. NW-1
+// update the rows of y and of the running column v, one step behind the
+// chain: in step j warp 0 first updates row j-2 itself and then evaluates
+// everything of step j-1's chain that does not need the new bounds, while
+// the other warps update rows 0 .. j-3; after a barrier warp 0 folds their
+// maxima into step j-1's third decision.  Every row sees the same operations
+// in the same order as in the unpipelined form, so the result is unchanged
+// bit for bit.  v and y live in shared memory as [row][lane] (real and
+// imaginary parts in separate arrays); when 4*32*b doubles do not fit, in a
+// global scratch region.  The bound of y(0:j-2) is the largest cabs1 at the
+// start of the step, times the step's scaling factors.
+//   NW = 8 with v/y in shared memory (two warps per sub-partition hide the
+//   FP64 latency), NW = 4 with v/y in global scratch, where the CTAs share
+//   SMs with the concurrent GEMM.
+constexpr int kDiagWarpsC = 4;       // v/y in global scratch
+constexpr int kDiagWarpsCSmem = 8;   // v/y in shared memory
 constexpr int kDiagBcastC = 12;
 
-constexpr size_t diagc_small_bytes(int b) {
-    return (size_t)(2 * (b + 1)) * sizeof(double) + (size_t)2 * kDiagWarpsC * 2 * 32 * 8 +
-           (size_t)kDiagBcastC * 32 * 8;
+// Everything but v/y: three staged columns of H, per-warp maxima [NW][2][32]
+// and the broadcast slots.
+__host__ __device__ constexpr size_t diagc_small_bytes(int b, int nw) {
+    return (size_t)(3 * (b + 1)) * sizeof(double) + (size_t)nw * 2 * 32 * 8 + (size_t)kDiagBcastC * 32 * 8;
 }
 size_t diag_c_smem_bytes(int b, bool *global_vy) {
-    const size_t small = diagc_small_bytes(b);
+    const size_t small = diagc_small_bytes(b, kDiagWarpsCSmem);
     const size_t full = small + (size_t)4 * 32 * b * sizeof(double);
     const bool fits = full <= 220 * 1024;
     if (global_vy) *global_vy = !fits;
     return fits ? full : small;
 }
 
-__global__ void __launch_bounds__(32 * kDiagWarpsC) k_diag_c(DevProblem P, int J, double *gscratch) {
+template <int NW>
+__global__ void __launch_bounds__(32 * NW) k_diag_c(DevProblem P, int J, double *gscratch) {
     extern __shared__ double sm[];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
@@ -118,10 +129,20 @@ __global__ void __launch_bounds__(32 * kDiagWarpsC) k_diag_c(DevProblem P, int J
     const int l = P.fr[J], b = P.fr[J + 1] - l;
     const bool is = P.is != 0;
     const size_t Spad = (size_t)P.Spad;
+    constexpr int NR = NW - 1;                                         // row warps
+    {
+        // A launch given less shared memory than the layout needs records a
+        // shape error and touches nothing.
+        const size_t need = diagc_small_bytes(b, NW) + (gscratch ? 0 : (size_t)4 * 32 * b * sizeof(double));
+        if (need > dynamic_smem_bytes()) {
+            if (threadIdx.x == 0) atomicOr(P.err, kErrShape);
+            return;
+        }
+    }
 
-    double *hc = sm;                                                   // [2][b+1]
-    unsigned long long *pmax = reinterpret_cast<unsigned long long *>(sm + 2 * (b + 1));
-    double *bc = sm + 2 * (b + 1) + 2 * kDiagWarpsC * 2 * 32;          // [kDiagBcastC][32]
+    double *hc = sm;                                                   // [3][b+1]
+    unsigned long long *pmax = reinterpret_cast<unsigned long long *>(sm + 3 * (b + 1));   // [NW][2][32]
+    double *bc = sm + 3 * (b + 1) + NW * 2 * 32;                       // [kDiagBcastC][32]
     double *vr_, *vi_, *yr_, *yi_;
     if (gscratch) {
         vr_ = gscratch + (size_t)blockIdx.x * 4 * 32 * b;
@@ -135,11 +156,12 @@ __global__ void __launch_bounds__(32 * kDiagWarpsC) k_diag_c(DevProblem P, int J
 #define VI(i) vi_[(size_t)(i) * 32 + lane]
 #define YR(i) yr_[(size_t)(i) * 32 + lane]
 #define YI(i) yi_[(size_t)(i) * 32 + lane]
-#define PMAX(par, w, which) pmax[(((par) * kDiagWarpsC + (w)) * 2 + (which)) * 32 + lane]
+#define PM(w, which) pmax[((w) * 2 + (which)) * 32 + lane]
 #define BC(q) bc[(q) * 32 + lane]
+#define HCOL(col) (hc + (size_t)((col) % 3) * (b + 1))
 
     // Load the crossover column and the solution tile, transposed.
-    for (int c = wid; c < 32; c += kDiagWarpsC) {
+    for (int c = wid; c < 32; c += NW) {
         const int pc = p0 + c;
         if (pc < np) {
             const double *rr = P.R + l + (size_t)(2 * pc) * P.ldr, *ri = rr + P.ldr;
@@ -167,155 +189,179 @@ __global__ void __launch_bounds__(32 * kDiagWarpsC) k_diag_c(DevProblem P, int J
     int pert = 0;
 
     const double *Hd = P.H + l + (size_t)l * P.ldh;
-    auto stage_col = [&](int col, double *dst) {                // H(l : l+col+1, l+col), warp 0
+    auto stage_col = [&](int col) {                                    // H(l : l+col+1, l+col), warp 0
         int rows = col + 2;
         if (rows > b) rows = b;
         const double *src = Hd + (size_t)col * P.ldh;
+        double *dst = HCOL(col);
         for (int i = lane; i < rows; i += 32) cp_async8(dst + i, src + i);
         cp_async_commit();
     };
-    if (wid == 0 && b >= 2) stage_col(b - 2, hc);
-    __syncthreads();
+    if (wid == 0 && b >= 2) stage_col(b - 2);
+    if (wid == 0 && b >= 3) stage_col(b - 3);
+    if (wid == 0) cp_async_wait_all();
+    __syncthreads();                                                   // tiles and columns loaded
 
+    // Largest cabs1 of y(0:b-3) and v(0:b-3) for the first step.
     {
         unsigned long long ym = 0, vm = 0;
-        for (int i = wid; i < b - 2; i += kDiagWarpsC) {
-            ym = umax64(ym, abs_bits(cabs1(cmk(YR(i), YI(i)))));
-            vm = umax64(vm, abs_bits(cabs1(cmk(VR(i), VI(i)))));
-        }
-        PMAX(0, wid, 0) = ym;
-        PMAX(0, wid, 1) = vm;
+        if (wid > 0)
+            for (int i = wid - 1; i < b - 2; i += NR) {
+                ym = umax64(ym, abs_bits(cabs1(cmk(YR(i), YI(i)))));
+                vm = umax64(vm, abs_bits(cabs1(cmk(VR(i), VI(i)))));
+            }
+        PM(wid, 0) = ym;
+        PM(wid, 1) = vm;
     }
+
+    // Chain state of warp 0.
     dcplx vcar = cmk(VR(b - 1), VI(b - 1)), ycar = cmk(YR(b - 1), YI(b - 1));
+    double c = 0.0, a1 = 1.0, a2 = 1.0, a3 = 1.0;
+    dcplx sg = cmk(0.0, 0.0), yc = sg, ys = sg, yj = sg, yjm1 = sg;
 
-    int buf = 0, par = 0;
-    for (int j = b - 1; j >= 1; --j) {
-        if (wid == 0) cp_async_wait_all();
-        __syncthreads();
-        const double *hcol = hc + buf * (b + 1);                      // column j-1 of the tile
-        if (wid == 0 && j >= 2) stage_col(j - 2, hc + (buf ^ 1) * (b + 1));
-        double c = 0.0, a1 = 1.0, a2 = 1.0, a3 = 1.0;
-        dcplx sg = cmk(0.0, 0.0), yc = sg, ys = sg, yj = sg, yjm1 = sg, hd = sg, vjm1 = sg;
-        if (wid == 0) {
-            unsigned long long ymb = 0, vmb = 0;
+    // Parts 1-2 of step jj's chain: Givens, the 1x1 solve, the y(jj-1)
+    // decision and update (solve-task.c:76-90), the next running column entry
+    // (solve-task.c:105-108).  vjm1, yjm1_in are row jj-1.
+    auto chain12 = [&](int jj, dcplx vjm1, dcplx yjm1_in) {
+        const double *hcol = HCOL(jj - 1);
+        const double hsub = hcol[jj];
+        const dcplx hd = cmk(hcol[jj - 1] - mu.re, -mu.im);
+        const dcplx vj = vcar;
+        yj = ycar;
+        yjm1 = yjm1_in;
+        cgivens(vj, hsub, c, sg);
+        if (act) {
+            P.Cr[(size_t)(l + jj) * Spad + k] = c;
+            P.Sr[(size_t)(l + jj) * Spad + k] = sg.re;
+            P.Sr[(size_t)(l + jj) * Spad + k + 1] = sg.im;
+        }
+        // y(j) := y(j) / R(j,j), R(j,j) = c v(j) - conj(sigma) H(j,j-1).
+        double phi = sc_one(is);
+        pert |= csolve_1x1(smin, c * vj.re, c * vj.im, sg.re * hsub, (-sg.im) * hsub, yj, phi, is);
+        beta = sc_combine(beta, phi, is);
+        a1 = sc_value(phi, is);
+        if (!is_one(a1)) yjm1 = cscal(a1, yjm1);
+        phi = protect_double_update(cabs1(vjm1), cabs1(yj), cabs1(hd), cabs1(yj), cabs1(yjm1), is);
+        a2 = sc_value(phi, is);
+        if (!is_one(a2)) {
+            yj = cscal(a2, yj);
+            yjm1 = cscal(a2, yjm1);
+        }
+        beta = sc_combine(beta, phi, is);
+        yc = cscal(c, yj);
+        ys = cmulc(sg, yj);
+        yjm1 = cfma(ys, hd, cfnma(yc, vjm1, yjm1));
+        const dcplx sv = cmul(sg, vjm1);
+        vcar = cmk(fma(c, hd.re, sv.re), fma(c, hd.im, sv.im));
+    };
+    // Part 3 of step jj's chain: the y(0:jj-2) decision (solve-task.c:92-100)
+    // with the maxima of rows 0 .. jj-2 folded by the row warps, then the
+    // step's scalars for the row warps, the solved entry y(jj) and y(jj-1).
+    auto chain3 = [&](int jj) {
+        unsigned long long ymb = 0, vmb = 0;
 #pragma unroll
-            for (int w = 0; w < kDiagWarpsC; ++w) {
-                ymb = umax64(ymb, PMAX(par, w, 0));
-                vmb = umax64(vmb, PMAX(par, w, 1));
-            }
-            double ymax = from_bits(ymb);
-            const double hsub = hcol[j];
-            hd = cmk(hcol[j - 1] - mu.re, -mu.im);
-            const dcplx vj = vcar;
-            vjm1 = cmk(VR(j - 1), VI(j - 1));
-            yj = ycar;
-            yjm1 = cmk(YR(j - 1), YI(j - 1));
-
-            cgivens(vj, hsub, c, sg);
-            if (act) {
-                P.Cr[(size_t)(l + j) * Spad + k] = c;
-                P.Sr[(size_t)(l + j) * Spad + k] = sg.re;
-                P.Sr[(size_t)(l + j) * Spad + k + 1] = sg.im;
-            }
-            // y(j) := y(j) / R(j,j), R(j,j) = c v(j) - conj(sigma) H(j,j-1).
-            double phi = sc_one(is);
-            pert |= csolve_1x1(smin, c * vj.re, c * vj.im, sg.re * hsub, (-sg.im) * hsub, yj, phi, is);
-            beta = sc_combine(beta, phi, is);
-            a1 = sc_value(phi, is);
-            if (!is_one(a1)) {
-                yjm1 = cscal(a1, yjm1);
-                ymax = a1 * ymax;
-            }
-            // y(j-1) (solve-task.c:84-90).
-            phi = protect_double_update(cabs1(vjm1), cabs1(yj), cabs1(hd), cabs1(yj), cabs1(yjm1), is);
-            a2 = sc_value(phi, is);
-            if (!is_one(a2)) {
-                yj = cscal(a2, yj);
-                yjm1 = cscal(a2, yjm1);
-                ymax = a2 * ymax;
-            }
-            beta = sc_combine(beta, phi, is);
+        for (int w = 1; w < NW; ++w) {
+            ymb = umax64(ymb, PM(w, 0));
+            vmb = umax64(vmb, PM(w, 1));
+        }
+        double ymax = from_bits(ymb);
+        if (!is_one(a1)) ymax = a1 * ymax;
+        if (!is_one(a2)) ymax = a2 * ymax;
+        const double phi = protect_double_update(from_bits(vmb), cabs1(yj), Hnorm, cabs1(yj), ymax, is);
+        a3 = sc_value(phi, is);
+        if (!is_one(a3)) {
+            yj = cscal(a3, yj);
+            yjm1 = cscal(a3, yjm1);
             yc = cscal(c, yj);
             ys = cmulc(sg, yj);
-            yjm1 = cfma(ys, hd, cfnma(yc, vjm1, yjm1));
-            // y(0:j-2) (solve-task.c:92-100).
-            phi = protect_double_update(from_bits(vmb), cabs1(yj), Hnorm, cabs1(yj), ymax, is);
-            a3 = sc_value(phi, is);
-            if (!is_one(a3)) {
-                yj = cscal(a3, yj);
-                yjm1 = cscal(a3, yjm1);
-                yc = cscal(c, yj);
-                ys = cmulc(sg, yj);
-            }
-            beta = sc_combine(beta, phi, is);
-            BC(0) = c;
-            BC(1) = sg.re;
-            BC(2) = sg.im;
-            BC(3) = yc.re;
-            BC(4) = yc.im;
-            BC(5) = ys.re;
-            BC(6) = ys.im;
-            BC(7) = a1;
-            BC(8) = a2;
-            BC(9) = a3;
         }
-        __syncthreads();                                              // this step's scalars visible
+        beta = sc_combine(beta, phi, is);
+        BC(0) = c;
+        BC(1) = sg.re;
+        BC(2) = sg.im;
+        BC(3) = yc.re;
+        BC(4) = yc.im;
+        BC(5) = ys.re;
+        BC(6) = ys.im;
+        BC(7) = a1;
+        BC(8) = a2;
+        BC(9) = a3;
+        YR(jj) = yj.re;
+        YI(jj) = yj.im;
+        ycar = yjm1;
+    };
+
+    if (wid == 0 && b >= 2) chain12(b - 1, cmk(VR(b - 2), VI(b - 2)), cmk(YR(b - 2), YI(b - 2)));
+    __syncthreads();                                                   // first maxima in
+    if (wid == 0 && b >= 2) chain3(b - 1);
+    __syncthreads();                                                   // step b-1's scalars visible
+
+    for (int j = b - 1; j >= 1; --j) {
+        // Step j's scalars: registers on warp 0, shared memory for the rest.
+        double sc_c = c, s1 = a1, s2 = a2, s3 = a3;
+        dcplx sc_sg = sg, sc_yc = yc, sc_ys = ys;
         if (wid != 0) {
-            c = BC(0);
-            sg = cmk(BC(1), BC(2));
-            yc = cmk(BC(3), BC(4));
-            ys = cmk(BC(5), BC(6));
-            a1 = BC(7);
-            a2 = BC(8);
-            a3 = BC(9);
+            sc_c = BC(0);
+            sc_sg = cmk(BC(1), BC(2));
+            sc_yc = cmk(BC(3), BC(4));
+            sc_ys = cmk(BC(5), BC(6));
+            s1 = BC(7);
+            s2 = BC(8);
+            s3 = BC(9);
         }
-        const bool scaled = (!is_one(a1)) || (!is_one(a2)) || (!is_one(a3));
-        if (scaled) {
-            for (int i = j + 1 + ((wid - (j + 1)) % kDiagWarpsC + kDiagWarpsC) % kDiagWarpsC; i < b;
-                 i += kDiagWarpsC) {
-                dcplx t = cmk(YR(i), YI(i));
-                if (!is_one(a1)) t = cscal(a1, t);
-                if (!is_one(a2)) t = cscal(a2, t);
-                if (!is_one(a3)) t = cscal(a3, t);
-                YR(i) = t.re;
-                YI(i) = t.im;
-            }
-        }
-        unsigned long long ymx = 0, vmx = 0;
-        const int lim = j - 1;
-        for (int i = wid; i < lim; i += kDiagWarpsC) {
+        const bool scaled = (!is_one(s1)) || (!is_one(s2)) || (!is_one(s3));
+        const double *hcol = HCOL(j - 1);
+        // Row i of step j (the unpipelined loop body).
+        auto row = [&](int i, dcplx &yo, dcplx &vo) {
             const double h = hcol[i];
-            dcplx yi = cmk(YR(i), YI(i));
-            const dcplx vi = cmk(VR(i), VI(i));
+            dcplx yv = cmk(YR(i), YI(i));
+            const dcplx vv = cmk(VR(i), VI(i));
             if (scaled) {
-                if (!is_one(a1)) yi = cscal(a1, yi);
-                if (!is_one(a2)) yi = cscal(a2, yi);
-                if (!is_one(a3)) yi = cscal(a3, yi);
+                if (!is_one(s1)) yv = cscal(s1, yv);
+                if (!is_one(s2)) yv = cscal(s2, yv);
+                if (!is_one(s3)) yv = cscal(s3, yv);
             }
-            yi = cfmar(ys, h, cfnma(yc, vi, yi));
-            const dcplx sv = cmul(sg, vi);
-            const dcplx vn = cmk(fma(c, h, sv.re), sv.im);
-            YR(i) = yi.re;
-            YI(i) = yi.im;
-            VR(i) = vn.re;
-            VI(i) = vn.im;
-            if (i < lim - 1) {
-                ymx = umax64(ymx, abs_bits(cabs1(yi)));
-                vmx = umax64(vmx, abs_bits(cabs1(vn)));
-            }
-        }
-        PMAX(par ^ 1, wid, 0) = ymx;
-        PMAX(par ^ 1, wid, 1) = vmx;
+            yo = cfmar(sc_ys, h, cfnma(sc_yc, vv, yv));
+            const dcplx sv = cmul(sc_sg, vv);
+            vo = cmk(fma(sc_c, h, sv.re), sv.im);
+            YR(i) = yo.re;
+            YI(i) = yo.im;
+            VR(i) = vo.re;
+            VI(i) = vo.im;
+        };
         if (wid == 0) {
-            YR(j) = yj.re;
-            YI(j) = yj.im;
-            // Next annihilation column entry (solve-task.c:105-108) and y(j-1).
-            const dcplx sv = cmul(sg, vjm1);
-            vcar = cmk(fma(c, hd.re, sv.re), fma(c, hd.im, sv.im));
-            ycar = yjm1;
+            if (j >= 2) {
+                dcplx yn, vn;
+                row(j - 2, yn, vn);                                    // enters step j-1's chain
+                cp_async_wait_all();                                   // column j-2, staged last step
+                __syncwarp();                                          // ... by all lanes of warp 0
+                chain12(j - 1, vn, yn);
+            }
+            if (j >= 3) stage_col(j - 3);                              // for step j-2's chain
+        } else {
+            if (scaled) {
+                for (int i = j + 1 + ((wid - 1 - (j + 1)) % NR + NR) % NR; i < b; i += NR) {
+                    dcplx t = cmk(YR(i), YI(i));
+                    if (!is_one(s1)) t = cscal(s1, t);
+                    if (!is_one(s2)) t = cscal(s2, t);
+                    if (!is_one(s3)) t = cscal(s3, t);
+                    YR(i) = t.re;
+                    YI(i) = t.im;
+                }
+            }
+            unsigned long long ymx = 0, vmx = 0;
+            for (int i = wid - 1; i < j - 2; i += NR) {                // rows 0 .. j-3
+                dcplx yo, vo;
+                row(i, yo, vo);
+                ymx = umax64(ymx, abs_bits(cabs1(yo)));
+                vmx = umax64(vmx, abs_bits(cabs1(vo)));
+            }
+            PM(wid, 0) = ymx;
+            PM(wid, 1) = vmx;
         }
-        buf ^= 1;
-        par ^= 1;
+        __syncthreads();                                               // rows of step j done, maxima in
+        if (wid == 0 && j >= 2) chain3(j - 1);
+        __syncthreads();                                               // step j-1's scalars visible
     }
 
     double c0 = 1.0;
@@ -358,7 +404,7 @@ __global__ void __launch_bounds__(32 * kDiagWarpsC) k_diag_c(DevProblem P, int J
             a = BC(3);
         }
         if (!is_one(a))
-            for (int i = 1 + ((wid - 1) % kDiagWarpsC + kDiagWarpsC) % kDiagWarpsC; i < b; i += kDiagWarpsC) {
+            for (int i = 1 + ((wid - 1) % NW + NW) % NW; i < b; i += NW) {
                 YR(i) = a * YR(i);
                 YI(i) = a * YI(i);
             }
@@ -369,7 +415,7 @@ __global__ void __launch_bounds__(32 * kDiagWarpsC) k_diag_c(DevProblem P, int J
     }
     __syncthreads();
 
-    for (int c = wid; c < 32; c += kDiagWarpsC) {
+    for (int c = wid; c < 32; c += NW) {
         const int pc = p0 + c;
         if (pc < np) {
             double *xr = P.X + l + (size_t)(2 * pc) * P.ldx, *xi = xr + P.ldx;
@@ -428,29 +474,33 @@ __global__ void __launch_bounds__(32 * kDiagWarpsC) k_diag_c(DevProblem P, int J
 #undef VI
 #undef YR
 #undef YI
-#undef PMAX
+#undef PM
+#undef HCOL
 #undef BC
 }
 
-// The dynamic shared-memory limit of k_diag_c only ever grows.
+// The dynamic shared-memory limit of each k_diag_c form only ever grows.
+template <int NW>
 cudaError_t diag_c_smem_attr(size_t smem) {
     static size_t configured = 0;
-    return raise_smem_limit((const void *)k_diag_c, &configured, smem);
+    return raise_smem_limit((const void *)k_diag_c<NW>, &configured, smem);
 }
 
 cudaError_t launch_diag_c(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st) {
     bool gvy = false;
-    size_t smem = diag_c_smem_bytes(b, &gvy);
+    const size_t smem = diag_c_smem_bytes(b, &gvy);
     if (gvy && !gscratch) return cudaErrorInvalidValue;
+    const int grid = (P.S / 2 + 31) / 32;
     if (gscratch) {
-        gvy = true;
-        smem = diagc_small_bytes(b);
-    }
-    {
-        cudaError_t e = diag_c_smem_attr(smem);
+        const size_t small = diagc_small_bytes(b, kDiagWarpsC);
+        const cudaError_t e = diag_c_smem_attr<kDiagWarpsC>(small);
         if (e != cudaSuccess) return e;
+        k_diag_c<kDiagWarpsC><<<grid, 32 * kDiagWarpsC, small, st>>>(P, J, gscratch);
+    } else {
+        const cudaError_t e = diag_c_smem_attr<kDiagWarpsCSmem>(smem);
+        if (e != cudaSuccess) return e;
+        k_diag_c<kDiagWarpsCSmem><<<grid, 32 * kDiagWarpsCSmem, smem, st>>>(P, J, nullptr);
     }
-    k_diag_c<<<(P.S / 2 + 31) / 32, 32 * kDiagWarpsC, smem, st>>>(P, J, gvy ? gscratch : nullptr);
     return cudaGetLastError();
 }
 
@@ -458,9 +508,10 @@ int diag_c_ctas_per_sm(int b) {
     bool gvy = false;
     const size_t smem = diag_c_smem_bytes(b, &gvy);
     if (gvy) return 0;
-    if (diag_c_smem_attr(smem) != cudaSuccess) return 0;
+    if (diag_c_smem_attr<kDiagWarpsCSmem>(smem) != cudaSuccess) return 0;
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_diag_c, 32 * kDiagWarpsC, smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_diag_c<kDiagWarpsCSmem>, 32 * kDiagWarpsCSmem,
+                                                      smem) != cudaSuccess)
         return 0;
     return nb;
 }

@@ -682,10 +682,9 @@ __device__ __forceinline__ void diag_body_pipe(const DevProblem &P, int J, int b
         ycar = yjm1;
     };
 
-    if (wid == 0 && b >= 2) {
-        chain12(b - 1, V(b - 2), Y(b - 2));
-        chain3(b - 1);
-    }
+    if (wid == 0 && b >= 2) chain12(b - 1, V(b - 2), Y(b - 2));
+    __syncthreads();                                                          // first maxima in
+    if (wid == 0 && b >= 2) chain3(b - 1);
     __syncthreads();                                                          // step b-1's scalars visible
 
     for (int j = b - 1; j >= 1; --j) {
