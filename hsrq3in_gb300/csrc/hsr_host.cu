@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -546,6 +547,48 @@ int check_args(int n, int ldH, int nrhs, int tlsz, int ldvr, const void *H, cons
     return HSR_OK;
 }
 
+// ----------------------------------------------------- caller's host blocks
+// A column block moved between a caller's host buffer and device memory by SM
+// loads and stores: dst(i, j) = src(i, j) for i < rows, j < cols, both
+// column-major.  Used when the host buffer is page-locked and mapped into the
+// device's address space; after long solves the copy engines were measured
+// running far below their idle rate on this path, the SMs were not.
+template <typename V>
+__global__ void __launch_bounds__(256) k_copy_cols(V *__restrict__ dst, long long ldd, const V *__restrict__ src,
+                                                   long long lds, int rows, int cols) {
+    for (int j = blockIdx.x; j < cols; j += gridDim.x) {
+        const V *s = src + (size_t)j * lds;
+        V *d = dst + (size_t)j * ldd;
+        for (int i = threadIdx.x; i < rows; i += blockDim.x) d[i] = s[i];
+    }
+}
+
+// Device address of a page-locked host buffer mapped into the device's
+// address space, or null (pageable or unmapped memory keeps the copy engines).
+void *mapped_view(const void *host) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+cudaError_t copy_cols(double *dst, long long ldd, const double *src, long long lds, int rows, int cols,
+                      cudaStream_t st) {
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    const int grid = cols < 1216 ? cols : 1216;
+    const bool wide = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) % 16 == 0) &&
+                      rows % 2 == 0 && ldd % 2 == 0 && lds % 2 == 0;
+    ++g_launches;
+    if (wide)
+        k_copy_cols<double2><<<grid, 256, 0, st>>>(reinterpret_cast<double2 *>(dst), ldd / 2,
+                                                    reinterpret_cast<const double2 *>(src), lds / 2, rows / 2, cols);
+    else
+        k_copy_cols<double><<<grid, 256, 0, st>>>(dst, ldd, src, lds, rows, cols);
+    return cudaGetLastError();
+}
+
 int host_call(int n, const double *H, int ldH, int nrhs, double *wr, int tlsz, int rhs_tlsz, double *vr,
               int ldvr, const hsr_options *opt, hsr_column_info *info) {
     g_launches = 0;
@@ -565,7 +608,9 @@ int host_call(int n, const double *H, int ldH, int nrhs, double *wr, int tlsz, i
     HSR_CK(w.X.ensure((size_t)ldx * nrhs * 8));
     HSR_CK(w.wr.ensure((size_t)nrhs * 8));
     g_timing.begin(kcH2D, st);
-    if (ldh == ldH)
+    if (const void *Hm = mapped_view(H))
+        HSR_CK(copy_cols(w.H.as<double>(), ldh, static_cast<const double *>(Hm), ldH, n, n, st));
+    else if (ldh == ldH)
         HSR_CK(cudaMemcpyAsync(w.H.p, H, ((size_t)ldH * (n - 1) + n) * 8, cudaMemcpyHostToDevice, st));
     else
         HSR_CK(cudaMemcpy2DAsync(w.H.p, ldh * 8, H, (size_t)ldH * 8, (size_t)n * 8, n, cudaMemcpyHostToDevice, st));
@@ -585,7 +630,9 @@ int host_call(int n, const double *H, int ldH, int nrhs, double *wr, int tlsz, i
                       want && info->norm ? &hn : nullptr, want && info->tile_scales ? &hts : nullptr);
     if (rc < 0) return rc;
     g_timing.begin(kcD2H, st);
-    if (ldvr == n)   // no padding rows in the caller's block: one contiguous copy
+    if (void *Xm = mapped_view(vr))   // the caller's padding rows stay untouched
+        HSR_CK(copy_cols(static_cast<double *>(Xm), ldvr, w.X.as<double>(), ldx, n, nrhs, st));
+    else if (ldvr == n)   // no padding rows in the caller's block: one contiguous copy
         HSR_CK(cudaMemcpyAsync(vr, w.X.p, (size_t)n * nrhs * 8, cudaMemcpyDeviceToHost, st));
     else             // leave the caller's padding rows untouched
         HSR_CK(cudaMemcpy2DAsync(vr, (size_t)ldvr * 8, w.X.p, ldx * 8, (size_t)n * 8, nrhs,
@@ -898,7 +945,9 @@ int host_call_c(int n, const double *H, int ldH, int np, const double *wr, const
         wc[2 * p + 1] = wi[p];
     }
     g_timing.begin(kcH2D, st);
-    if (ldh == ldH)
+    if (const void *Hm = mapped_view(H))
+        HSR_CK(copy_cols(w.H.as<double>(), ldh, static_cast<const double *>(Hm), ldH, n, n, st));
+    else if (ldh == ldH)
         HSR_CK(cudaMemcpyAsync(w.H.p, H, ((size_t)ldH * (n - 1) + n) * 8, cudaMemcpyHostToDevice, st));
     else
         HSR_CK(cudaMemcpy2DAsync(w.H.p, ldh * 8, H, (size_t)ldH * 8, (size_t)n * 8, n, cudaMemcpyHostToDevice, st));
@@ -914,7 +963,9 @@ int host_call_c(int n, const double *H, int ldH, int np, const double *wr, const
                            want && info->norm ? &hn : nullptr);
     if (rc < 0) return rc;
     g_timing.begin(kcD2H, st);
-    if (ldvr == n)
+    if (void *Xm = mapped_view(vr))
+        HSR_CK(copy_cols(static_cast<double *>(Xm), ldvr, w.X.as<double>(), ldx, n, 2 * np, st));
+    else if (ldvr == n)
         HSR_CK(cudaMemcpyAsync(vr, w.X.p, (size_t)n * 2 * np * 8, cudaMemcpyDeviceToHost, st));
     else
         HSR_CK(cudaMemcpy2DAsync(vr, (size_t)ldvr * 8, w.X.p, ldx * 8, (size_t)n * 8, 2 * np,

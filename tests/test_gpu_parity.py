@@ -236,6 +236,44 @@ def test_leading_dimensions_through_c_abi(gpu_lib, extra_h, extra_v):
     assert np.array_equal(vc[:n], cref["vr"]) and np.all(vc[n:] == -3.25)
 
 
+@pytest.mark.parametrize("extra_h,extra_v", [(0, 0), (1, 3), (2, 2)])
+def test_pinned_host_buffers_through_c_abi(gpu_lib, extra_h, extra_v):
+    """With page-locked host buffers the drop-in calls move H in and X out by
+    SM copies through the mapped pointers (paired-double and single-double
+    forms, depending on the pitches); the result equals the pageable call bit
+    for bit and the caller's padding rows of vr stay untouched."""
+    import ctypes as C
+    import torch
+    from hsrq3in_gb300 import _lib
+    n, tlsz, m = 98, 24, 20
+    H, lam = G.real_spectrum(n, 81)
+    wr = np.ascontiguousarray(G.perturbed_shifts(lam, 82)[:m])
+    ldh, ldv = n + extra_h, n + extra_v
+    ref = _device(H, wr, tlsz)
+    Hp = torch.full((n, ldh), 7.0, dtype=torch.float64).pin_memory()
+    Hp.numpy()[:, :n] = H.T
+    vr = torch.full((m, ldv), -3.25, dtype=torch.float64).pin_memory()
+    w = torch.from_numpy(wr.copy()).pin_memory()
+    assert Hp.is_pinned() and vr.is_pinned()
+    gpu_lib.tiled_inverse_iteration(n, Hp.data_ptr(), ldh, m, w.data_ptr(), tlsz, 16, vr.data_ptr(), ldv)
+    assert gpu_lib.hsr_last_status() == 0
+    got = vr.numpy()
+    assert np.array_equal(got[:, :n].T, ref["vr"]) and np.array_equal(w.numpy(), ref["wr"])
+    assert np.all(got[:, n:] == -3.25)
+    Hc, pairs, _ = G.complex_spectrum(n, 83)
+    Hcp = torch.full((n, ldh), 7.0, dtype=torch.float64).pin_memory()
+    Hcp.numpy()[:, :n] = Hc.T
+    cref = hsr_cplx(Hc, pairs[:10], tlsz)
+    vc = torch.full((20, ldv), -3.25, dtype=torch.float64).pin_memory()
+    a, b = np.ascontiguousarray(pairs[:10].real), np.ascontiguousarray(pairs[:10].imag)
+    opt = _lib.Options(0, 0, -1, 0.0)
+    rc = gpu_lib.hsr_inverse_iteration_cplx_ex(n, Hcp.data_ptr(), ldh, 10, a.ctypes.data, b.ctypes.data, tlsz, 16,
+                                               vc.data_ptr(), ldv, C.byref(opt), None)
+    assert rc == 0
+    gc = vc.numpy()
+    assert np.array_equal(gc[:, :n].T, cref["vr"]) and np.all(gc[:, n:] == -3.25)
+
+
 def hsr_cplx(H, mu, tlsz):
     import hsrq3in_gb300 as hsr
     return hsr.inverse_iteration_cplx(H, mu, tlsz, 16)
