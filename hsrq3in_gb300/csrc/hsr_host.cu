@@ -563,8 +563,11 @@ __global__ void __launch_bounds__(256) k_copy_cols(V *__restrict__ dst, long lon
     }
 }
 
-// Device address of a page-locked host buffer mapped into the device's
-// address space, or null (pageable or unmapped memory keeps the copy engines).
+// Device address of a page-locked host buffer mapped into the current
+// device's address space, or null: cudaPointerAttributes::devicePointer is
+// the address the current device may dereference, null where there is none
+// (pageable memory, or a block pinned for another device without the
+// portable flag), and those buffers keep the copy engines.
 void *mapped_view(const void *host) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
