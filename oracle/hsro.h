@@ -100,7 +100,7 @@ int hsro_csolve_1x1(double smin, double tr, double ti, double lr, double li,
 
 /* Number of OpenMP threads the oracle may use (0 = runtime default).        */
 void hsro_set_threads(int nthreads);
-/* Which arithmetic mode this build implements: 0 ref, 1 fma.                */
+/* Arithmetic mode the library was compiled for: 0 ref, 1 fma.              */
 int  hsro_mode(void);
 
 #ifdef __cplusplus
