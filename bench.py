@@ -3,7 +3,7 @@
 
 Workload (the plain large configuration): one real upper-Hessenberg H of
 order n = 10000 from the seeded real-spectrum generator, all 10000 eigenvalues
-as shifts with relative 1e-12 noise, tlsz = 200.  One step = one complete
+as shifts with relative 1e-12 noise, tlsz = 160.  One step = one complete
 solve (tile sweep, reconciliation, back-transform, normalisation, convergence
 check) of all shifts.
 
@@ -12,7 +12,8 @@ check) of all shifts.
   stream.  H (800 MB) is larger than L2, so no flush is needed between steps.
 * e2e: the same metric through the drop-in C entry point
   tiled_inverse_iteration with pinned host buffers: H and the shifts copied
-  in, the eigenvectors and shifts copied out, every step.
+  in, the eigenvectors and shifts copied out, every step (the library moves
+  the page-locked blocks by SM copies through their mapped pointers).
 * roofline: the dominant kernel (the crossover/update GEMM) against the FP64
   DFMA peak measured in the same run; traffic from the committed ncu capture.
 * cpu_baseline: the C restatement of the reference (oracle port, OpenMP over
