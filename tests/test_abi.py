@@ -113,3 +113,40 @@ def test_mixed_layout_errors_without_gpu(lib):
 
 def test_version_string(lib):
     assert b"sm_103a" in lib.hsr_version()
+
+
+def test_header_compiles_as_c_and_links(lib, tmp_path):
+    """A C99 caller: the header beside the reference's own declaration of the
+    entry point (inverse_iteration.h:19-22, restrict-qualified pointers)
+    compiles with -Wall -Wextra -pedantic -Werror, so the two declarations
+    are compatible; the address of every declared function resolves against
+    the library at link time; the program then runs a call that needs no GPU."""
+    from hsrq3in_gb300 import _lib
+    names = declared_functions()
+    prog = tmp_path / "caller.c"
+    prog.write_text("\n".join([
+        "#include <stdio.h>",
+        "#include \"hsrq3in_gb300.h\"",
+        "void tiled_inverse_iteration(int n, const double *restrict H, int ldH, int nrhs,",
+        "                             double *restrict wr, int tlsz, int rhs_tlsz,",
+        "                             double *restrict vr, int ldvr);",
+        "typedef void (*any_fn)(void);",
+        "int main(void) {",
+        "    any_fn fns[] = {" + ", ".join("(any_fn)%s" % nm for nm in names) + "};",
+        "    int resolved = 0;",
+        "    for (size_t i = 0; i < sizeof fns / sizeof fns[0]; ++i) resolved += fns[i] != 0;",
+        "    printf(\"%d %s\\n\", resolved, hsr_version());",
+        "    return 0;",
+        "}", ""]))
+    libdir = os.path.dirname(_lib.lib_path())
+    exe = tmp_path / "caller"
+    cc = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                         "-I", os.path.join(ROOT, "include"), str(prog), "-L", libdir, "-lhsrq3in_gb300",
+                         "-Wl,-rpath," + libdir, "-o", str(exe)], capture_output=True, text=True)
+    assert cc.returncode == 0, cc.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert run.returncode == 0, run.stderr
+    count, version = run.stdout.split(" ", 1)
+    assert int(count) == len(names)
+    assert version.strip() == lib.hsr_version().decode()
+
