@@ -63,8 +63,10 @@ def test_dlartg_matches_lapack_bitwise():
     assert bad == 0
 
 
-@pytest.mark.parametrize("variant", ["ref", "fma"])
+@pytest.mark.parametrize("variant", ["ref", "fma", "ref_fast"])
 def test_residual_bound(variant):
+    """Every variant, including ref_fast (the build the CPU baseline times),
+    solves to the residual bound."""
     n = 300
     H, lam = G.real_spectrum(n, 11)
     wr = G.perturbed_shifts(lam, 12)
@@ -74,13 +76,16 @@ def test_residual_bound(variant):
 
 
 def test_angle_well_conditioned():
-    """ref vs fma arithmetic on the well-conditioned companion generator."""
+    """ref vs fma and ref_fast arithmetic on the well-conditioned companion
+    generator."""
     n = 200
     H, lam = G.well_conditioned(n, 13)
     a = O.oracle_inverse_iteration(H, lam, 40, 16, variant="ref")
     b = O.oracle_inverse_iteration(H, lam, 40, 16, variant="fma")
-    assert np.all(a["status"] == 1)
+    c = O.oracle_inverse_iteration(H, lam, 40, 16, variant="ref_fast")
+    assert np.all(a["status"] == 1) and np.all(c["status"] == 1)
     assert O.eigvec_angles(a["vr"], b["vr"]).max() <= 1e-10
+    assert O.eigvec_angles(a["vr"], c["vr"]).max() <= 1e-10
 
 
 def test_angle_filtered_by_sensitivity():
