@@ -45,7 +45,7 @@ METRIC = "FP64 eigenvectors/s at n=10k"
 UNIT = "eigenvectors/s"
 # DRAM bytes per algorithmic FMA of k_gemm, from one ncu capture of the
 # n=4096, S=4096, tlsz=200 case (stage 10 rest launch: 183.61 MB of
-# dram__bytes_read+write for 1696*399*4096 FMAs; profiles/k_gemm_n4096.md).
+# dram__bytes_read+write for 1696*399*4096 FMAs).
 # Traffic and FMAs both grow with rows x shifts, so the ratio scales the
 # capture to the launches of this workload.
 GEMM_DRAM_BYTES_PER_FMA = (127.772928e6 + 54.166528e6) / (1696 * 399 * 4096)

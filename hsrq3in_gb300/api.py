@@ -330,10 +330,16 @@ class Server:
         pinned for copy/compute overlap.  Returns (latencies_s, statuses, stats)."""
         n = len(requests)
         arr = (_lib.Request * max(n, 1))()
+        def ld(a):
+            # column-major view: unit row stride, column stride = leading dimension
+            if a.strides[0] != 8:
+                raise ValueError("request blocks must be column-major float64 views")
+            return a.strides[1] // 8 if a.shape[1] > 1 else a.shape[0]
+
         for i, r in enumerate(requests):
             H, wr, vr = r["H"], r["wr"], r["vr"]
-            arr[i] = _lib.Request(H.shape[0], H.ctypes.data, H.shape[0] if H.flags.f_contiguous else H.strides[1] // 8,
-                                  wr.shape[0], wr.ctypes.data, vr.ctypes.data, vr.shape[0], float(r["arrival_s"]))
+            arr[i] = _lib.Request(H.shape[0], H.ctypes.data, ld(H), wr.shape[0], wr.ctypes.data, vr.ctypes.data,
+                                  ld(vr), float(r["arrival_s"]))
         lat = (C.c_double * max(n, 1))()
         st = (C.c_int * max(n, 1))()
         stats = _lib.ServerStats()

@@ -824,6 +824,24 @@ extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, dou
     }
     if (cudaMallocHost(&h_status.p, sizeof(int) * std::max<size_t>(total_cols, 1)) != cudaSuccess)
         return HSR_ERR_NOMEM;
+    // A failed CUDA call ends the replay: the work already enqueued is
+    // waited for, every request that has not completed reports
+    // HSR_ERR_CUDA, and so does the call.
+    std::vector<char> finished(nreq, 0);
+    auto fail = [&](cudaError_t e) -> int {
+        (void)cudaStreamSynchronize(st);
+        (void)cudaStreamSynchronize(s->side);
+        for (auto &a : active)
+            if (a.done) cudaEventDestroy(a.done);
+        for (int i = 0; i < nreq; ++i)
+            if (!finished[i] && status_out) status_out[i] = HSR_ERR_CUDA;
+        return record_status(HSR_ERR_CUDA, e);
+    };
+#define SRV_CK(x)                              \
+    do {                                       \
+        const cudaError_t e_ = (x);            \
+        if (e_ != cudaSuccess) return fail(e_); \
+    } while (0)
 
     while (completed < nreq) {
         const double now = elapsed();
@@ -832,7 +850,9 @@ extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, dou
         // Retire requests whose results reached the host.
         for (size_t i = 0; i < active.size();) {
             ActiveReq &a = active[i];
-            if (a.retiring && cudaEventQuery(a.done) == cudaSuccess) {
+            const cudaError_t q = a.retiring ? cudaEventQuery(a.done) : cudaErrorNotReady;
+            if (q != cudaSuccess && q != cudaErrorNotReady) return fail(q);
+            if (q == cudaSuccess) {
                 const hsr_request &r = reqs[a.req];
                 bool all = true;
                 for (int k = 0; k < r.nrhs; ++k) all = all && a.h_status[k];
@@ -847,7 +867,9 @@ extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, dou
                 }
                 if (status_out) status_out[a.req] = rc;
                 if (latency) latency[a.req] = elapsed() - r.arrival_s;
+                finished[a.req] = 1;
                 cudaEventDestroy(a.done);
+                a.done = nullptr;
                 s->alloc.release(a.off, a.bytes);
                 s->free_slots.push_back(a.slot);
                 active[i] = std::move(active.back());
@@ -867,6 +889,7 @@ extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, dou
             if (r.nrhs == 0) {
                 queue.pop_front();
                 if (latency) latency[ri] = elapsed() - r.arrival_s;
+                finished[ri] = 1;
                 ++completed;
                 continue;
             }
@@ -880,6 +903,7 @@ extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, dou
                 queue.pop_front();
                 if (status_out) status_out[ri] = HSR_ERR_NOMEM;
                 result = HSR_ERR_NOMEM;
+                finished[ri] = 1;
                 ++completed;
                 continue;
             }
@@ -893,19 +917,28 @@ extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, dou
             double *dX = reinterpret_cast<double *>(reinterpret_cast<char *>(dwr) + up((size_t)r.nrhs * 8, 256));
             partition_rows(r.n, a.L.T, b, a.fr);
             a.h_status = h_status.p + status_at[ri];
-            cudaMemcpy2DAsync(dH, a.ldh * 8, r.H, (size_t)r.ldH * 8, (size_t)r.n * 8, r.n, cudaMemcpyHostToDevice, st);
-            cudaMemcpyAsync(dwr, r.wr, (size_t)r.nrhs * 8, cudaMemcpyHostToDevice, st);
-            cudaMemcpyAsync(base + a.L.fr, a.fr.data(), (a.L.T + 1) * sizeof(int), cudaMemcpyHostToDevice, st);
-            cudaMemsetAsync(base, 0, a.L.zero_bytes, st);
+            // A page-locked request block moves by SM loads through its mapped
+            // pointer, like the drop-in call's; other buffers by copy engine.
+            if (const void *Hm = mapped_view(r.H)) {
+                ++launches;
+                SRV_CK(copy_cols(dH, a.ldh, static_cast<const double *>(Hm), r.ldH, r.n, r.n, st));
+            } else {
+                SRV_CK(cudaMemcpy2DAsync(dH, a.ldh * 8, r.H, (size_t)r.ldH * 8, (size_t)r.n * 8, r.n,
+                                         cudaMemcpyHostToDevice, st));
+            }
+            SRV_CK(cudaMemcpyAsync(dwr, r.wr, (size_t)r.nrhs * 8, cudaMemcpyHostToDevice, st));
+            SRV_CK(cudaMemcpyAsync(base + a.L.fr, a.fr.data(), (a.L.T + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                                   st));
+            SRV_CK(cudaMemsetAsync(base, 0, a.L.zero_bytes, st));
             const int d0 = desc(a.slot, 0);
             for (int par = 0; par < 2; ++par) {
                 s->h_prob_stage[d0 + par] = make_problem(a.L, base, dH, a.ldh, dwr, dX, a.ldx, s->is, s->d_err, par);
                 make_maps(&s->h_map_stage[3 * (size_t)(d0 + par)], a.L, dH, a.ldh, base, par);
             }
-            cudaMemcpyAsync(s->d_probs + d0, s->h_prob_stage + d0, 2 * sizeof(DevProblem), cudaMemcpyHostToDevice,
-                            st);
-            cudaMemcpyAsync(s->d_maps + 3 * (size_t)d0, s->h_map_stage + 3 * (size_t)d0, 6 * sizeof(CUtensorMap),
-                            cudaMemcpyHostToDevice, st);
+            SRV_CK(cudaMemcpyAsync(s->d_probs + d0, s->h_prob_stage + d0, 2 * sizeof(DevProblem),
+                                   cudaMemcpyHostToDevice, st));
+            SRV_CK(cudaMemcpyAsync(s->d_maps + 3 * (size_t)d0, s->h_map_stage + 3 * (size_t)d0,
+                                   6 * sizeof(CUtensorMap), cudaMemcpyHostToDevice, st));
             add_setup(tl, a.slot, a.L);
             flops += 2.0 * (double)r.n * r.n * r.nrhs;
             a.stage = a.L.T - 1;
@@ -938,7 +971,7 @@ extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, dou
         // The item buffer of this parity was last used two ticks ago.
         if (tick_used[parity]) {
             const double w0 = elapsed();
-            cudaEventSynchronize(s->tick_ev[parity]);
+            SRV_CK(cudaEventSynchronize(s->tick_ev[parity]));
             wait_s += elapsed() - w0;
         }
         if (count > s->items_cap[parity]) {
@@ -946,15 +979,19 @@ extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, dou
             if (s->h_items[parity]) cudaFreeHost(s->h_items[parity]);
             s->items_cap[parity] = std::max<size_t>(count * 2, 4096);
             if (cudaMalloc(&s->d_items[parity], sizeof(BatchItem) * s->items_cap[parity]) != cudaSuccess ||
-                cudaMallocHost(&s->h_items[parity], sizeof(BatchItem) * s->items_cap[parity]) != cudaSuccess)
-                return HSR_ERR_NOMEM;
+                cudaMallocHost(&s->h_items[parity], sizeof(BatchItem) * s->items_cap[parity]) != cudaSuccess) {
+                s->d_items[parity] = nullptr;
+                s->h_items[parity] = nullptr;
+                s->items_cap[parity] = 0;
+                (void)fail(cudaErrorMemoryAllocation);
+                return record_status(HSR_ERR_NOMEM, cudaSuccess);
+            }
         }
         pack_tick(tl, s->h_items[parity], 0, spans);
-        cudaMemcpyAsync(s->d_items[parity], s->h_items[parity], sizeof(BatchItem) * count, cudaMemcpyHostToDevice,
-                        st);
-        if (launch_tick(spans, s->d_probs, s->d_items[parity], b, s->d_maps, st, s->side, s->fork, s->join, launches,
-                        tm) != cudaSuccess)
-            return HSR_ERR_CUDA;
+        SRV_CK(cudaMemcpyAsync(s->d_items[parity], s->h_items[parity], sizeof(BatchItem) * count,
+                               cudaMemcpyHostToDevice, st));
+        SRV_CK(launch_tick(spans, s->d_probs, s->d_items[parity], b, s->d_maps, st, s->side, s->fork, s->join,
+                           launches, tm));
         // Requests that finished this tick: copy results to the host.
         for (auto &a : active) {
             if (a.retiring) continue;
@@ -963,24 +1000,31 @@ extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, dou
                 char *base = s->pool + a.off;
                 double *dwr = reinterpret_cast<double *>(base + a.L.total + up((size_t)a.ldh * r.n * 8, 256));
                 double *dX = reinterpret_cast<double *>(reinterpret_cast<char *>(dwr) + up((size_t)r.nrhs * 8, 256));
-                cudaMemcpy2DAsync(r.vr, (size_t)r.ldvr * 8, dX, a.ldx * 8, (size_t)r.n * 8, r.nrhs,
-                                  cudaMemcpyDeviceToHost, st);
-                cudaMemcpyAsync(a.h_status, base + a.L.status, r.nrhs * sizeof(int), cudaMemcpyDeviceToHost, st);
-                cudaEventCreateWithFlags(&a.done, cudaEventDisableTiming);
-                cudaEventRecord(a.done, st);
+                if (void *Xm = mapped_view(r.vr)) {   // the caller's padding rows stay untouched
+                    ++launches;
+                    SRV_CK(copy_cols(static_cast<double *>(Xm), r.ldvr, dX, a.ldx, r.n, r.nrhs, st));
+                } else {
+                    SRV_CK(cudaMemcpy2DAsync(r.vr, (size_t)r.ldvr * 8, dX, a.ldx * 8, (size_t)r.n * 8, r.nrhs,
+                                             cudaMemcpyDeviceToHost, st));
+                }
+                SRV_CK(cudaMemcpyAsync(a.h_status, base + a.L.status, r.nrhs * sizeof(int), cudaMemcpyDeviceToHost,
+                                       st));
+                SRV_CK(cudaEventCreateWithFlags(&a.done, cudaEventDisableTiming));
+                SRV_CK(cudaEventRecord(a.done, st));
                 a.retiring = true;
             } else {
                 --a.stage;
             }
         }
-        cudaEventRecord(s->tick_ev[parity], st);
+        SRV_CK(cudaEventRecord(s->tick_ev[parity], st));
         tick_used[parity] = true;
         parity ^= 1;
         ++ticks;
     }
-    cudaStreamSynchronize(st);
+    SRV_CK(cudaStreamSynchronize(st));
     int errw = 0;
-    cudaMemcpy(&errw, s->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    SRV_CK(cudaMemcpy(&errw, s->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+#undef SRV_CK
     if (errw) result = HSR_ERR_DEVICE;
     if (stats) {
         stats->wall_s = elapsed();
@@ -993,5 +1037,5 @@ extern "C" int hsr_server_replay(hsr_server *s, int nreq, hsr_request *reqs, dou
         for (int ph = 0; ph < phCount; ++ph) stats->phase_ms[ph] = 0.0;
         timer.add_to(stats->phase_ms);
     }
-    return result;
+    return record_status(result, cudaSuccess);
 }

@@ -103,16 +103,18 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+// Looked up once; the initialiser of a function-local static runs exactly
+// once even when several host threads make their first call together.
 EncodeTiledFn encode_fn() {
-    static EncodeTiledFn fn = nullptr;
-    if (!fn) {
+    static const EncodeTiledFn fn = []() -> EncodeTiledFn {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiledFn>(p);
-    }
+            return reinterpret_cast<EncodeTiledFn>(p);
+        return nullptr;
+    }();
     return fn;
 }
 
@@ -547,6 +549,8 @@ int check_args(int n, int ldH, int nrhs, int tlsz, int ldvr, const void *H, cons
     return HSR_OK;
 }
 
+}  // namespace
+
 // ----------------------------------------------------- caller's host blocks
 // A column block moved between a caller's host buffer and device memory by SM
 // loads and stores: dst(i, j) = src(i, j) for i < rows, j < cols, both
@@ -591,6 +595,8 @@ cudaError_t copy_cols(double *dst, long long ldd, const double *src, long long l
         k_copy_cols<double><<<grid, 256, 0, st>>>(dst, ldd, src, lds, rows, cols);
     return cudaGetLastError();
 }
+
+namespace {
 
 int host_call(int n, const double *H, int ldH, int nrhs, double *wr, int tlsz, int rhs_tlsz, double *vr,
               int ldvr, const hsr_options *opt, hsr_column_info *info) {
@@ -1231,3 +1237,8 @@ const char *hsr_version(void) { return "hsrq3in_gb300 0.1 (sm_103a, FP64 DFMA)";
 }  // extern "C"
 
 bool hsr::kernel_timing_enabled() { return g_timing.enabled; }
+
+int hsr::record_status(int status, cudaError_t cuda_error) {
+    if (cuda_error != cudaSuccess) last_cuda_error() = cuda_error;
+    return g_last_status = status;
+}

@@ -158,7 +158,7 @@ cudaError_t launch_init(const DevProblem &P, int mode, const double *eps3_dev, i
 // y(0:j-2) and of the running column) by row, one step behind the chain
 // (diag_body_pipe).  Where many CTAs share the GPU (the batched engine) one
 // warp per CTA does the same work with the fewest FP64 instructions
-// (diag_body<1>).  v (running column) and y (solution tile) live in shared
+// (diag_body_1w).  v (running column) and y (solution tile) live in shared
 // memory as [row][lane]; columns of H are staged ahead with cp.async and
 // read as broadcasts.  Per-warp maxima of |y| and |v| meet in shared memory
 // once per step.  When 2*32*b doubles do not fit, v/y live in a global
@@ -185,13 +185,14 @@ size_t diag_smem_bytes_nw(int b, int nw) {
 }
 size_t diag_smem_bytes(int b) { return diag_smem_bytes_nw(b, kDiagWarpsSmem); }
 
-// Body of the diagonal kernel for the 32 shifts of block bx; vy_scratch is
-// this block's global v/y region, or null when v/y fit in shared memory.
-template <int kDiagWarps>
-__device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, double *vy_scratch) {
-    extern __shared__ double sm[];
+// One-warp body of the diagonal kernel for the 32 shifts of block bx, one
+// per lane: each step's scalar chain and the row updates run on the same
+// warp.  `sm` is the warp's own shared-memory region (diag_small_bytes(b, 1),
+// then v/y unless vy_scratch is given); the warp orders its shared-memory
+// accesses with __syncwarp only, so several warps of one CTA may each run
+// their own block.
+__device__ __forceinline__ void diag_body_1w(const DevProblem &P, int J, int bx, double *sm, double *vy_scratch) {
     const int lane = threadIdx.x & 31;
-    const int wid = threadIdx.x >> 5;
     const int k0 = bx * 32;
     const int k = k0 + lane;
     const bool act = k < P.S;
@@ -199,28 +200,22 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
     const bool is = P.is != 0;
     const size_t Spad = (size_t)P.Spad;
 
-    // With several warps, warp 0 alone evaluates each step's scalar chain and
-    // hands its per-lane results to the others through shared memory.
-    constexpr bool kBcast = kDiagWarps > 1;
     double *hc = sm;                                          // [2][b+1]
-    // Per-warp partial maxima, double-buffered by step parity: [2][W][2][32].
+    // Maxima of |y| and |v| over rows 0 .. j-2, double-buffered by step parity: [2][2][32].
     unsigned long long *pmax = reinterpret_cast<unsigned long long *>(sm + 2 * (b + 1));
-    double *bc = sm + 2 * (b + 1) + 2 * kDiagWarps * 2 * 32;  // [kDiagBcast][32]
     double *v, *y;
     if (vy_scratch) {
         v = vy_scratch;
-        y = v + (size_t)32 * b;
     } else {
-        v = bc + (kBcast ? kDiagBcast * 32 : 0);
-        y = v + (size_t)32 * b;
+        v = sm + 2 * (b + 1) + 2 * 2 * 32;
     }
+    y = v + (size_t)32 * b;
 #define V(i) v[(size_t)(i) * 32 + lane]
 #define Y(i) y[(size_t)(i) * 32 + lane]
-#define PMAX(par, w, which) pmax[(((par) * kDiagWarps + (w)) * 2 + (which)) * 32 + lane]
-#define BC(q) bc[(q) * 32 + lane]
+#define PMAX(par, which) pmax[((par) * 2 + (which)) * 32 + lane]
 
     // Load the crossover column and the right-hand side tile, transposed.
-    for (int c = wid; c < 32; c += kDiagWarps) {
+    for (int c = 0; c < 32; ++c) {
         const int kc = k0 + c;
         if (kc < P.S) {
             const double *rc = P.R + l + (size_t)kc * P.ldr;
@@ -244,45 +239,38 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
     int pert = 0;
 
     const double *Hd = P.H + l + (size_t)l * P.ldh;          // H(l, l)
-    auto stage_col = [&](int col, double *dst) {              // H(l : l+col+1, l+col), warp 0
+    auto stage_col = [&](int col, double *dst) {              // H(l : l+col+1, l+col)
         int rows = col + 2;
         if (rows > b) rows = b;
         const double *src = Hd + (size_t)col * P.ldh;
         for (int i = lane; i < rows; i += 32) cp_async8(dst + i, src + i);
         cp_async_commit();
     };
-    if (wid == 0 && b >= 2) stage_col(b - 2, hc);
-    __syncthreads();                                           // tiles loaded
+    if (b >= 2) stage_col(b - 2, hc);
+    __syncwarp();                                             // tiles loaded
 
-    // Per-warp maxima of |y(0:b-3)| and |v(0:b-3)| for the first step.
+    // Maxima of |y(0:b-3)| and |v(0:b-3)| for the first step.
     {
         unsigned long long ym = 0, vm = 0;
-        for (int i = wid; i < b - 2; i += kDiagWarps) {
+        for (int i = 0; i < b - 2; ++i) {
             ym = umax64(ym, abs_bits(Y(i)));
             vm = umax64(vm, abs_bits(V(i)));
         }
-        PMAX(0, wid, 0) = ym;
-        PMAX(0, wid, 1) = vm;
+        PMAX(0, 0) = ym;
+        PMAX(0, 1) = vm;
     }
-    // v(j) and y(j) of the current step are carried in registers: every warp
-    // computes them identically in the previous step.
+    // v(j) and y(j) of the current step are carried in registers.
     double vcar = V(b - 1), ycar = Y(b - 1);
 
     int buf = 0, par = 0;
     for (int j = b - 1; j >= 1; --j) {
-        if (wid == 0) cp_async_wait_all();
-        __syncthreads();                                       // previous step's rows and column j-1 visible
+        cp_async_wait_all();
+        __syncwarp();                                         // previous step's rows and column j-1 visible
         const double *hcol = hc + buf * (b + 1);              // column j-1 of the tile
-        if (wid == 0 && j >= 2) stage_col(j - 2, hc + (buf ^ 1) * (b + 1));
-        double c = 0.0, s = 0.0, yc = 0.0, ys = 0.0, a1 = 1.0, a2 = 1.0, a3 = 1.0;
-        double yj = 0.0, yjm1 = 0.0, hdiag = 0.0, vjm1 = 0.0;
-        if (!kBcast || wid == 0) {
-            unsigned long long ymax = 0, vmax = 0;
-#pragma unroll
-            for (int w = 0; w < kDiagWarps; ++w) {
-                ymax = umax64(ymax, PMAX(par, w, 0));
-                vmax = umax64(vmax, PMAX(par, w, 1));
-            }
+        if (j >= 2) stage_col(j - 2, hc + (buf ^ 1) * (b + 1));
+        double c, s, yc, ys, a1, a2, a3, yj, yjm1, hdiag, vjm1;
+        {
+            unsigned long long ymax = PMAX(par, 0), vmax = PMAX(par, 1);
             const double hsub = hcol[j];
             hdiag = hcol[j - 1] - mu;
             const double vj = vcar;
@@ -291,7 +279,7 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
             yjm1 = Y(j - 1);
 
             givens(vj, hsub, c, s);
-            if (act && wid == 0) {
+            if (act) {
                 P.Cr[(size_t)(l + j) * Spad + k] = c;
                 P.Sr[(size_t)(l + j) * Spad + k] = s;
             }
@@ -326,32 +314,11 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
                 ys = yj * s;
             }
             beta = sc_combine(beta, phi, is);
-            if (kBcast) {
-                BC(0) = c;
-                BC(1) = s;
-                BC(2) = yc;
-                BC(3) = ys;
-                BC(4) = a1;
-                BC(5) = a2;
-                BC(6) = a3;
-            }
-        }
-        if (kBcast) {
-            __syncthreads();                                   // this step's scalars visible
-            if (wid != 0) {
-                c = BC(0);
-                s = BC(1);
-                yc = BC(2);
-                ys = BC(3);
-                a1 = BC(4);
-                a2 = BC(5);
-                a3 = BC(6);
-            }
         }
         const bool scaled = (!is_one(a1)) || (!is_one(a2)) || (!is_one(a3));
         if (scaled) {
             // Rare: the whole-vector scale() also reaches the solved rows j+1 .. b-1.
-            for (int i = j + 1 + ((wid - (j + 1)) % kDiagWarps + kDiagWarps) % kDiagWarps; i < b; i += kDiagWarps) {
+            for (int i = j + 1; i < b; ++i) {
                 double t = Y(i);
                 if (!is_one(a1)) t = a1 * t;
                 if (!is_one(a2)) t = a2 * t;
@@ -361,16 +328,16 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
         }
         unsigned long long ymx = 0, vmx = 0;
         const int lim = j - 1;
-        // Rows i = wid, wid+4, ... < j-1 in batches of 4: loads first, then
-        // the independent FMA chains, then the stores.
-        int i = wid;
-        for (; i + 3 * kDiagWarps < lim; i += 4 * kDiagWarps) {
+        // Rows 0 .. j-2 in batches of 4: loads first, then the independent
+        // FMA chains, then the stores.
+        int i = 0;
+        for (; i + 3 < lim; i += 4) {
             double hh[4], yy[4], vv[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                hh[q] = hcol[i + q * kDiagWarps];
-                yy[q] = Y(i + q * kDiagWarps);
-                vv[q] = V(i + q * kDiagWarps);
+                hh[q] = hcol[i + q];
+                yy[q] = Y(i + q);
+                vv[q] = V(i + q);
             }
             if (scaled) {
 #pragma unroll
@@ -387,7 +354,7 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
             }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                const int r = i + q * kDiagWarps;
+                const int r = i + q;
                 Y(r) = yy[q];
                 V(r) = vv[q];
                 if (r < lim - 1) {
@@ -396,7 +363,7 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
                 }
             }
         }
-        for (; i < lim; i += kDiagWarps) {
+        for (; i < lim; ++i) {
             const double h = hcol[i];
             double yi = Y(i), vi = V(i);
             if (scaled) {
@@ -413,79 +380,63 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
                 vmx = umax64(vmx, abs_bits(vi));
             }
         }
-        PMAX(par ^ 1, wid, 0) = ymx;
-        PMAX(par ^ 1, wid, 1) = vmx;
-        if (kBcast ? wid == 0 : j % kDiagWarps == wid) Y(j) = yj;   // solved entry, by the chain warp
-        if (!kBcast || wid == 0) {
-            // Next annihilation column entry (solve-task.c:105-108) and y(j-1).
-            vcar = fma(c, hdiag, s * vjm1);
-            ycar = yjm1;
-        }
+        PMAX(par ^ 1, 0) = ymx;
+        PMAX(par ^ 1, 1) = vmx;
+        Y(j) = yj;                                            // the solved entry
+        // Next annihilation column entry (solve-task.c:105-108) and y(j-1).
+        vcar = fma(c, hdiag, s * vjm1);
+        ycar = yjm1;
         buf ^= 1;
         par ^= 1;
     }
 
     double c0 = 0.0, s0 = 0.0;
     {
-        double y0 = 0.0, a = 1.0;
-        if (!kBcast || wid == 0) {
-            double v0 = b >= 2 ? vcar : V(0);
-            y0 = b >= 2 ? ycar : Y(0);
-            double hleft = 0.0;
-            if (J > 0) {
-                // Final rotation with H(l, l-1) (reduce.c:53-61, solve-task.c:111-118).
-                hleft = P.H[l + (size_t)(l - 1) * P.ldh];
-                if (hleft != 0) {
-                    givens(v0, hleft, c0, s0);
-                } else {
-                    c0 = 1.0;
-                    s0 = 0.0;
-                }
-                if (act && wid == 0) {
-                    P.Cr[(size_t)l * Spad + k] = c0;
-                    P.Sr[(size_t)l * Spad + k] = s0;
-                }
-                v0 = fma(v0, c0, -(hleft * s0));
+        double v0 = b >= 2 ? vcar : V(0);
+        const double y0 = b >= 2 ? ycar : Y(0);
+        double y0s = y0;
+        if (J > 0) {
+            // Final rotation with H(l, l-1) (reduce.c:53-61, solve-task.c:111-118).
+            const double hleft = P.H[l + (size_t)(l - 1) * P.ldh];
+            if (hleft != 0) {
+                givens(v0, hleft, c0, s0);
+            } else {
+                c0 = 1.0;
+                s0 = 0.0;
             }
-            double phi = sc_one(is);
-            pert |= solve_1x1(smin, v0, 0.0, y0, phi, is);
-            beta = sc_combine(beta, phi, is);
-            a = sc_value(phi, is);
-            if (kBcast) {
-                BC(0) = c0;
-                BC(1) = s0;
-                BC(2) = a;
+            if (act) {
+                P.Cr[(size_t)l * Spad + k] = c0;
+                P.Sr[(size_t)l * Spad + k] = s0;
             }
+            v0 = fma(v0, c0, -(hleft * s0));
         }
-        __syncthreads();                                       // last step's rows (and the scalars) written
-        if (kBcast && wid != 0) {
-            c0 = BC(0);
-            s0 = BC(1);
-            a = BC(2);
-        }
+        double phi = sc_one(is);
+        pert |= solve_1x1(smin, v0, 0.0, y0s, phi, is);
+        beta = sc_combine(beta, phi, is);
+        const double a = sc_value(phi, is);
+        __syncwarp();                                         // last step's rows written
         if (!is_one(a))
-            for (int i = 1 + ((wid - 1) % kDiagWarps + kDiagWarps) % kDiagWarps; i < b; i += kDiagWarps)
-                Y(i) = a * Y(i);
-        if (wid == 0) Y(0) = y0;
+            for (int i = 1; i < b; ++i) Y(i) = a * Y(i);
+        Y(0) = y0s;
     }
-    __syncthreads();
+    __syncwarp();
 
     // Store the solved tile, its scaling factor and the perturbation flag.
-    for (int c = wid; c < 32; c += kDiagWarps) {
+    for (int c = 0; c < 32; ++c) {
         const int kc = k0 + c;
         if (kc < P.S) {
             double *xc = P.X + l + (size_t)kc * P.ldx;
             for (int i = lane; i < b; i += 32) xc[i] = y[(size_t)i * 32 + c];
         }
     }
-    if (act && wid == 0) {
+    if (act) {
         P.beta[(size_t)J * Spad + k] = beta;
         if (pert) P.pert[k] = 1;
     }
     if (J == 0 || !act) return;
 
-    if (wid == 0) {
-        // W(q) = c_q * prod_{p<q} s_p, pi = prod s (crossover propagation).
+    // W(q) = c_q * prod_{p<q} s_p, pi = prod s (crossover propagation).
+    {
         double pk = 1.0;
         for (int q = 0; q < b; ++q) {
             const double cq = P.Cr[(size_t)(l + q) * Spad + k];
@@ -495,7 +446,7 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
         }
         P.pi[k] = pk;
     }
-    if (wid == (kDiagWarps > 1 ? 1 : 0)) {
+    {
         // Ytilde2 = G_{b-1}^T ... G_1^T (c_0 x_0, x_1, ...) (update-task.c:193-220);
         // Zs(q) = Ytilde2(q-1), Zs(0) = 0, zlast = Ytilde2(b-1).
         unsigned long long zmx = 0;
@@ -518,7 +469,6 @@ __device__ __forceinline__ void diag_body(const DevProblem &P, int J, int bx, do
 #undef V
 #undef Y
 #undef PMAX
-#undef BC
 }
 
 // The four-warp diagonal kernel, software-pipelined by one step.  Step j's
@@ -1617,8 +1567,9 @@ __global__ void k_init_b(const DevProblem *probs, const BatchItem *items) {
 }
 
 __global__ void __launch_bounds__(32 * kDiagWarpsB) k_diag_b(const DevProblem *probs, const BatchItem *items) {
+    extern __shared__ double sm[];
     const BatchItem it = items[blockIdx.x];
-    diag_body<kDiagWarpsB>(probs[it.x], it.y, it.z, nullptr);
+    diag_body_1w(probs[it.x], it.y, it.z, sm, nullptr);
 }
 
 // One block per (problem, stage, 8 shifts); the tiles above the diagonal

@@ -20,7 +20,18 @@
 // and writes everything else before reading it.  The first call on a device
 // resolves the array's device address (cudaGetSymbolAddress, with that device
 // current) and caches it, so that first call should come before any stream
-// capture.
+// capture.  Under CUDA's default lazy module loading that first call also
+// loads the library's kernels on the device and commits the array's device
+// memory -- an allocation made by the driver on the caller's behalf -- so a
+// caller whose pool takes the free memory later should make its first call
+// before that (or load modules eagerly, CUDA_MODULE_LOADING=EAGER).
+//
+// The call returns only after the solve has finished: it synchronises the
+// stream to read the norm of H, the convergence status of each restart round
+// and the error word.  On a failure after work was enqueued it also waits
+// for that work before returning, so a following call (on any stream) does
+// not race with the failed one.
+#include "hsr_common.h"
 #include "hsr_kernels.h"
 #include "../../include/hsrq3in_gb300.h"
 
@@ -61,16 +72,18 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
 
 bool encode_map(CUtensorMap *m, const double *base, unsigned long long inner, unsigned long long outer,
                 unsigned long long ld, unsigned bx, unsigned by) {
-    static EncodeTiledFn fn = nullptr;
-    if (!fn) {
+    // Looked up once; a function-local static's initialiser runs exactly once
+    // even when several host threads make their first call together.
+    static const EncodeTiledFn fn = []() -> EncodeTiledFn {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
                 cudaSuccess ||
             q != cudaDriverEntryPointSuccess)
-            return false;
-        fn = reinterpret_cast<EncodeTiledFn>(p);
-    }
+            return nullptr;
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    if (!fn) return false;
     cuuint64_t dims[2] = {inner, outer};
     cuuint64_t strides[1] = {ld * sizeof(double)};
     cuuint32_t box[2] = {bx, by};
@@ -94,9 +107,16 @@ struct Carve {
     }
 };
 
-#define NA_CK(x)                              \
-    do {                                      \
-        if ((x) != cudaSuccess) return HSR_ERR_CUDA; \
+// The CUDA error behind the last HSR_ERR_CUDA of this thread's call.
+thread_local cudaError_t t_na_error = cudaSuccess;
+
+#define NA_CK(x)                                 \
+    do {                                         \
+        const cudaError_t e_ = (x);              \
+        if (e_ != cudaSuccess) {                 \
+            t_na_error = e_;                     \
+            return HSR_ERR_CUDA;                 \
+        }                                        \
     } while (0)
 
 struct NoallocSolve {
@@ -141,8 +161,10 @@ int noalloc_pass(NoallocSolve &s, int mode, int its, int off, int cnt) {
 
 using namespace hsr;
 
-extern "C" int hsr_inverse_iteration_noalloc(int n, const double *dH, int lddH, int nrhs, double *dwr, int tlsz,
-                                             double *dvr, int lddvr, int scaling, void *stream, int *status) {
+namespace {
+
+int noalloc_solve(int n, const double *dH, int lddH, int nrhs, double *dwr, int tlsz, double *dvr, int lddvr,
+                  int scaling, cudaStream_t st_caller, int *status, bool *enqueued) {
     if (n <= 0 || lddH < n || nrhs < 0 || tlsz <= 0 || (tlsz % 4) != 0 || lddvr < n || !dH) return HSR_ERR_ARG;
     if (nrhs > 0 && (!dwr || !dvr)) return HSR_ERR_ARG;
     if (n > HSR_NOALLOC_MAX_N || nrhs > HSR_NOALLOC_MAX_NRHS) return HSR_ERR_ARG;
@@ -157,7 +179,7 @@ extern "C" int hsr_inverse_iteration_noalloc(int n, const double *dH, int lddH, 
     s.S = nrhs;
     s.Spad = (int)up((size_t)nrhs, 64);
     s.is = scaling == HSR_SCALING_DOUBLE ? 0 : 1;
-    s.st = static_cast<cudaStream_t>(stream);
+    s.st = st_caller;
     s.X = dvr;
     s.ldx = lddvr;
     s.wr = dwr;
@@ -220,6 +242,7 @@ extern "C" int hsr_inverse_iteration_noalloc(int n, const double *dH, int lddH, 
         P.smlnum = std::fmax(2 * DBL_MIN, DBL_MIN * ((double)n / eps));
     }
     cudaStream_t st = s.st;
+    *enqueued = true;
 
     if (copyH) {
         NA_CK(cudaMemcpy2DAsync(Hpad, (size_t)ldh_pad * 8, dH, (size_t)lddH * 8, (size_t)n * 8, n,
@@ -318,4 +341,19 @@ extern "C" int hsr_inverse_iteration_noalloc(int n, const double *dH, int lddH, 
         nonconv += !st_h[k];
     }
     return nonconv ? HSR_ERR_NOT_CONVERGED : HSR_OK;
+}
+
+}  // namespace
+
+extern "C" int hsr_inverse_iteration_noalloc(int n, const double *dH, int lddH, int nrhs, double *dwr, int tlsz,
+                                             double *dvr, int lddvr, int scaling, void *stream, int *status) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    bool enqueued = false;
+    t_na_error = cudaSuccess;
+    const int rc = noalloc_solve(n, dH, lddH, nrhs, dwr, tlsz, dvr, lddvr, scaling, st, status, &enqueued);
+    // After a failure, wait for whatever this call already enqueued: it
+    // writes the shared scratch array and dvr, and the caller's next call
+    // must not overlap with it.  Its own result does not change the status.
+    if (rc < 0 && enqueued) (void)cudaStreamSynchronize(st);
+    return record_status(rc, rc == HSR_ERR_CUDA ? t_na_error : cudaSuccess);
 }

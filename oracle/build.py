@@ -11,7 +11,8 @@
   as the CPU baseline.
 
 ``build_reference()`` compiles the *unmodified* reference sources where they
-lie (``/root/reference``, read-only) into ``oracle/_ref/`` -- only when they
+lie (``$HSRQ3IN_REFERENCE``, default ``/root/reference``, read-only) into
+``oracle/_ref/`` -- only when they
 are present, which is the case in the development container and never on a
 GPU host.  The reference needs BLAS/LAPACK (``dgemm_``, ``dlange_``,
 ``dlartg_``); it is linked against the OpenBLAS that ships inside scipy,
@@ -32,7 +33,9 @@ import tempfile
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_SRC = "/root/reference"
+# Where the reference sources lie: $HSRQ3IN_REFERENCE, else the read-only
+# checkout of the development container.
+REFERENCE_SRC = os.environ.get("HSRQ3IN_REFERENCE", "/root/reference")
 
 REF_SOURCES = [
     "inverse_iteration.c", "partition.c", "reduce.c", "robust.c",

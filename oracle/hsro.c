@@ -193,12 +193,27 @@ static double protect_double_update(double t1, double x1, double t2, double x2,
 
 /* solve_1x1_real_system (robust.c:422-479): x := (scale*x)/(t-lambda) with
  * |t-lambda| lifted to smin when smaller; returns 1 if lifted.             */
+/* Pivot log (test instrumentation): when hsro_set_pivot_log() installed a
+ * buffer, each 1x1 solve folds |t - lambda| / smin of its column into the
+ * buffer's entry for that column (the minimum over the column's solves), so a
+ * test can tell how close a perturbation decision was to its threshold.
+ * t_piv points at the entry of the column being solved on this thread.      */
+static double *g_pivlog;
+static const unsigned char *g_pert_base;
+static _Thread_local double *t_piv;
+
+void hsro_set_pivot_log(double *buf) { g_pivlog = buf; }
+
 int hsro_solve_1x1(double smin, double t, double lambda, double *x,
                    double *scale, int is)
 {
     int info = 0;
     const double s = protect_sum(t, -lambda);
     double csr = (s * t) - (s * lambda);
+    if (t_piv) {
+        const double r = fabs(csr) / smin;
+        if (!(r >= *t_piv)) *t_piv = r;
+    }
     if (fabs(csr) < smin) {
         csr = smin;
         info = 1;
@@ -741,8 +756,10 @@ static int shift_tile(const prob_t *P, int ns, const double *wr, double *vr,
         for (int k = 0; k < ns; k++) {
             double *v = w->v;
             memcpy(v, RT(J) + (size_t)k * b, (size_t)b * sizeof(double));
+            t_piv = (g_pivlog && pert && g_pert_base) ? g_pivlog + ((pert + k) - g_pert_base) : NULL;
             const int pk = diag_tile(P, J, wr[k], v, Y(J, k), SC(J) + k,
                                      CT(J) + (size_t)k * b, ST(J) + (size_t)k * b, cn);
+            t_piv = NULL;
             if (pert && pk) pert[k] = 1;
         }
         if (J == 0) break;
@@ -956,6 +973,8 @@ static int separate(int n, int nrhs, const int *conv, double *wr, double *vr,
     double *svr = (double *)malloc(sizeof(double) * (size_t)n * nrhs);
     unsigned char *sp = (unsigned char *)malloc((size_t)nrhs);
     double *scs = (double *)malloc(sizeof(double) * (size_t)nrhs);
+    double *piv = (g_pivlog && pert && g_pert_base) ? g_pivlog + (pert - g_pert_base) : NULL;
+    double *spv = (double *)malloc(sizeof(double) * (size_t)nrhs);
     int pc = 0, pn = nc;
     for (int k = 0; k < nrhs; k++) {
         const int pos = conv[k] ? pc++ : pn++;
@@ -963,7 +982,10 @@ static int separate(int n, int nrhs, const int *conv, double *wr, double *vr,
         memcpy(svr + (size_t)pos * n, vr + (size_t)k * ldvr, sizeof(double) * (size_t)n);
         sp[pos] = pert ? pert[k] : 0;
         scs[pos] = colscale ? colscale[k] : 0.0;
+        spv[pos] = piv ? piv[k] : 0.0;
     }
+    if (piv) memcpy(piv, spv, sizeof(double) * (size_t)nrhs);
+    free(spv);
     memcpy(wr, swr, sizeof(double) * (size_t)nrhs);
     for (int k = 0; k < nrhs; k++)
         memcpy(vr + (size_t)k * ldvr, svr + (size_t)k * n, sizeof(double) * (size_t)n);
@@ -998,6 +1020,9 @@ int hsro_inverse_iteration(int n, const double *H, int ldH, int nrhs,
     int *conv = (int *)malloc(sizeof(int) * (size_t)nrhs);
     if (!vrnorms || !conv) { free(vrnorms); free(conv); free(fr); free((void *)P.Hn); return -2; }
     if (perturbed) memset(perturbed, 0, (size_t)nrhs);
+    g_pert_base = perturbed;
+    if (g_pivlog)
+        for (int k = 0; k < nrhs; k++) g_pivlog[k] = INFINITY;
 
     /* init_real_eigenvectors (inverse_iteration.c:19-34). */
     for (int k = 0; k < nrhs; k++)
@@ -1033,6 +1058,8 @@ int hsro_inverse_iteration(int n, const double *H, int ldH, int nrhs,
         const double ub = fmax(fmax(eps3, tmp), fabs(tmp - eps3 / sqrt(n)));
         for (int i = 0; i < T * mm; i++) vrnorms[i] = ub;
         if (perturbed) memset(perturbed + nconv_front, 0, (size_t)mm);
+        if (g_pivlog && perturbed)
+            for (int k = 0; k < mm; k++) g_pivlog[nconv_front + k] = INFINITY;
         rc = solve_all(&P, mm, wr + nconv_front, v0, ldvr, vrnorms, rhs_tlsz,
                        perturbed ? perturbed + nconv_front : NULL,
                        colscale ? colscale + nconv_front : NULL, &total);
@@ -1051,6 +1078,7 @@ int hsro_inverse_iteration(int n, const double *H, int ldH, int nrhs,
         (void)m;
     }
     stats_out(stats, &total);
+    g_pert_base = NULL;
     if (stats) { stats->restarts = restarts; stats->nonconverged = nonconv; }
     free(vrnorms); free(conv); free(fr); free((void *)P.Hn);
     return rc;

@@ -98,6 +98,12 @@ int hsro_robust_cmplx_div(double smin, double a, double b, double c, double d,
 int hsro_csolve_1x1(double smin, double tr, double ti, double lr, double li,
                     double *xr, double *xi, double *scale, int intscale);
 
+/* Pivot log for the decision tests: while buf is set, hsro_inverse_iteration
+ * stores in buf[k] (nrhs entries) the smallest |t - lambda| / smin over the
+ * 1x1 solves of output column k (< 1 where the solve was perturbed).  NULL
+ * switches it off.  Not thread-safe across concurrent calls.               */
+void hsro_set_pivot_log(double *buf);
+
 /* Number of OpenMP threads the oracle may use (0 = runtime default).        */
 void hsro_set_threads(int nthreads);
 /* Arithmetic mode the library was compiled for: 0 ref, 1 fma.              */

@@ -49,6 +49,8 @@ def _lib(variant: str) -> C.CDLL:
         lib.hsro_dlartg.restype = None
         lib.hsro_dlartg.argtypes = [C.c_double, C.c_double] + [C.POINTER(C.c_double)] * 3
         lib.hsro_set_threads.argtypes = [C.c_int]
+        lib.hsro_set_pivot_log.argtypes = [C.c_void_p]
+        lib.hsro_set_pivot_log.restype = None
         lib.hsro_inverse_iteration_cplx.restype = C.c_int
         lib.hsro_cgivens.restype = None
         lib.hsro_cgivens.argtypes = [C.c_double] * 3 + [C.POINTER(C.c_double)] * 3
@@ -87,10 +89,23 @@ def _call(fn_name: str, H, wr, tlsz, rhs_tlsz, vr, intscale, variant):
                 colscale=colscale[:nrhs], status=status[:nrhs], stats=st.as_dict())
 
 
-def oracle_inverse_iteration(H, wr, tlsz, rhs_tlsz, intscale=0, variant="ref"):
+def oracle_inverse_iteration(H, wr, tlsz, rhs_tlsz, intscale=0, variant="ref", pivot_log=False):
+    """pivot_log: also return ``pivot``, per output column the smallest
+    |t - lambda| / smin over its 1x1 solves (< 1 exactly where the column was
+    perturbed), which tells how close each perturbation decision was."""
     n = np.asarray(H).shape[0]
     vr = np.zeros((n, len(wr)), dtype=np.float64, order="F")
-    return _call("hsro_inverse_iteration", H, wr, tlsz, rhs_tlsz, vr, intscale, variant)
+    if not pivot_log:
+        return _call("hsro_inverse_iteration", H, wr, tlsz, rhs_tlsz, vr, intscale, variant)
+    lib = _lib(variant)
+    piv = np.full(max(len(wr), 1), np.inf)
+    lib.hsro_set_pivot_log(piv.ctypes.data_as(C.c_void_p))
+    try:
+        out = _call("hsro_inverse_iteration", H, wr, tlsz, rhs_tlsz, vr, intscale, variant)
+    finally:
+        lib.hsro_set_pivot_log(None)
+    out["pivot"] = piv[:len(wr)]
+    return out
 
 
 def oracle_solve_rhs(H, wr, rhs, tlsz, rhs_tlsz, intscale=0, variant="ref"):

@@ -10,7 +10,7 @@ complex robust kernels, which no reference driver calls.
 Every reference run happens in a child process: the reference aborts on some
 inputs (its restart path), which must not take this script down.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--n1000-only]
 """
 from __future__ import annotations
 
@@ -95,9 +95,106 @@ def complex_kernels(ctx):
     print("cplx_kernels: %d rows per kernel and scaling build" % len(res["div_in_0"]))
 
 
+def pack_hessenberg(H: np.ndarray) -> np.ndarray:
+    """The upper-Hessenberg part of H, column by column (rows 0 .. j+1 of
+    column j), which is all the solver reads."""
+    n = H.shape[0]
+    keep = np.arange(n)[:, None] <= np.arange(n)[None, :] + 1        # keep[i, j]: i <= j + 1
+    return np.ascontiguousarray(np.asarray(H).T[keep.T])
+
+
+def unpack_hessenberg(packed: np.ndarray, n: int) -> np.ndarray:
+    keep = np.arange(n)[:, None] <= np.arange(n)[None, :] + 1
+    Ht = np.zeros((n, n))
+    Ht[keep.T] = packed
+    return np.asfortranarray(Ht.T)
+
+
+def flags_from_events(events, wr: np.ndarray, smlnum: float) -> np.ndarray:
+    """Per-column perturbation flags from the reference's recorded 1x1-solve
+    decisions: each event carries the smin it was taken with, and smin =
+    max(eps/2 |mu|, smlnum) (solve-task.c:149) identifies the column."""
+    kind, key, _ = events
+    smin = np.maximum(np.finfo(np.float64).eps / 2 * np.abs(wr), smlnum)
+    hit = set(key[kind == 1].tolist())
+    return np.array([s in hit for s in smin], dtype=np.uint8)
+
+
+def _run_n1000(args, q):
+    """Reference solves of one order-1000 problem at (tlsz, rhs_tlsz) and
+    (200, 64), with the oracle's pivot log taken on the same input."""
+    H, wr, tlsz, rhs, cols, cols_alt = args
+    from oracle import pyoracle as O
+    r = O.reference_inverse_iteration(H, wr, tlsz, rhs)
+    o = O.oracle_inverse_iteration(H, wr, tlsz, rhs, variant="ref", pivot_log=True)
+    assert np.array_equal(o["vr"], r["vr"]) and np.array_equal(o["wr"], r["wr"])
+    alt = O.reference_inverse_iteration(H, wr, 200, 64) if cols_alt is not None else None
+    res = O.residuals(H, r["wr"], r["vr"])
+    q.put(dict(vr=r["vr"][:, cols], wr_out=r["wr"], counts=r["counts"], events=r["events"],
+               pert_oracle=o["perturbed"].astype(np.uint8), pivot=o["pivot"], residual=res,
+               vr_alt=None if alt is None else alt["vr"][:, cols_alt],
+               wr_alt=None if alt is None else alt["wr"]))
+
+
+def n1000_fixtures(ctx):
+    """Two order-1000 problems at the benchmark's tiling (tlsz 160, rhs_tlsz
+    64), with the reference's output:
+      n1000_real_t160: the plain small workload (real-spectrum generator,
+        seed 1234, all 1000 eigenvalues with relative 1e-12 noise, seed 1235);
+        128 sampled columns of the reference's eigenvectors at this tiling and
+        at (200, 64), per-column perturbation flags and pivot log, and the
+        eigenvalue sensitivities and relative gaps of every shift;
+      n1000_wellcond_t160: the well-conditioned companion (strictly-upper
+        entries scaled by 1/n, seed 1234, the exact eigenvalues as shifts);
+        160 sampled columns.
+    H is stored as its packed upper-Hessenberg part."""
+    from oracle import pyoracle as O
+    eps = np.finfo(np.float64).eps
+    n = 1000
+    tiny = np.finfo(np.float64).tiny
+    smlnum = max(2 * tiny, tiny * (n / eps))             # shifted_Hessenberg_solve.c:71
+    H, lam = G.real_spectrum(n, 1234)
+    wr = G.perturbed_shifts(lam, 1235)
+    cols = np.linspace(0, n - 1, 128).astype(np.int64)
+    specs = [("n1000_real_t160", H, lam, wr, cols, cols)]
+    H2, lam2 = G.well_conditioned(n, 1234)
+    specs.append(("n1000_wellcond_t160", H2, lam2, lam2.copy(), np.linspace(0, n - 1, 160).astype(np.int64), None))
+    for name, Hm, lm, w, cs, ca in specs:
+        q = ctx.Queue()
+        p = ctx.Process(target=_run_n1000, args=((Hm, w, 160, 64, cs, ca), q))
+        p.start()
+        out = q.get(timeout=1200)
+        p.join(60)
+        pert = flags_from_events(out["events"], out["wr_out"], smlnum)
+        assert np.array_equal(pert, out["pert_oracle"]), "event flags disagree with the oracle's"
+        srt = np.sort(lm)
+        gaps = np.minimum(np.abs(np.diff(srt, prepend=-np.inf)), np.abs(np.diff(srt, append=np.inf)))
+        idx = np.searchsorted(srt, lm)
+        relgap = gaps[idx] / np.abs(lm)
+        near = np.array([int(np.argmin(np.abs(lm - m))) for m in out["wr_out"]])
+        sens = O.eigen_sensitivity(Hm, out["wr_out"])
+        extra = {}
+        if out["vr_alt"] is not None:
+            assert np.array_equal(out["wr_alt"], out["wr_out"])
+            extra = dict(vr_alt=out["vr_alt"], alt_tlsz=200, alt_rhs_tlsz=64)
+        c = out["counts"]
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), Hp=pack_hessenberg(Hm), n=n, wr_in=w,
+                            wr_out=out["wr_out"], cols=cs, vr=out["vr"], tlsz=160, rhs_tlsz=64, intscale=0,
+                            perturbed=pert, pivot=out["pivot"], residual=out["residual"],
+                            relgap=relgap[near], sensitivity=sens,
+                            perturbations=c["perturbations"], div_rescales=c["div_rescales"],
+                            solve_rescales=c["solve_rescales"], part1_rescales=c["part1_rescales"],
+                            part2_rescales=c["part2_rescales"], **extra)
+        print("%s: %s, %d perturbed columns" % (name, c, int(pert.sum())))
+
+
 def main():
     ctx = mp.get_context("spawn")
+    if "--n1000-only" in sys.argv:
+        n1000_fixtures(ctx)
+        return
     complex_kernels(ctx)
+    n1000_fixtures(ctx)
     for case in cases():
         name, H, wr, tlsz, rhs, isc = case
         q = ctx.Queue()

@@ -111,3 +111,46 @@ def test_autotune_picks_a_candidate(gpu_lib):
     nlo = min(H.shape[0] for H, _ in probs)
     nhi = max(H.shape[0] for H, _ in probs)
     assert _lib.load().hsr_autotune_tlsz(nlo, nhi) == best
+
+
+def test_served_pinned_host_buffers(gpu_lib):
+    """Page-locked request buffers move by SM loads and stores through their
+    mapped pointers, pageable ones by copy engine: both replays give the same
+    results bit for bit, including padded leading dimensions, whose padding
+    rows the output copy must leave untouched."""
+    import torch
+    import hsrq3in_gb300 as hsr
+    probs = _mixed(10, 11, 30, 300)
+
+    def make(pinned):
+        reqs = []
+        for i, (H, wr) in enumerate(probs):
+            n, m = H.shape[0], len(wr)
+            ldh, ldv = n + 3, n + 5
+            if pinned:
+                Hb = torch.zeros(ldh * n, dtype=torch.float64).pin_memory().numpy()
+                Vb = torch.full((ldv * m,), -7.0, dtype=torch.float64).pin_memory().numpy()
+                Wb = torch.zeros(m, dtype=torch.float64).pin_memory().numpy()
+            else:
+                Hb = np.zeros(ldh * n)
+                Vb = np.full(ldv * m, -7.0)
+                Wb = np.zeros(m)
+            Hv = Hb.reshape((ldh, n), order="F")
+            Hv[:n, :] = H
+            Wb[:] = wr
+            reqs.append(dict(H=Hv[:n, :], wr=Wb, vr=Vb.reshape((ldv, m), order="F")[:n, :],
+                             vr_full=Vb.reshape((ldv, m), order="F"), arrival_s=0.002 * i))
+        return reqs
+
+    srv = hsr.Server(hbm_budget_bytes=2e9, tlsz=32)
+    a, b = make(True), make(False)
+    _, st_a, _ = srv.replay(a)
+    _, st_b, _ = srv.replay(b)
+    assert all(s == 0 for s in st_a) and all(s == 0 for s in st_b)
+    for ra, rb, (H, wr) in zip(a, b, probs):
+        n = H.shape[0]
+        assert np.array_equal(ra["vr"], rb["vr"])
+        assert np.array_equal(ra["wr"], rb["wr"])
+        assert np.all(ra["vr_full"][n:, :] == -7.0) and np.all(rb["vr_full"][n:, :] == -7.0)
+        ref = hsr.inverse_iteration(H, wr, 32, 16)
+        assert np.array_equal(ra["vr"], ref["vr"])

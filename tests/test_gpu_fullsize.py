@@ -1,5 +1,6 @@
 """The plain large configuration at its full size: n = 10000, all 10000
-eigenvalues (relative 1e-12 noise) as shifts, tlsz = 200, device-resident.
+eigenvalues (relative 1e-12 noise) as shifts, device-resident, at the
+benchmark's tile size 160 and at 200.
 
 Size-independent properties over every column -- finite, converged, unit
 2-norm, device residual ||Hx - lambda x|| / (||H||_F ||x||) <= 10 n eps --
@@ -16,11 +17,12 @@ pytestmark = pytest.mark.gpu
 EPS = np.finfo(np.float64).eps
 
 
-def test_plain_large_full_size(gpu_lib):
+@pytest.mark.parametrize("tlsz", [160, 200])
+def test_plain_large_full_size(gpu_lib, tlsz):
     import torch
     import bench
     import hsrq3in_gb300 as hsr
-    n, tlsz = 10000, 200
+    n = 10000
     H, wr = bench.workload(n, 1234)
     dev = torch.device("cuda:0")
     ld = n + (n & 1)

@@ -14,7 +14,9 @@ EPS = np.finfo(np.float64).eps
 # Driver fixtures: one problem and the reference's solve each (the scalar
 # kernel fixture cplx_kernels.npz is checked in test_oracle_cplx.py).
 GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
-                if os.path.basename(p) != "cplx_kernels.npz")
+                if os.path.basename(p) != "cplx_kernels.npz" and not os.path.basename(p).startswith("n1000_"))
+# Order-1000 fixtures at the benchmark tiling: packed H, sampled columns.
+GOLDEN_N1000 = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "n1000_*.npz")))
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
@@ -31,6 +33,35 @@ def test_oracle_reproduces_reference_golden(path):
 
 def test_golden_fixtures_present():
     assert len(GOLDEN) >= 7
+    assert len(GOLDEN_N1000) == 2
+
+
+def unpack_hessenberg(packed, n):
+    keep = np.arange(n)[:, None] <= np.arange(n)[None, :] + 1
+    Ht = np.zeros((n, n))
+    Ht[keep.T] = packed
+    return np.asfortranarray(Ht.T)
+
+
+@pytest.mark.parametrize("path", GOLDEN_N1000, ids=[os.path.basename(p)[:-4] for p in GOLDEN_N1000])
+def test_oracle_reproduces_reference_n1000(path):
+    """Order 1000 at tlsz 160, rhs_tlsz 64: the reference's shifts, sampled
+    eigenvector columns (bit for bit), per-column perturbation flags (mapped
+    from its recorded decisions) and decision counts."""
+    z = np.load(path)
+    n = int(z["n"])
+    H = unpack_hessenberg(z["Hp"], n)
+    O.set_threads(os.cpu_count() or 1, "ref")
+    o = O.oracle_inverse_iteration(H, z["wr_in"], int(z["tlsz"]), int(z["rhs_tlsz"]), variant="ref",
+                                   pivot_log=True)
+    assert np.array_equal(o["wr"], z["wr_out"])
+    assert np.array_equal(o["vr"][:, z["cols"]], z["vr"])
+    assert np.array_equal(o["perturbed"], z["perturbed"].astype(bool))
+    assert np.array_equal(o["pivot"], z["pivot"])
+    assert o["stats"]["perturbations"] == int(z["perturbations"])
+    for k in ("div_rescales", "solve_rescales", "part1_rescales", "part2_rescales"):
+        assert o["stats"][k] == int(z[k]) == 0, k
+    assert np.all(z["residual"] <= 10 * n * EPS)
 
 
 @pytest.mark.skipif(not O.reference_available(), reason="reference sources not on this host")
