@@ -72,9 +72,11 @@ def parse():
                          "served: a Poisson request trace through the request loop; complex: n=10k with "
                          "n/2 complex-conjugate shifts; dense: reduce + solve + back-transform of a dense matrix")
     ap.add_argument("--problems", type=int, default=4096, help="batched: number of problems")
-    ap.add_argument("--requests", type=int, default=800, help="served: number of requests")
-    ap.add_argument("--rate", type=float, default=120.0, help="served: arrivals per second")
-    ap.add_argument("--pool", type=int, default=48, help="served: distinct generated matrices")
+    ap.add_argument("--requests", type=int, default=20000, help="served: number of requests")
+    ap.add_argument("--rate", type=float, default=200.0, help="served: arrivals per second")
+    ap.add_argument("--saturate", type=int, default=4000,
+                    help="served: the first this many requests arriving at once (capacity)")
+    ap.add_argument("--pool", type=int, default=256, help="served: distinct matrices generated on the device")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="served: HBM budget")
     ap.add_argument("--batch-tlsz", type=int, default=0, help="batched/served tile size (0: autotune)")
     ap.add_argument("--stress-order", type=int, default=5000, help="stress: n of the robustness-stress problem")
@@ -373,6 +375,145 @@ def run_gpu(args, H, wr, rank, world):
     return out
 
 
+SMALL_N = 1000
+SMALL_STEPS = 50
+SMALL_TLSZ = 160
+
+
+def run_plain_small(args, tlsz: int):
+    """The plain small workload: one H of order 1000 from the same generator
+    (seed 1234), all 1000 eigenvalues with relative 1e-12 noise as shifts.
+    Its inputs and workspaces fit in L2, so a 512 MB buffer is written
+    between timed steps and every step is timed alone with CUDA events on the
+    launching stream.  value: device-resident (hsr_inverse_iteration_device);
+    e2e: the drop-in tiled_inverse_iteration with pinned host buffers, each
+    step after the same flush; the same-run CPU time of the oracle port on all
+    host cores over all 1000 shifts; perturbation counts of the device and of
+    the reference arithmetic (oracle "ref", bit-identical to the reference) at
+    the same tiling."""
+    import torch
+    import hsrq3in_gb300 as hsr
+    from hsrq3in_gb300 import _lib
+    lib = hsr.load(build_if_missing=True)
+    n = SMALL_N
+    H, wr = workload(n, args.seed)
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    ldh = n + (n & 1)
+    dHt = torch.zeros((n, ldh), dtype=torch.float64, device=dev)
+    dHt[:, :n] = torch.from_numpy(np.ascontiguousarray(H.T)).to(dev)
+    dwr0 = torch.from_numpy(np.ascontiguousarray(wr)).to(dev)
+    dwr = dwr0.clone()
+    dX = torch.empty((n, ldh), dtype=torch.float64, device=dev)
+    flush = torch.empty(64 << 20, dtype=torch.float64, device=dev)     # 512 MB > L2
+    stream = torch.cuda.Stream(device=dev)
+    opt = _lib.Options(0, 0, -1, 0.0)
+    steps = max(args.steps, SMALL_STEPS)
+
+    def step():
+        rc = lib.hsr_inverse_iteration_device(n, dHt.data_ptr(), ldh, n, dwr.data_ptr(), tlsz, dX.data_ptr(), ldh,
+                                              C.byref(opt), C.c_void_p(stream.cuda_stream), None, None)
+        if rc < 0:
+            raise RuntimeError("device call failed: %d" % rc)
+
+    ncls = len(_lib.KERNEL_CLASSES)
+    kms = np.zeros(ncls)
+    times = []
+    launches = 0
+    with ClockSampler(0) as clk:
+        with torch.cuda.stream(stream):
+            for it in range(args.warmup + steps):
+                dwr.copy_(dwr0)
+                flush.fill_(float(it))
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                step()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                if it >= args.warmup:
+                    times.append(e0.elapsed_time(e1))
+                    launches += lib.hsr_last_launch_count()
+            # one more pass with per-kernel-class timing (not part of the value)
+            lib.hsr_set_kernel_timing(1)
+            dwr.copy_(dwr0)
+            flush.fill_(0.0)
+            step()
+            torch.cuda.synchronize()
+            ms = (C.c_double * ncls)()
+            lib.hsr_last_kernel_times(ms, None, None)
+            kms = np.array(ms[:])
+            lib.hsr_set_kernel_timing(0)
+    ms_step = float(np.mean(times))
+    dfma, _ = hsr.fp64_peak(100.0)
+    peak = dfma / 1e3
+    whole = 2.0 * n * n * n / (ms_step * 1e-3) / 1e12
+    out = {"value": n / (ms_step / 1e3), "unit": UNIT, "ms_per_step": ms_step,
+           "ms_min": float(np.min(times)), "steps": steps, "warmup": args.warmup,
+           "whole_solve_tflops_2n2S": whole,
+           "roofline": {"bound": "fp64", "achieved": whole, "peak": peak, "unit": "TFLOP/s", "frac": whole / peak,
+                        "kernel": "whole solve (2 n^2 S algorithmic flops over the solve's wall time; at this "
+                                  "order the sequential diagonal chain, not one kernel, sets the time)",
+                        "peak_source": "FP64 DFMA stream measured in this run"},
+           "kernel_ms_one_step": {k: round(float(v), 3) for k, v in zip(_lib.KERNEL_CLASSES, kms)},
+           "gpu_launches_per_step": launches / steps, "clocks": clk.summary()}
+    # e2e through the drop-in entry point, pinned host buffers, flush between steps
+    Hp = torch.from_numpy(np.asfortranarray(H).ravel(order="F")).pin_memory()
+    Xp = torch.empty(n * n, dtype=torch.float64).pin_memory()
+    wp = torch.empty(n, dtype=torch.float64).pin_memory()
+    w0 = np.ascontiguousarray(wr)
+    lib.tiled_inverse_iteration.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                            C.c_int, C.c_int, C.c_void_p, C.c_int]
+    te = []
+    for it in range(args.warmup + steps):
+        wp.numpy()[:] = w0
+        flush.fill_(float(it))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lib.tiled_inverse_iteration(n, Hp.data_ptr(), n, n, wp.data_ptr(), tlsz, args.rhs_tlsz, Xp.data_ptr(), n)
+        te.append(time.perf_counter() - t0)
+        if lib.hsr_last_status() < 0:
+            raise RuntimeError("drop-in call failed")
+    te = float(np.mean(te[args.warmup:]))
+    out["e2e"] = {"value": n / te, "unit": UNIT, "ms_per_step": te * 1e3, "h2d_bytes_per_step": 8 * (n * n + n),
+                  "d2h_bytes_per_step": 8 * (n * n + n), "api": "tiled_inverse_iteration (C ABI, pinned host buffers)"}
+    info = hsr.inverse_iteration(H, wr, tlsz, args.rhs_tlsz, scaling="double")
+    dXc = torch.from_numpy(np.ascontiguousarray(info["vr"].T)).to(dev)
+    res = hsr.residuals_device(dHt, torch.from_numpy(info["wr"]).to(dev), dXc).cpu().numpy()
+    out["check"] = {"max_residual_all_columns": float(np.max(res)), "residual_bound_10n_eps": 10 * n * 2.0 ** -52,
+                    "perturbed_columns_device": int(np.sum(info["perturbed"])), "converged": int(np.sum(info["status"]))}
+    if not args.no_cpu_baseline:
+        v, t, c = cpu_sample(H, wr, tlsz, args.rhs_tlsz, n, 5, 1)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": c, "kind": "port",
+                               "sample": "n=%d, all %d shifts, mean of 5 solves (%.3f s each), tlsz=%d, rhs_tlsz=%d"
+                                         % (n, n, t, tlsz, args.rhs_tlsz),
+                               "perturbed_columns_reference_arithmetic": reference_perturbations(
+                                   H, wr, tlsz, args.rhs_tlsz, args.seed)}
+    out["config"] = {"workload": "plain small: n=%d, %d real shifts (eigenvalues, rel. 1e-12 noise), tlsz=%d"
+                                 % (n, n, tlsz), "n": n, "nrhs": n, "tlsz": tlsz, "rhs_tlsz": args.rhs_tlsz,
+                     "seed": args.seed, "l2": "inputs fit in L2: a 512 MB buffer is written between timed steps"}
+    return out
+
+
+def reference_perturbations(H, wr, tlsz, rhs_tlsz, seed):
+    """Columns whose 1x1 solves the reference arithmetic perturbs (the oracle's
+    "ref" build, bit-identical to the unmodified reference) at this tiling;
+    part of the CPU-baseline leg, computed once per host and cached."""
+    from oracle import pyoracle as O
+    n, S = H.shape[0], len(wr)
+    d = os.path.join(tempfile.gettempdir(), "hsrq3in_bench")
+    os.makedirs(d, exist_ok=True)
+    f = os.path.join(d, "ref_pert_n%d_S%d_s%d_t%d_r%d_v1.txt" % (n, S, seed, tlsz, rhs_tlsz))
+    if os.path.exists(f):
+        return int(open(f).read())
+    O.set_threads(os.cpu_count() or 1, "ref")
+    r = O.oracle_inverse_iteration(H, wr, tlsz, rhs_tlsz, variant="ref")
+    cnt = int(np.sum(r["perturbed"]))
+    with open(f, "w") as fh:
+        fh.write(str(cnt))
+    return cnt
+
+
 def run_batched(args):
     """Config 4: independent problems of mixed order in one graph launch."""
     import torch
@@ -436,6 +577,27 @@ def run_batched(args):
         got = tens[i][2][:, :H.shape[0]].cpu().numpy().T
         ok = ok and bool(np.array_equal(got, alone["vr"]))
     value = total_shifts / (ms / 1e3)
+    cpu = None
+    if not args.no_cpu_baseline:
+        # The reference looped over the problems (CPU port, all host cores),
+        # over a seeded sample of them within a bounded time.
+        from oracle import pyoracle as O
+        cores = os.cpu_count() or 1
+        O.set_threads(cores, variant="ref_fast")
+        order = np.random.default_rng(13).permutation(len(probs))
+        busy, shifts, cnt = 0.0, 0, 0
+        for i in order:
+            if busy > 15.0:
+                break
+            H, wr = probs[i]
+            t0 = time.perf_counter()
+            O.oracle_inverse_iteration(H, wr, tl, 64, variant="ref_fast")
+            busy += time.perf_counter() - t0
+            shifts += len(wr)
+            cnt += 1
+        cpu = {"value": shifts / busy, "unit": "eigenvectors/s", "cores": cores, "kind": "port",
+               "sample": "%d of the %d problems (seeded sample), one after another, tlsz %d, rhs_tlsz 64, %.1f s"
+                         % (cnt, len(probs), tl, busy)}
     return {"metric": "FP64 eigenvectors/s, batched mixed-size problems", "value": value,
             "unit": "eigenvectors/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -449,29 +611,60 @@ def run_batched(args):
             "plain_loop": {"eigenvectors_per_s": loop_rate, "sample_problems": int(len(idx)),
                            "speedup_batched_over_loop": value / loop_rate},
             "check": {"bitwise_equal_to_lone_solve_8_problems": ok},
+            "cpu_baseline": cpu,
             "clocks": clk.summary()}
 
 
-def served_pool(args):
-    """Distinct served matrices (n log-uniform [64, 4096], all eigenvalues),
-    generated once per host and cached in the temp directory."""
-    d = os.path.join(tempfile.gettempdir(), "hsrq3in_bench")
-    os.makedirs(d, exist_ok=True)
-    f = os.path.join(d, "served_pool_%d_s%d_v1.npz" % (args.pool, args.seed))
-    if os.path.exists(f):
-        z = np.load(f)
-        return [(np.asfortranarray(z["H%d" % i]), z["w%d" % i]) for i in range(args.pool)]
-    base = mixed_problems(args.pool, 64, 4096, 1.0, 1.0, args.seed + 1)
-    tmp = f + ".%d.tmp.npz" % os.getpid()
-    np.savez(tmp, **{("H%d" % i): H for i, (H, _) in enumerate(base)},
-             **{("w%d" % i): w for i, (_, w) in enumerate(base)})
-    os.replace(tmp, f)
-    return base
+def device_pool(count: int, nlo: int, nhi: int, seed: int):
+    """count distinct matrices of the real-spectrum generator, n log-uniform in
+    [nlo, nhi], generated on the GPU: T (jittered-grid diagonal, N(0,1) above)
+    drawn per matrix, A = P T P with P the Householder reflector mapping e1 to
+    a random unit vector, and A reduced to Hessenberg form by the library's
+    own hsr_hessenberg_device.  Returns [(H host Fortran array, eigenvalues)]
+    and the generation time in seconds."""
+    import torch
+    import hsrq3in_gb300 as hsr
+    from hsrq3in_gb300 import generators as G
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(seed)
+    ns = np.round(np.exp(rng.uniform(np.log(nlo), np.log(nhi), count))).astype(int)
+    t0 = time.perf_counter()
+    out = []
+    for i, n in enumerate(ns):
+        n = int(n)
+        r = np.random.default_rng(seed * 1000003 + i)
+        lam = G.jittered_eigenvalues(n, r)
+        g = torch.Generator(device=dev)
+        g.manual_seed(int(seed * 1000003 + i))
+        Tt = torch.triu(torch.randn((n, n), dtype=torch.float64, device=dev, generator=g), 1).T.contiguous()
+        Tt.diagonal().copy_(torch.from_numpy(lam).to(dev))       # Tt[c, r] = T[r, c]
+        q = torch.randn(n, dtype=torch.float64, device=dev, generator=g)
+        q /= torch.linalg.norm(q)
+        w = -q
+        w[0] += 1.0
+        w /= torch.linalg.norm(w)
+        T = Tt.T
+        Tw = T @ w
+        wT = Tt @ w
+        c = torch.dot(w, Tw)
+        A = T - 2.0 * torch.outer(w, wT) - 2.0 * torch.outer(Tw, w) + 4.0 * c * torch.outer(w, w)
+        ld = n + (n & 1)
+        dA = torch.zeros((n, ld), dtype=torch.float64, device=dev)
+        dA[:, :n] = A.T
+        del A, T, Tt
+        hsr.hessenberg_device(dA)
+        keep = torch.tril(torch.ones((n, n), dtype=torch.bool, device=dev), diagonal=1)   # rows r <= c+1
+        Ht = torch.where(keep, dA[:, :n], torch.zeros((), dtype=torch.float64, device=dev))
+        out.append((np.asfortranarray(Ht.T.cpu().numpy()), lam))
+    torch.cuda.synchronize()
+    return out, time.perf_counter() - t0
 
 
 def served_trace(args, base, nreq, rate, seed):
-    """Requests drawing a pool matrix and a random 10-100% subset of its
-    eigenvalues; Poisson arrivals at `rate` per second (rate 0: all at t=0)."""
+    """Requests with Poisson arrivals at `rate` per second (rate 0: all at
+    t=0).  Request i draws, from its own seed (seed, i), one of the generated
+    matrices and a random 10-100% subset of its eigenvalues as shifts, with
+    relative 1e-12 noise."""
     rng = np.random.default_rng(seed)
     if rate > 0:
         arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
@@ -480,11 +673,14 @@ def served_trace(args, base, nreq, rate, seed):
         arrivals = np.zeros(nreq)
     reqs = []
     for i in range(nreq):
-        j = int(rng.integers(len(base)))
+        r = np.random.default_rng([seed, i])
+        j = int(r.integers(len(base)))
         H, lam = base[j]
         n = H.shape[0]
-        m = max(1, int(round(n * rng.uniform(0.1, 1.0))))
-        reqs.append((j, n, np.sort(rng.choice(lam, size=m, replace=False)), float(arrivals[i])))
+        m = max(1, int(round(n * r.uniform(0.1, 1.0))))
+        wr = np.sort(r.choice(lam, size=m, replace=False))
+        wr = wr * (1.0 + 1e-12 * r.standard_normal(m))
+        reqs.append((j, n, wr, float(arrivals[i])))
     return reqs
 
 
@@ -553,28 +749,61 @@ def plain_served(base, reqs, tl, limit_s=12.0):
             "eigenvectors_per_s": shifts / wall}
 
 
+def cpu_served(base, reqs, tl, limit_s=20.0):
+    """The CPU baseline of the served trace: the oracle port (reference
+    arithmetic, all host cores) solving one request at a time in arrival
+    order on the same trace, latency including queueing, over the requests it
+    reaches in limit_s seconds of its own service time."""
+    from oracle import pyoracle as O
+    cores = os.cpu_count() or 1
+    O.set_threads(cores, variant="ref_fast")
+    clock = 0.0
+    lat, shifts, busy = [], 0, 0.0
+    for (j, n, wr, t) in reqs:
+        if busy > limit_s:
+            break
+        start = max(clock, t)
+        t0 = time.perf_counter()
+        O.oracle_inverse_iteration(base[j][0], wr, tl, 64, variant="ref_fast")
+        dt = time.perf_counter() - t0
+        busy += dt
+        clock = start + dt
+        lat.append(clock - t)
+        shifts += len(wr)
+    return {"requests": len(lat), "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "eigenvectors_per_s": shifts / busy, "cores": cores, "kind": "port",
+            "sample": "the first %d requests of the trace in arrival order (%.1f s of service time)"
+                      % (len(lat), busy)}
+
+
 def run_served(args):
-    """Config 5: a Poisson trace through the request loop (latency at the
-    configured rate), and the same request mix arriving at once (capacity);
-    each against the plain path run per request."""
-    base = served_pool(args)
+    """The served workload: a Poisson trace of `requests` requests through
+    the request loop (latency at the configured rate) and the first
+    `saturate` of them arriving at once (capacity); each against the plain
+    device path run per request and the CPU port per request."""
+    base, gen_s = device_pool(args.pool, 64, 4096, args.seed + 1)
     tl = args.batch_tlsz or 64
     with ClockSampler(0) as clk:
         paced = served_trace(args, base, args.requests, args.rate, args.seed + 2)
         r_paced = replay_served(base, paced, tl, args.budget_gb)
-        burst = served_trace(args, base, args.requests, 0.0, args.seed + 3)
+        burst = [(j, n, wr, 0.0) for (j, n, wr, _) in paced[:args.saturate]]
         r_burst = replay_served(base, burst, tl, args.budget_gb)
     p_paced = plain_served(base, paced, tl)
     p_burst = plain_served(base, burst, tl)
-    return {"paced": {"rate_per_s": args.rate, "server": r_paced, "plain_per_request": p_paced},
-            "saturated": {"server": r_burst, "plain_per_request": p_burst,
-                          "speedup_server_over_plain": r_burst["eigenvectors_per_s"] / p_burst["eigenvectors_per_s"]},
-            "config": "%d requests, n log-uniform [64,4096] from %d distinct generated matrices, shift fraction "
-                      "U[0.1,1], HBM budget %.0f GB, tlsz %d%s" % (
-                          args.requests, len(base), args.budget_gb, tl,
-                          "; outputs on one matrix share a host buffer" if args.requests > SHARED_OUTPUT_ABOVE
-                          else ""),
-            "clocks": clk.summary()}
+    out = {"paced": {"rate_per_s": args.rate, "server": r_paced, "plain_per_request": p_paced},
+           "saturated": {"server": r_burst, "plain_per_request": p_burst,
+                         "speedup_server_over_plain": r_burst["eigenvectors_per_s"] / p_burst["eigenvectors_per_s"]},
+           "config": "%d requests (Poisson, %.0f/s), each seeded per request: n log-uniform [64,4096] through one "
+                     "of %d matrices generated on the device (hsr_hessenberg_device, %.1f s), a U[0.1,1] fraction "
+                     "of its eigenvalues with rel. 1e-12 noise; HBM budget %.0f GB, tlsz %d; capacity from the first "
+                     "%d requests arriving at once%s" % (
+                         args.requests, args.rate, len(base), gen_s, args.budget_gb, tl, len(burst),
+                         "; outputs on one matrix share a host buffer" if args.requests > SHARED_OUTPUT_ABOVE
+                         else ""),
+           "clocks": clk.summary()}
+    if not args.no_cpu_baseline:
+        out["paced"]["cpu_baseline_per_request"] = cpu_served(base, paced, tl)
+    return out
 
 
 def run_stress(args):
@@ -972,8 +1201,7 @@ def main():
         dist.init_process_group(backend=backend)
     n = args.order
     S = args.nrhs or n
-    cores = os.cpu_count() or 1
-    sample = args.cpu_sample or min(S, 64 * cores)
+    sample = args.cpu_sample or S
     config = {"workload": "plain large: n=%d, %d real shifts (eigenvalues, rel. 1e-12 noise), tlsz=%d"
                           % (n, S, args.tlsz),
               "n": n, "nrhs": S, "tlsz": args.tlsz, "rhs_tlsz": args.rhs_tlsz, "seed": args.seed,
@@ -992,9 +1220,9 @@ def main():
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)", "config": config,
                 "impl": "reference",
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": c, "kind": "port",
-                                 "sample": "n=%d, first %d of %d shifts per step, tlsz=%d, rhs_tlsz=%d; the C "
-                                           "restatement of the reference (reference sources are not on this "
-                                           "host)" % (n, sample, S, args.tlsz, args.rhs_tlsz)},
+                                 "sample": "n=%d, %d of %d shifts per step (one whole solve), tlsz=%d, "
+                                           "rhs_tlsz=%d; the C restatement of the reference (reference sources "
+                                           "are not on this host)" % (n, sample, S, args.tlsz, args.rhs_tlsz)},
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -1010,19 +1238,40 @@ def main():
               "whole_solve_tflops_2n2S", "whole_solve_frac", "check"):
         if k in g:
             line[k] = g[k]
+    if rank == 0 and world == 1 and n == 10000:
+        # perturbed columns of the device at this tiling (host call, outside the timed region)
+        import hsrq3in_gb300 as hsr
+        info = hsr.inverse_iteration(H, wr, args.tlsz, args.rhs_tlsz, scaling="double")
+        line["check"]["perturbed_columns_device"] = int(np.sum(info["perturbed"]))
+        line["check"]["converged"] = int(np.sum(info["status"]))
+        del info
     if rank == 0 and world == 1 and not args.only_plain:
+        sub = argparse.Namespace(**vars(args))
+        sub.steps, sub.warmup = min(args.steps, 5), min(args.warmup, 3)
+        line["plain_small"] = run_plain_small(args, SMALL_TLSZ)
         b = run_batched(args)
         line["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "solves_per_s", "whole_tflops_2n2S",
-                                              "frac_of_fp64_peak", "plain_loop", "check")}
+                                              "frac_of_fp64_peak", "plain_loop", "check", "cpu_baseline")}
         line["batched"]["config"] = b["config"]
         sv = run_served(args)
         line["served"] = sv
-        line["stress"] = run_stress(args)
+        line["stress"] = run_stress(sub)
+        cx = run_complex(sub)
+        line["complex"] = {k: cx[k] for k in ("value", "unit", "ms_per_step", "pairs_per_s", "whole_tflops_2n2S",
+                                              "roofline", "e2e", "cpu_baseline", "check", "config", "clocks")
+                           if k in cx}
+        line["complex"]["steps"], line["complex"]["warmup"] = sub.steps, sub.warmup
+        hh = run_hessenberg(sub)
+        hh["steps"], hh["warmup"] = sub.steps, sub.warmup
+        line["hessenberg"] = hh
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, t, c = cpu_sample(H, wr, args.tlsz, args.rhs_tlsz, sample, 1, 0)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": c, "kind": "port",
-                                "sample": "n=%d, first %d of %d shifts, one solve (%.1f s), tlsz=%d, rhs_tlsz=%d"
+                                "sample": "n=%d, %d of %d shifts, one solve (%.1f s), tlsz=%d, rhs_tlsz=%d"
                                           % (n, sample, S, t, args.tlsz, args.rhs_tlsz)}
+        if sample == S:
+            line["cpu_baseline"]["perturbed_columns_reference_arithmetic"] = reference_perturbations(
+                H, wr, args.tlsz, args.rhs_tlsz, args.seed)
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -19,6 +19,8 @@ HSR_ERR_DEVICE = -4
 HSR_ERR_NOT_CONVERGED = 1
 HSR_SCALING_POW2 = 0
 HSR_SCALING_DOUBLE = 1
+HSR_BATCH_ENGINE_TICKS = 0
+HSR_BATCH_ENGINE_QUEUE = 1
 
 # Every symbol include/hsrq3in_gb300.h declares.
 EXPORTS = [
@@ -29,6 +31,7 @@ EXPORTS = [
     "hsr_inverse_iteration_noalloc", "hsr_residuals_device",
     "hsr_hessenberg_device", "hsr_hessenberg_apply_q_device",
     "hsr_batch_plan_create", "hsr_batch_plan_execute", "hsr_batch_plan_info", "hsr_batch_plan_destroy",
+    "hsr_batch_plan_set_engine", "hsr_batch_plan_queue_info",
     "hsr_autotune_tlsz", "hsr_autotune_batch",
     "hsr_server_create", "hsr_server_replay", "hsr_server_destroy",
     "hsr_inverse_iteration_cplx_ex", "hsr_inverse_iteration_cplx_device", "hsr_inverse_iteration_mixed",
@@ -145,6 +148,11 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     lib.hsr_batch_plan_execute.argtypes = [C.c_void_p, C.c_void_p]
     lib.hsr_batch_plan_info.restype = C.c_int
     lib.hsr_batch_plan_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_long)]
+    lib.hsr_batch_plan_set_engine.restype = C.c_int
+    lib.hsr_batch_plan_set_engine.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    lib.hsr_batch_plan_queue_info.restype = C.c_int
+    lib.hsr_batch_plan_queue_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_long),
+                                              C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.hsr_batch_plan_destroy.restype = None
     lib.hsr_batch_plan_destroy.argtypes = [C.c_void_p]
     lib.hsr_autotune_tlsz.restype = C.c_int

@@ -247,9 +247,11 @@ class BatchPlan:
 
     problems: list of (dH, dwr, dvr) torch tensors on the device, where dH and
     dvr are column-major views (tensors of shape (cols, ld) holding columns as
-    rows).  tlsz=0 uses the autotuned tile size."""
+    rows).  tlsz=0 uses the autotuned tile size.  engine: "ticks" (a graph of
+    per-phase launches, all problems in lock step) or "queue" (one persistent
+    launch over a device work queue with per-problem dependencies)."""
 
-    def __init__(self, problems, tlsz: int = 0, scaling: str = "pow2", stream=None):
+    def __init__(self, problems, tlsz: int = 0, scaling: str = "pow2", stream=None, engine: str = "ticks"):
         lib = _lib.load()
         self._lib = lib
         self._keep = problems
@@ -267,6 +269,20 @@ class BatchPlan:
         if rc != 0:
             raise HsrError(rc)
         self._h = h
+        self.set_engine(engine)
+
+    def set_engine(self, engine: str):
+        code = {"ticks": _lib.HSR_BATCH_ENGINE_TICKS, "queue": _lib.HSR_BATCH_ENGINE_QUEUE}[engine]
+        rc = self._lib.hsr_batch_plan_set_engine(self._h, code, None if self._stream is None
+                                                 else C.c_void_p(self._stream.cuda_stream))
+        if rc != 0:
+            raise HsrError(rc)
+
+    def queue_info(self):
+        e, it, g, dw, ig = C.c_int(), C.c_long(), C.c_int(), C.c_int(), C.c_int()
+        self._lib.hsr_batch_plan_queue_info(self._h, C.byref(e), C.byref(it), C.byref(g), C.byref(dw), C.byref(ig))
+        return dict(engine="queue" if e.value == _lib.HSR_BATCH_ENGINE_QUEUE else "ticks", items=it.value,
+                    grid=g.value, diag_warps=dw.value, in_graph=bool(ig.value))
 
     def execute(self) -> int:
         rc = self._lib.hsr_batch_plan_execute(self._h, None if self._stream is None

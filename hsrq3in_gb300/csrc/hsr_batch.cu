@@ -338,7 +338,22 @@ struct hsr_batch_plan {
     std::vector<size_t> status_off;           // first column of each problem in d_status
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    // Persistent-queue engine (built on first use).
+    int engine = HSR_BATCH_ENGINE_TICKS;
+    std::vector<std::vector<int>> frs;
+    QueueItem *d_qitems = nullptr;
+    int n_qitems = 0;
+    int *d_ctr = nullptr;      // counters, then the ticket
+    size_t n_ctr = 0;
+    int qgrid = 0, qdiag_warps = 0;
+    bool qdirect = false;      // the cooperative launch could not be captured
+    cudaGraph_t qgraph = nullptr;
+    cudaGraphExec_t qexec = nullptr;
     ~hsr_batch_plan() {
+        if (qexec) cudaGraphExecDestroy(qexec);
+        if (qgraph) cudaGraphDestroy(qgraph);
+        if (d_qitems) cudaFree(d_qitems);
+        if (d_ctr) cudaFree(d_ctr);
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         if (pool) cudaFree(pool);
@@ -448,6 +463,7 @@ extern "C" int hsr_batch_plan_create(hsr_batch_plan **out, int nprob, const hsr_
             }
         }
         partition_rows(L.n, L.T, b, frs[i]);
+        pl->frs.push_back(frs[i]);
         BP_CK(cudaMemcpyAsync(base + L.fr, frs[i].data(), (L.T + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
         pl->status_off.push_back(ncols);
         ncols += (size_t)probs[i].nrhs;
@@ -536,10 +552,17 @@ extern "C" int hsr_batch_plan_create(hsr_batch_plan **out, int nprob, const hsr_
     return HSR_OK;
 }
 
+static cudaError_t queue_direct(hsr_batch_plan *pl, cudaStream_t st);
+
 extern "C" int hsr_batch_plan_execute(hsr_batch_plan *pl, void *stream) {
     if (!pl) return HSR_ERR_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (cudaGraphLaunch(pl->exec, st) != cudaSuccess) return HSR_ERR_CUDA;
+    if (pl->engine == HSR_BATCH_ENGINE_QUEUE) {
+        const cudaError_t e = pl->qdirect ? queue_direct(pl, st) : cudaGraphLaunch(pl->qexec, st);
+        if (e != cudaSuccess) return record_status(HSR_ERR_CUDA, e);
+    } else if (cudaGraphLaunch(pl->exec, st) != cudaSuccess) {
+        return HSR_ERR_CUDA;
+    }
     // Convergence: status of every column of every problem.
     int result = HSR_OK;
     int errw = 0;
@@ -567,6 +590,212 @@ extern "C" int hsr_batch_plan_execute(hsr_batch_plan *pl, void *stream) {
         if (rc == HSR_ERR_NOT_CONVERGED) result = HSR_ERR_NOT_CONVERGED;
     }
     return result;
+}
+
+// ------------------------------------------------------- queue engine
+namespace {
+
+// Counters of problem i start at base[i]: four fixed ones (norms, init,
+// finalize, normalize), then four per stage J (diagonal solve of tile J,
+// part 1, GEMM over the rows of tile J-1, GEMM over the rows above).
+enum { qcNorms = 0, qcInit, qcFinal, qcNormalize, qcFixed };
+inline int qc_stage(int J, int which) { return qcFixed + 4 * J + which; }
+enum { qsDiag = 0, qsPart1, qsTop, qsRest };
+
+// The work list of the queue engine: the ticks of the graph engine, in the
+// order the graph launches them, with every item's dependencies on the
+// counters of its own problem.  Initial vectors, diagonal solves and
+// finalisation are grouped (a warp per column or 32-shift block) so that an
+// item uses the CTA.
+void build_queue(const hsr_batch_plan *pl, int dw, std::vector<QueueItem> &out, std::vector<int> &base,
+                 size_t &n_ctr) {
+    const int nprob = pl->nprob;
+    base.assign(nprob, 0);
+    n_ctr = 0;
+    for (int i = 0; i < nprob; ++i) {
+        base[i] = (int)n_ctr;
+        n_ctr += qcFixed + 4 * (size_t)pl->layouts[i].T;
+    }
+    auto item = [](int x, int y, int z, int w, int kind, int ctr, int d0, int t0, int d1 = -1, int t1 = 0) {
+        QueueItem q{};
+        q.it = make_int4(x, y, z, w);
+        q.kind = kind;
+        q.ctr = ctr;
+        q.dep0 = d0;
+        q.tgt0 = t0;
+        q.dep1 = d1;
+        q.tgt1 = t1;
+        return q;
+    };
+    struct Counts {
+        int norms, init, diag, part1, fin, cbs;
+    };
+    std::vector<Counts> cnt(nprob);
+    auto top_rows = [&](int i, int J) {
+        const std::vector<int> &fr = pl->frs[i];
+        return (fr[J] - (fr[J - 1] & ~7) + kGemmBM - 1) / kGemmBM;
+    };
+    auto rest_rows = [&](int i, int J) { return (pl->frs[i][J - 1] + kGemmBM - 1) / kGemmBM; };
+    for (int i = 0; i < nprob; ++i) {
+        const Layout &L = pl->layouts[i];
+        const int sb32 = (L.S + 31) / 32;
+        cnt[i] = Counts{(L.n + kNormRows - 1) / kNormRows, (L.S + kQueueInitCols - 1) / kQueueInitCols,
+                        (sb32 + dw - 1) / dw, (L.S + kPart1Shifts - 1) / kPart1Shifts,
+                        (sb32 + kQueueFinalBlocks - 1) / kQueueFinalBlocks, (L.S + kGemmBN - 1) / kGemmBN};
+    }
+    std::vector<QueueItem> ph[phCount];
+    auto flush = [&]() {
+        for (auto &v : ph) {
+            out.insert(out.end(), v.begin(), v.end());
+            v.clear();
+        }
+    };
+    std::vector<int> stage(nprob, -1);
+    int live = 0;
+    for (int i = 0; i < nprob; ++i) {
+        const Layout &L = pl->layouts[i];
+        if (L.S == 0) continue;
+        const int b0 = base[i], J = L.T - 1;
+        for (int r = 0; r < cnt[i].norms; ++r)
+            ph[phNorms].push_back(item(desc(i, 0), 0, r, 0, qkNorms, b0 + qcNorms, -1, 0));
+        for (int g = 0; g < cnt[i].init; ++g)
+            ph[phInit].push_back(item(desc(i, 0), 0, g, 0, qkInit, b0 + qcInit, b0 + qcNorms, cnt[i].norms));
+        for (int g = 0; g < cnt[i].diag; ++g)
+            ph[phDiagFirst].push_back(item(desc(i, J), J, g, 0, qkDiag, b0 + qc_stage(J, qsDiag), b0 + qcInit,
+                                           cnt[i].init));
+        stage[i] = J;
+        ++live;
+    }
+    while (live > 0) {
+        for (int i = 0; i < nprob; ++i) {
+            const int J = stage[i];
+            if (J < 0) continue;
+            const Layout &L = pl->layouts[i];
+            const int b0 = base[i];
+            const Counts &c = cnt[i];
+            if (J >= 1) {
+                const int p = desc(i, J), pn = desc(i, J - 1);
+                const int ntop = top_rows(i, J) * c.cbs;
+                const int nrest = rest_rows(i, J) * c.cbs;
+                const int prev_rest = J + 1 <= L.T - 1 ? rest_rows(i, J + 1) * c.cbs : 0;
+                for (int x = 0; x < c.part1; ++x)
+                    ph[phPart1].push_back(item(p, J, x, 0, qkPart1, b0 + qc_stage(J, qsPart1),
+                                               b0 + qc_stage(J, qsDiag), c.diag,
+                                               prev_rest > 0 ? b0 + qc_stage(J + 1, qsRest) : -1, prev_rest));
+                for (int r = 0; r < top_rows(i, J); ++r)
+                    for (int cb = 0; cb < c.cbs; ++cb)
+                        ph[phGemmTop].push_back(item(p, J, r | kGemmTopFlag, cb, qkGemm, b0 + qc_stage(J, qsTop),
+                                                     b0 + qc_stage(J, qsPart1), c.part1));
+                for (int g = 0; g < c.diag; ++g)
+                    ph[phDiagNext].push_back(item(pn, J - 1, g, 0, qkDiag, b0 + qc_stage(J - 1, qsDiag),
+                                                  b0 + qc_stage(J, qsTop), ntop));
+                for (int r = 0; r < rest_rows(i, J); ++r)
+                    for (int cb = 0; cb < c.cbs; ++cb)
+                        ph[phGemmRest].push_back(item(p, J, r, cb, qkGemm, b0 + qc_stage(J, qsRest),
+                                                      b0 + qc_stage(J, qsPart1), c.part1));
+                (void)nrest;
+            }
+            if (J <= 1) {
+                for (int g = 0; g < c.fin; ++g)
+                    ph[phFinal].push_back(item(desc(i, 0), 0, g, 0, qkFinal, b0 + qcFinal, b0 + qc_stage(0, qsDiag),
+                                               c.diag));
+                const int nn = (L.S + kNormalizeCols - 1) / kNormalizeCols;
+                for (int x = 0; x < nn; ++x)
+                    ph[phNormalize].push_back(item(desc(i, 0), 0, x, 0, qkNormalize, b0 + qcNormalize,
+                                                   b0 + qcFinal, c.fin));
+                stage[i] = -1;
+                --live;
+            } else {
+                stage[i] = J - 1;
+            }
+        }
+        flush();
+    }
+    flush();
+}
+
+}  // namespace
+
+// Builds the queue engine's work list, counters and graph (once per plan).
+static int build_queue_engine(hsr_batch_plan *pl, cudaStream_t st) {
+    if (pl->qexec || pl->qdirect) return HSR_OK;
+    const int dw = queue_diag_warps(pl->b);
+    std::vector<QueueItem> items;
+    std::vector<int> base;
+    size_t n_ctr = 0;
+    build_queue(pl, dw, items, base, n_ctr);
+    const int grid = queue_max_grid(pl->b);
+    if (grid <= 0) return HSR_ERR_CUDA;
+    if (cudaMalloc(&pl->d_qitems, sizeof(QueueItem) * std::max<size_t>(items.size(), 1)) != cudaSuccess ||
+        cudaMalloc(&pl->d_ctr, sizeof(int) * (n_ctr + 32)) != cudaSuccess)
+        return HSR_ERR_NOMEM;
+    if (!items.empty() &&
+        cudaMemcpyAsync(pl->d_qitems, items.data(), sizeof(QueueItem) * items.size(), cudaMemcpyHostToDevice,
+                        st) != cudaSuccess)
+        return HSR_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return HSR_ERR_CUDA;
+    pl->n_qitems = (int)items.size();
+    pl->n_ctr = n_ctr;
+    pl->qgrid = grid;
+    pl->qdiag_warps = dw;
+    int *ticket = pl->d_ctr + n_ctr;
+    // One graph: zero the accumulators, counters, ticket and error word, then
+    // the single persistent launch.
+    cudaStream_t cap = nullptr;
+    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return HSR_ERR_CUDA;
+    bool ok = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    const bool capturing = ok;
+    if (ok) ok = cudaMemsetAsync(pl->pool, 0, std::max<size_t>(pl->zero_bytes, 1), cap) == cudaSuccess;
+    if (ok) ok = cudaMemsetAsync(pl->d_err, 0, 16, cap) == cudaSuccess;
+    if (ok) ok = cudaMemsetAsync(pl->d_ctr, 0, sizeof(int) * (n_ctr + 32), cap) == cudaSuccess;
+    if (ok)
+        ok = launch_queue(pl->d_probs, pl->d_qitems, pl->n_qitems, pl->d_maps, pl->d_ctr, ticket, pl->d_err, pl->b,
+                          grid, cap) == cudaSuccess;
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = capturing ? cudaStreamEndCapture(cap, &g) : cudaErrorInvalidValue;
+    cudaStreamDestroy(cap);
+    if (ok && ce == cudaSuccess && cudaGraphInstantiate(&pl->qexec, g, 0) == cudaSuccess) {
+        pl->qgraph = g;
+        return HSR_OK;
+    }
+    // A runtime that cannot capture the cooperative launch: the same memsets
+    // and launch are issued directly by every execute.
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    pl->qexec = nullptr;
+    pl->qdirect = true;
+    return HSR_OK;
+}
+
+static cudaError_t queue_direct(hsr_batch_plan *pl, cudaStream_t st) {
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(pl->pool, 0, std::max<size_t>(pl->zero_bytes, 1), st)) != cudaSuccess ||
+        (e = cudaMemsetAsync(pl->d_err, 0, 16, st)) != cudaSuccess ||
+        (e = cudaMemsetAsync(pl->d_ctr, 0, sizeof(int) * (pl->n_ctr + 32), st)) != cudaSuccess)
+        return e;
+    return launch_queue(pl->d_probs, pl->d_qitems, pl->n_qitems, pl->d_maps, pl->d_ctr, pl->d_ctr + pl->n_ctr,
+                        pl->d_err, pl->b, pl->qgrid, st);
+}
+
+extern "C" int hsr_batch_plan_set_engine(hsr_batch_plan *pl, int engine, void *stream) {
+    if (!pl || (engine != HSR_BATCH_ENGINE_TICKS && engine != HSR_BATCH_ENGINE_QUEUE)) return HSR_ERR_ARG;
+    if (engine == HSR_BATCH_ENGINE_QUEUE) {
+        const int rc = build_queue_engine(pl, static_cast<cudaStream_t>(stream));
+        if (rc) return rc;
+    }
+    pl->engine = engine;
+    return HSR_OK;
+}
+
+extern "C" int hsr_batch_plan_queue_info(const hsr_batch_plan *pl, int *engine, long *items, int *grid,
+                                         int *diag_warps, int *in_graph) {
+    if (!pl) return HSR_ERR_ARG;
+    if (in_graph) *in_graph = pl->qexec != nullptr;
+    if (engine) *engine = pl->engine;
+    if (items) *items = pl->n_qitems;
+    if (grid) *grid = pl->qgrid;
+    if (diag_warps) *diag_warps = pl->qdiag_warps;
+    return HSR_OK;
 }
 
 extern "C" int hsr_batch_plan_info(const hsr_batch_plan *pl, int *tlsz, int *ticks, long *launches) {

@@ -16,6 +16,7 @@ namespace hsr {
 enum : int {
     kErrWaitTimeout = 1,   // an mbarrier wait gave up
     kErrShape = 2,         // a kernel was launched with an impossible shape
+    kErrQueueTimeout = 4,  // a work-queue item gave up waiting for its dependencies
 };
 
 // Overflow threshold Omega and its reciprocal (robust.c:14-15).
@@ -430,6 +431,19 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, u
         "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
         ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
         : "memory");
+}
+// Invalidate an mbarrier whose memory is about to serve another purpose.
+__device__ __forceinline__ void mbar_inval(uint64_t *bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// Order earlier generic-proxy accesses before later async-proxy (TMA) ones:
+// shared memory the CTA wrote itself, and global memory written by other
+// CTAs whose completion this thread has observed.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_global() {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
 }
 __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap *map) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");

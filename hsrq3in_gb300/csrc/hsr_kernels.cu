@@ -25,6 +25,7 @@
 #include "hsr_kernels.h"
 
 #include <cfloat>
+#include <cstdlib>
 #include <mutex>
 
 namespace hsr {
@@ -839,6 +840,389 @@ __device__ __forceinline__ void diag_body_pipe(const DevProblem &P, int J, int b
 }
 
 
+// Narrow form of the pipelined body for solves with few shifts: SC (< 32)
+// shifts per CTA, so that a small shift count still spreads over many SMs.
+// The scalar chain of each step runs on warp 0, lane s (and its duplicates
+// s + SC, s + 2 SC, ..., which compute the same values and store nothing);
+// the row warps 1 .. NW-1 hold RL = 32 / SC rows x SC shifts per
+// instruction, so a step's vector work takes RL times fewer instructions than
+// with a lane per shift.  Every (row, shift) element sees the same operations
+// in the same order as in diag_body_pipe, and the maxima cover the same rows
+// (a maximum does not depend on the order it is taken in), so the result is
+// bit-identical to the wide form.  v/y live in shared memory as [row][SC].
+template <int SC>
+__host__ __device__ constexpr size_t diag_narrow_smem_bytes(int b, int nw) {
+    return (size_t)(3 * (b + 1) + nw * 2 * SC + kDiagBcast * SC + 2 * SC * b) * sizeof(double);
+}
+
+template <int SC, int NW>
+__device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int bx) {
+    static_assert(32 % SC == 0 && SC >= 4 && SC < 32, "shifts per CTA");
+    constexpr int RL = 32 / SC;                                               // rows per row-warp instruction
+    constexpr int NR = NW - 1;                                                // row warps
+    extern __shared__ double sm[];
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int wid = tid >> 5;
+    const int sh = lane % SC;                                                 // shift slot
+    const int rs = lane / SC;                                                 // row slot (row warps)
+    const bool store_lane = lane < SC;                                        // chain results are stored once
+    const int k0 = bx * SC;
+    const int k = k0 + sh;
+    const bool act = k < P.S;
+    const int l = P.fr[J], b = P.fr[J + 1] - l;
+    const bool is = P.is != 0;
+    const size_t Spad = (size_t)P.Spad;
+
+    double *hc = sm;                                                          // [3][b+1]
+    unsigned long long *pm = reinterpret_cast<unsigned long long *>(sm + 3 * (b + 1));   // [NW][2][SC]
+    double *bc = sm + 3 * (b + 1) + NW * 2 * SC;                              // [kDiagBcast][SC]
+    double *v = bc + kDiagBcast * SC;                                         // [b][SC]
+    double *y = v + (size_t)SC * b;                                           // [b][SC]
+#define V(i) v[(size_t)(i) * SC + sh]
+#define Y(i) y[(size_t)(i) * SC + sh]
+#define PM(w, which) pm[(((w) * 2) + (which)) * SC + sh]
+#define BC(q) bc[(q) * SC + sh]
+#define HCOL(col) (hc + (size_t)((col) % 3) * (b + 1))
+
+    for (int idx = tid; idx < SC * b; idx += 32 * NW) {
+        const int c = idx / b, i = idx - c * b;
+        const int kc = k0 + c;
+        if (kc < P.S) {
+            v[(size_t)i * SC + c] = P.R[l + i + (size_t)kc * P.ldr];
+            y[(size_t)i * SC + c] = P.X[l + i + (size_t)kc * P.ldx];
+        } else {
+            v[(size_t)i * SC + c] = 1.0;
+            y[(size_t)i * SC + c] = 0.0;
+        }
+    }
+
+    const double mu = act ? P.wr[k] : 0.0;
+    const double smin = fmax(DBL_EPSILON / 2 * fabs(mu), P.smlnum);
+    const double Hnorm = P.Hn[J + (size_t)J * P.T];
+    double beta = act ? P.beta[(size_t)J * Spad + k] : sc_one(is);
+    int pert = 0;
+
+    const double *Hd = P.H + l + (size_t)l * P.ldh;                           // H(l, l)
+    auto stage_col = [&](int col) {                                           // H(l : l+col+1, l+col), warp 0
+        int rows = col + 2;
+        if (rows > b) rows = b;
+        const double *src = Hd + (size_t)col * P.ldh;
+        double *dst = HCOL(col);
+        for (int i = lane; i < rows; i += 32) cp_async8(dst + i, src + i);
+        cp_async_commit();
+    };
+    if (wid == 0 && b >= 2) stage_col(b - 2);
+    if (wid == 0 && b >= 3) stage_col(b - 3);
+    if (wid == 0) cp_async_wait_all();
+    __syncthreads();                                                          // tiles and columns loaded
+
+    // Maxima over the RL row slots of one shift (lanes sh, sh + SC, ...).
+    auto slot_max = [&](unsigned long long m) {
+#pragma unroll
+        for (int o = SC; o < 32; o <<= 1) m = umax64(m, __shfl_xor_sync(0xffffffffu, m, o));
+        return m;
+    };
+    // Maxima of |y(0:b-3)| and |v(0:b-3)| for the first step, by the row warps.
+    {
+        unsigned long long ym = 0, vm = 0;
+        if (wid > 0)
+            for (int i = (wid - 1) * RL + rs; i < b - 2; i += NR * RL) {
+                ym = umax64(ym, abs_bits(Y(i)));
+                vm = umax64(vm, abs_bits(V(i)));
+            }
+        ym = slot_max(ym);
+        vm = slot_max(vm);
+        if (store_lane) {
+            PM(wid, 0) = ym;
+            PM(wid, 1) = vm;
+        }
+    }
+
+    // Chain state of warp 0.
+    double vcar = V(b - 1), ycar = Y(b - 1);
+    double c = 0.0, s = 0.0, yc = 0.0, ys = 0.0, a1 = 1.0, a2 = 1.0, a3 = 1.0, yj = 0.0, yjm1 = 0.0;
+
+    auto chain12 = [&](int jj, double vjm1, double yjm1_in) {
+        const double *hcol = HCOL(jj - 1);
+        const double hsub = hcol[jj];
+        const double hdiag = hcol[jj - 1] - mu;
+        const double vj = vcar;
+        yj = ycar;
+        yjm1 = yjm1_in;
+        givens(vj, hsub, c, s);
+        if (act && store_lane) {
+            P.Cr[(size_t)(l + jj) * Spad + k] = c;
+            P.Sr[(size_t)(l + jj) * Spad + k] = s;
+        }
+        double phi = sc_one(is);
+        pert |= solve_1x1(smin, c * vj, s * hsub, yj, phi, is);
+        beta = sc_combine(beta, phi, is);
+        a1 = sc_value(phi, is);
+        if (!is_one(a1)) yjm1 = a1 * yjm1;
+        phi = protect_double_update(fabs(vjm1), fabs(yj), fabs(hdiag), fabs(yj), fabs(yjm1), is);
+        a2 = sc_value(phi, is);
+        if (!is_one(a2)) {
+            yj = a2 * yj;
+            yjm1 = a2 * yjm1;
+        }
+        beta = sc_combine(beta, phi, is);
+        yc = yj * c;
+        ys = yj * s;
+        yjm1 = fma(ys, hdiag, fma(-yc, vjm1, yjm1));
+        vcar = fma(c, hdiag, s * vjm1);
+    };
+    auto chain3 = [&](int jj) {
+        unsigned long long ymb = 0, vmb = 0;
+#pragma unroll
+        for (int w = 1; w < NW; ++w) {
+            ymb = umax64(ymb, PM(w, 0));
+            vmb = umax64(vmb, PM(w, 1));
+        }
+        double ymax = from_bits(ymb);
+        if (!is_one(a1)) ymax = from_bits(abs_bits(a1 * ymax));
+        if (!is_one(a2)) ymax = from_bits(abs_bits(a2 * ymax));
+        const double phi = protect_double_update(from_bits(vmb), fabs(yj), Hnorm, fabs(yj), ymax, is);
+        a3 = sc_value(phi, is);
+        if (!is_one(a3)) {
+            yj = a3 * yj;
+            yjm1 = a3 * yjm1;
+            yc = yj * c;
+            ys = yj * s;
+        }
+        beta = sc_combine(beta, phi, is);
+        if (store_lane) {
+            BC(0) = c;
+            BC(1) = s;
+            BC(2) = yc;
+            BC(3) = ys;
+            BC(4) = a1;
+            BC(5) = a2;
+            BC(6) = a3;
+            Y(jj) = yj;
+        }
+        ycar = yjm1;
+    };
+
+    if (wid == 0 && b >= 2) chain12(b - 1, V(b - 2), Y(b - 2));
+    __syncthreads();                                                          // first maxima in
+    if (wid == 0 && b >= 2) chain3(b - 1);
+    __syncthreads();                                                          // step b-1's scalars visible
+
+    for (int j = b - 1; j >= 1; --j) {
+        double sc_c = c, sc_s = s, sc_yc = yc, sc_ys = ys, s1 = a1, s2 = a2, s3 = a3;
+        if (wid != 0) {
+            sc_c = BC(0);
+            sc_s = BC(1);
+            sc_yc = BC(2);
+            sc_ys = BC(3);
+            s1 = BC(4);
+            s2 = BC(5);
+            s3 = BC(6);
+        }
+        const bool scaled = (!is_one(s1)) || (!is_one(s2)) || (!is_one(s3));
+        const double *hcol = HCOL(j - 1);
+        if (wid == 0) {
+            // Row j-2 first: it enters step j-1's chain.
+            double vn = 0.0, yn = 0.0;
+            if (j >= 2) {
+                const double h = hcol[j - 2];
+                double yi = Y(j - 2);
+                const double vi = V(j - 2);
+                if (scaled) {
+                    if (!is_one(s1)) yi = s1 * yi;
+                    if (!is_one(s2)) yi = s2 * yi;
+                    if (!is_one(s3)) yi = s3 * yi;
+                }
+                yn = fma(sc_ys, h, fma(-sc_yc, vi, yi));
+                vn = fma(sc_c, h, sc_s * vi);
+                __syncwarp();                                                 // every lane read row j-2
+                if (store_lane) {
+                    Y(j - 2) = yn;
+                    V(j - 2) = vn;
+                }
+            }
+            if (j >= 2) {
+                cp_async_wait_all();                                          // column j-2, staged last step
+                __syncwarp();                                                 // ... by all lanes of warp 0
+                chain12(j - 1, vn, yn);
+            }
+            if (j >= 3) stage_col(j - 3);                                     // for step j-2's chain
+        } else {
+            if (scaled) {
+                for (int i = j + 1 + (wid - 1) * RL + rs; i < b; i += NR * RL) {
+                    double t = Y(i);
+                    if (!is_one(s1)) t = s1 * t;
+                    if (!is_one(s2)) t = s2 * t;
+                    if (!is_one(s3)) t = s3 * t;
+                    Y(i) = t;
+                }
+            }
+            unsigned long long ymx = 0, vmx = 0;
+            const int lim = j - 2;                                            // rows 0 .. j-3
+            int i = (wid - 1) * RL + rs;
+            constexpr int ST = NR * RL;                                       // row stride of one lane
+            for (; i + 3 * ST < lim; i += 4 * ST) {
+                double hh[4], yy[4], vv[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    hh[q] = hcol[i + q * ST];
+                    yy[q] = Y(i + q * ST);
+                    vv[q] = V(i + q * ST);
+                }
+                if (scaled) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        if (!is_one(s1)) yy[q] = s1 * yy[q];
+                        if (!is_one(s2)) yy[q] = s2 * yy[q];
+                        if (!is_one(s3)) yy[q] = s3 * yy[q];
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    yy[q] = fma(sc_ys, hh[q], fma(-sc_yc, vv[q], yy[q]));
+                    vv[q] = fma(sc_c, hh[q], sc_s * vv[q]);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int r = i + q * ST;
+                    Y(r) = yy[q];
+                    V(r) = vv[q];
+                    ymx = umax64(ymx, abs_bits(yy[q]));
+                    vmx = umax64(vmx, abs_bits(vv[q]));
+                }
+            }
+            for (; i < lim; i += ST) {
+                const double h = hcol[i];
+                double yi = Y(i), vi = V(i);
+                if (scaled) {
+                    if (!is_one(s1)) yi = s1 * yi;
+                    if (!is_one(s2)) yi = s2 * yi;
+                    if (!is_one(s3)) yi = s3 * yi;
+                }
+                yi = fma(sc_ys, h, fma(-sc_yc, vi, yi));
+                vi = fma(sc_c, h, sc_s * vi);
+                Y(i) = yi;
+                V(i) = vi;
+                ymx = umax64(ymx, abs_bits(yi));
+                vmx = umax64(vmx, abs_bits(vi));
+            }
+            ymx = slot_max(ymx);
+            vmx = slot_max(vmx);
+            if (store_lane) {
+                PM(wid, 0) = ymx;
+                PM(wid, 1) = vmx;
+            }
+        }
+        __syncthreads();                                                      // rows of step j done, maxima in
+        if (wid == 0 && j >= 2) chain3(j - 1);
+        __syncthreads();                                                      // step j-1's scalars visible
+    }
+
+    double c0 = 0.0, s0 = 0.0;
+    {
+        double y0 = 0.0, a = 1.0;
+        if (wid == 0) {
+            double v0 = b >= 2 ? vcar : V(0);
+            y0 = b >= 2 ? ycar : Y(0);
+            if (J > 0) {
+                // Final rotation with H(l, l-1) (reduce.c:53-61, solve-task.c:111-118).
+                const double hleft = P.H[l + (size_t)(l - 1) * P.ldh];
+                if (hleft != 0) {
+                    givens(v0, hleft, c0, s0);
+                } else {
+                    c0 = 1.0;
+                    s0 = 0.0;
+                }
+                if (act && store_lane) {
+                    P.Cr[(size_t)l * Spad + k] = c0;
+                    P.Sr[(size_t)l * Spad + k] = s0;
+                }
+                v0 = fma(v0, c0, -(hleft * s0));
+            }
+            double phi = sc_one(is);
+            pert |= solve_1x1(smin, v0, 0.0, y0, phi, is);
+            beta = sc_combine(beta, phi, is);
+            a = sc_value(phi, is);
+            if (store_lane) {
+                BC(0) = c0;
+                BC(1) = s0;
+                BC(2) = a;
+            }
+        }
+        __syncthreads();                                       // last step's rows (and the scalars) written
+        if (wid != 0) {
+            c0 = BC(0);
+            s0 = BC(1);
+            a = BC(2);
+        }
+        if (!is_one(a))
+            for (int i = 1 + wid * RL + rs; i < b; i += NW * RL)
+                Y(i) = a * Y(i);
+        if (wid == 0 && store_lane) Y(0) = y0;
+    }
+    __syncthreads();
+
+    // Store the solved tile, its scaling factor and the perturbation flag.
+    for (int idx = tid; idx < SC * b; idx += 32 * NW) {
+        const int cc = idx / b, i = idx - cc * b;
+        const int kc = k0 + cc;
+        if (kc < P.S) P.X[l + i + (size_t)kc * P.ldx] = y[(size_t)i * SC + cc];
+    }
+    if (act && wid == 0 && store_lane) {
+        P.beta[(size_t)J * Spad + k] = beta;
+        if (pert) P.pert[k] = 1;
+    }
+    if (J == 0 || !act || !store_lane) return;
+
+    if (wid == 0) {
+        // W(q) = c_q * prod_{p<q} s_p, pi = prod s (crossover propagation).
+        double pk = 1.0;
+        for (int q = 0; q < b; ++q) {
+            const double cq = P.Cr[(size_t)(l + q) * Spad + k];
+            const double sq = P.Sr[(size_t)(l + q) * Spad + k];
+            P.W[(size_t)q * Spad + k] = cq * pk;
+            pk = pk * sq;
+        }
+        P.pi[k] = pk;
+    }
+    if (wid == 1) {
+        // Ytilde2 = G_{b-1}^T ... G_1^T (c_0 x_0, x_1, ...) (update-task.c:193-220);
+        // Zs(q) = Ytilde2(q-1), Zs(0) = 0, zlast = Ytilde2(b-1).
+        unsigned long long zmx = 0;
+        double z = c0 * Y(0);
+        P.Zs[k] = 0.0;
+        for (int q = 1; q < b; ++q) {
+            const double cq = P.Cr[(size_t)(l + q) * Spad + k];
+            const double sq = P.Sr[(size_t)(l + q) * Spad + k];
+            const double t1 = z, t2 = Y(q);
+            const double zo = fma(cq, t1, -(sq * t2));
+            z = fma(sq, t1, cq * t2);
+            P.Zs[(size_t)q * Spad + k] = zo;
+            zmx = umax64(zmx, abs_bits(zo));
+        }
+        zmx = umax64(zmx, abs_bits(z));
+        P.zlast[k] = z;
+        P.z2n[k] = from_bits(zmx);
+        P.ytil[k] = -s0 * Y(0);
+    }
+#undef V
+#undef Y
+#undef PM
+#undef HCOL
+#undef BC
+}
+
+template <int SC, int NW>
+__global__ void __launch_bounds__(32 * NW) k_diag_n(DevProblem P, int J) {
+    const int b = P.fr[J + 1] - P.fr[J];
+    if (diag_narrow_smem_bytes<SC>(b, NW) > dynamic_smem_bytes()) {
+        if (threadIdx.x == 0) atomicOr(P.err, kErrShape);
+        return;
+    }
+    diag_body_narrow<SC, NW>(P, J, blockIdx.x);
+}
+
 // NW warps: 8 (two per sub-partition, hiding FP64 latency) when v/y sit in
 // shared memory and the CTA has its SM mostly to itself; 4 when v/y are in
 // global scratch, where the CTAs share SMs with the concurrent GEMM's and a
@@ -864,8 +1248,45 @@ cudaError_t diag_smem_attr(size_t smem) {
     return raise_smem_limit((const void *)k_diag<NW>, &configured, smem);
 }
 
+template <int SC, int NW>
+cudaError_t launch_diag_narrow(const DevProblem &P, int J, int b, cudaStream_t st) {
+    static size_t configured = 0;
+    const size_t smem = diag_narrow_smem_bytes<SC>(b, NW);
+    const cudaError_t e = raise_smem_limit((const void *)k_diag_n<SC, NW>, &configured, smem);
+    if (e != cudaSuccess) return e;
+    k_diag_n<SC, NW><<<(P.S + SC - 1) / SC, 32 * NW, smem, st>>>(P, J);
+    return cudaGetLastError();
+}
+
+// Shifts per diagonal CTA: 32 (a lane per shift) while the 32-shift CTAs
+// cover the GPU; fewer when they would leave most SMs idle -- 16 below half
+// the SMs, 8 below a quarter.  HSR_DIAG_SHIFTS_PER_CTA (8, 16 or 32)
+// overrides the choice for tuning; every choice gives the same result.
+int diag_shifts_per_cta(int S) {
+    const char *env = getenv("HSR_DIAG_SHIFTS_PER_CTA");   // read per launch: tests switch it
+    const int forced = env ? atoi(env) : 0;
+    if (forced == 8 || forced == 16 || forced == 32) return forced;
+    static const int sms = []() {
+        int dev = 0, n = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return 0;
+        return n;
+    }();
+    const int wide = (S + 31) / 32;
+    if (sms <= 0) return 32;
+    if (4 * wide <= sms) return 8;
+    if (2 * wide <= sms) return 16;
+    return 32;
+}
+
 cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st) {
     const int grid = (P.S + 31) / 32;
+    switch (diag_shifts_per_cta(P.S)) {
+    case 8: return launch_diag_narrow<8, kDiagWarpsSmem>(P, J, b, st);
+    case 16: return launch_diag_narrow<16, kDiagWarpsSmem>(P, J, b, st);
+    default: break;
+    }
     if (gscratch) {
         const size_t smem = diag_small_bytes(b, kDiagWarps);
         const cudaError_t e = diag_smem_attr<kDiagWarps>(smem);
@@ -1390,10 +1811,9 @@ cudaError_t launch_gemm_c(const DevProblem &P, int J, int row_lo, int row_hi, co
 // three-accumulator 2-norm and the convergence test ||y|| > 0.1/sqrt(n)
 // (:33-40, :229-273).  Rows move through shared memory 32 at a time so that
 // the column-major block is read and written coalesced.
-__device__ __forceinline__ void finalize_body(const DevProblem &P, int bx, double *colnorm, int *status,
-                                              double *scale_out) {
-    __shared__ double buf[32][33];
-    const int lane = threadIdx.x;
+__device__ __forceinline__ void finalize_body_buf(const DevProblem &P, int bx, double *colnorm, int *status,
+                                                  double *scale_out, double (*buf)[33]) {
+    const int lane = threadIdx.x & 31;
     const int k0 = bx * 32;
     const int k = k0 + lane;
     const bool act = k < P.S;
@@ -1457,6 +1877,12 @@ __device__ __forceinline__ void finalize_body(const DevProblem &P, int bx, doubl
     }
 }
 
+__device__ __forceinline__ void finalize_body(const DevProblem &P, int bx, double *colnorm, int *status,
+                                              double *scale_out) {
+    __shared__ double buf[32][33];
+    finalize_body_buf(P, bx, colnorm, status, scale_out, buf);
+}
+
 __global__ void __launch_bounds__(32) k_finalize(DevProblem P, double *colnorm, int *status,
                                                  double *scale_out) {
     finalize_body(P, blockIdx.x, colnorm, status, scale_out);
@@ -1512,10 +1938,8 @@ cudaError_t launch_gather_cols(double *dst, long long ldd, const double *src, lo
 // One pass per row: the row sum over all columns (||H||_oo) and, at every
 // tile boundary at or right of the row's own tile, that tile's row sum; each
 // sum accumulates its columns in order, as dlange does.
-__global__ void k_norms_b(const DevProblem *probs, const BatchItem *items) {
-    const BatchItem it = items[blockIdx.x];
-    const DevProblem &P = probs[it.x];
-    const int i = it.z * kNormRows + threadIdx.x;
+__device__ __forceinline__ void norms_rows(const DevProblem &P, int rb) {
+    const int i = rb * kNormRows + threadIdx.x;
     if (i >= P.n || threadIdx.x >= kNormRows) return;
     const double *row = P.H + i;
     const int T = P.T;
@@ -1540,12 +1964,15 @@ __global__ void k_norms_b(const DevProblem *probs, const BatchItem *items) {
     atomicMax(&P.nbits[2 * (size_t)T * T], (unsigned long long)__double_as_longlong(full));
 }
 
-// Start vector eps3 = ||H||_oo * eps/2 (inverse_iteration.c:154-158, 19-34),
-// computed on the device from the norm accumulators.
-__global__ void k_init_b(const DevProblem *probs, const BatchItem *items) {
+__global__ void k_norms_b(const DevProblem *probs, const BatchItem *items) {
     const BatchItem it = items[blockIdx.x];
-    const DevProblem &P = probs[it.x];
-    const int k = it.z;
+    norms_rows(probs[it.x], it.z);
+}
+
+// Start vector eps3 = ||H||_oo * eps/2 (inverse_iteration.c:154-158, 19-34),
+// computed on the device from the norm accumulators: column k's start vector
+// and bounds, by `nth` threads numbered t = 0 .. nth-1.
+__device__ __forceinline__ void init_column(const DevProblem &P, int k, int t, int nth) {
     const int T = P.T, n = P.n;
     double hinf = from_bits(P.nbits[2 * (size_t)T * T]);
     if (P.nanflag[0] & 1) hinf = __longlong_as_double(0x7ff8000000000000LL);
@@ -1553,17 +1980,22 @@ __global__ void k_init_b(const DevProblem *probs, const BatchItem *items) {
     double *x = P.X + (size_t)k * P.ldx;
     double *r = P.R + (size_t)k * P.ldr;
     const double *hl = P.H + (size_t)(n - 1) * P.ldh;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = t; i < n; i += nth) {
         double h = hl[i];
         if (i == n - 1) h = h - P.wr[k];
         r[i] = h;
         x[i] = eps3;
     }
-    for (int I = threadIdx.x; I < T; I += blockDim.x) {
+    for (int I = t; I < T; I += nth) {
         P.beta[(size_t)I * P.Spad + k] = sc_one(P.is);
         P.ynorm[(size_t)I * P.Spad + k] = eps3;
     }
-    if (threadIdx.x == 0) P.pert[k] = 0;
+    if (t == 0) P.pert[k] = 0;
+}
+
+__global__ void k_init_b(const DevProblem *probs, const BatchItem *items) {
+    const BatchItem it = items[blockIdx.x];
+    init_column(probs[it.x], it.z, threadIdx.x, blockDim.x);
 }
 
 __global__ void __launch_bounds__(32 * kDiagWarpsB) k_diag_b(const DevProblem *probs, const BatchItem *items) {
@@ -1664,6 +2096,171 @@ cudaError_t launch_normalize_b(const DevProblem *probs, const BatchItem *items, 
     if (n_items <= 0) return cudaSuccess;
     k_normalize_b<<<n_items, 32 * kNormalizeCols, 0, st>>>(probs, items);
     return cudaGetLastError();
+}
+
+// ------------------------------------------------------ persistent queue
+// The batched work as one cooperative launch: CTAs take items in list order
+// from a ticket counter, wait (bounded) for the per-problem counters their
+// item depends on, run the same body the batched kernels run, and complete
+// their own counter.  A stage of one problem thus starts as soon as its own
+// predecessors are done, instead of at the next tick of the whole batch.
+// Producers publish with a fence before the counter increment; consumers
+// fence after observing it (and, before TMA reads of data other CTAs wrote,
+// a generic-to-async proxy fence).
+
+// Diagonal blocks per item: as many warps as fit beside the GEMM's operand
+// ring with v/y in shared memory, at least one, at most eight.
+__host__ __device__ inline size_t queue_diag_warp_bytes(int b) {
+    return diag_small_bytes(b, 1) + (size_t)64 * b * sizeof(double);
+}
+int queue_diag_warps(int bmax) {
+    const size_t budget = gemm_smem_bytes();
+    int w = (int)(budget / queue_diag_warp_bytes(bmax));
+    return w < 1 ? 1 : (w > 8 ? 8 : w);
+}
+size_t queue_smem_bytes(int bmax) {
+    size_t need = gemm_smem_bytes();
+    const size_t diag = queue_diag_warps(bmax) * queue_diag_warp_bytes(bmax);
+    const size_t fin = (size_t)kQueueFinalBlocks * 32 * 33 * sizeof(double);
+    if (diag + 128 > need) need = diag + 128;     // + room to align the base to 128 bytes
+    if (fin + 128 > need) need = fin + 128;
+    return need;
+}
+
+__device__ __forceinline__ bool queue_wait(const int *ctr, int dep, int tgt, int *err, long limit) {
+    if (dep < 0 || tgt <= 0) return true;
+    const volatile int *c = ctr + dep;
+    const volatile int *e = err;
+    unsigned ns = 32;
+    for (long it = 0; it < limit; ++it) {
+        if (*c >= tgt) return true;
+        if (*e & kErrQueueTimeout) return false;
+        __nanosleep(ns);
+        if (ns < 1024) ns <<= 1;
+    }
+    atomicOr(err, kErrQueueTimeout);
+    return false;
+}
+
+__global__ void __launch_bounds__(kQueueThreads, 2) k_queue(const DevProblem *__restrict__ probs,
+                                                           const QueueItem *__restrict__ items, int n_items,
+                                                           const CUtensorMap *maps, int *ctr, int *ticket, int *err,
+                                                           int diag_warps, long spin_limit) {
+    extern __shared__ unsigned char smraw[];
+    __shared__ DevProblem Ps;
+    __shared__ int s_idx, s_ok;
+    static_assert(sizeof(DevProblem) % 8 == 0 && sizeof(DevProblem) / 8 <= kQueueThreads, "descriptor copy");
+    const int tid = threadIdx.x, wid = tid >> 5;
+    double *smd = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(smraw) + 127) & ~uintptr_t(127));
+    for (;;) {
+        if (tid == 0) {
+            const int idx = atomicAdd(ticket, 1);
+            int ok = 1;
+            if (idx < n_items) {
+                const QueueItem &q = items[idx];
+                ok = queue_wait(ctr, q.dep0, q.tgt0, err, spin_limit) && queue_wait(ctr, q.dep1, q.tgt1, err, spin_limit);
+                __threadfence();
+            }
+            s_idx = idx;
+            s_ok = ok;
+        }
+        __syncthreads();
+        const int idx = s_idx;
+        if (idx >= n_items) break;
+        const QueueItem q = items[idx];
+        const BatchItem it = q.it;
+        if (tid < (int)(sizeof(DevProblem) / 8))
+            reinterpret_cast<long long *>(&Ps)[tid] = reinterpret_cast<const long long *>(probs + it.x)[tid];
+        __syncthreads();
+        const DevProblem &P = Ps;
+        if (s_ok) {
+            switch (q.kind) {
+            case qkNorms:
+                norms_rows(P, it.z);
+                break;
+            case qkInit: {
+                const int k = it.z * kQueueInitCols + wid;
+                if (wid < kQueueInitCols && k < P.S) init_column(P, k, tid & 31, 32);
+                break;
+            }
+            case qkDiag: {
+                const int blk = it.z * diag_warps + wid;
+                const int b = P.fr[it.y + 1] - P.fr[it.y];
+                if (wid < diag_warps && blk * 32 < P.S)
+                    diag_body_1w(P, it.y, blk, smd + (size_t)wid * (queue_diag_warp_bytes(b) / sizeof(double)),
+                                 nullptr);
+                break;
+            }
+            case qkPart1:
+                part1_block(P, it.y, it.z * kPart1Shifts);
+                break;
+            case qkGemm: {
+                if (tid == 0) {
+                    fence_proxy_async_global();    // operands other CTAs wrote, read by TMA below
+                    fence_proxy_async_smem();      // this CTA's earlier generic use of the ring
+                }
+                const CUtensorMap *m = maps + 3 * (size_t)it.x;
+                const int J = it.y;
+                const bool top = (it.z & kGemmTopFlag) != 0;
+                const int lo = top ? P.fr[J - 1] : 0, hi = top ? P.fr[J] : P.fr[J - 1];
+                gemm_body<false>(P, J, lo, hi, it.z & ~kGemmTopFlag, it.w, m, m + 1, m + 2);
+                __syncthreads();
+                if (tid == 0) {
+                    GemmSmem &gs = *reinterpret_cast<GemmSmem *>(smd);
+                    for (int st = 0; st < kGemmStages; ++st) mbar_inval(&gs.full[st]);
+                }
+                break;
+            }
+            case qkFinal: {
+                const int blk = it.z * kQueueFinalBlocks + wid;
+                if (wid < kQueueFinalBlocks && blk * 32 < P.S)
+                    finalize_body_buf(P, blk, P.colnorm, P.status, P.scale,
+                                      reinterpret_cast<double(*)[33]>(smd + (size_t)wid * 32 * 33));
+                break;
+            }
+            case qkNormalize: {
+                const int k = it.z * kNormalizeCols + wid;
+                if (k < P.S && P.status[k]) {
+                    const double nrm = P.colnorm[k];
+                    double *x = P.X + (size_t)k * P.ldx;
+                    for (int i = tid & 31; i < P.n; i += 32) x[i] = x[i] / nrm;
+                }
+                break;
+            }
+            default:
+                break;
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();
+            atomicAdd(&ctr[q.ctr], 1);
+        }
+    }
+}
+
+int queue_max_grid(int bmax) {
+    static size_t configured = 0;
+    const size_t smem = queue_smem_bytes(bmax);
+    if (raise_smem_limit((const void *)k_queue, &configured, smem) != cudaSuccess) return 0;
+    int nb = 0, dev = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_queue, kQueueThreads, smem) != cudaSuccess ||
+        cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return 0;
+    return nb * sms;
+}
+
+cudaError_t launch_queue(const DevProblem *probs, const QueueItem *items, int n_items, const CUtensorMap *maps,
+                         int *ctr, int *ticket, int *err, int bmax, int grid, cudaStream_t st) {
+    const int maxg = queue_max_grid(bmax);
+    if (maxg <= 0 || grid <= 0 || grid > maxg) return cudaErrorInvalidConfiguration;
+    int dw = queue_diag_warps(bmax);
+    long spin = 1L << 22;      // ~4 s of polls with the back-off: far above any item's wait
+    void *args[] = {(void *)&probs, (void *)&items, (void *)&n_items, (void *)&maps, (void *)&ctr,
+                    (void *)&ticket, (void *)&err, (void *)&dw, (void *)&spin};
+    return cudaLaunchCooperativeKernel((const void *)k_queue, dim3(grid), dim3(kQueueThreads), args,
+                                       queue_smem_bytes(bmax), st);
 }
 
 // ------------------------------------------------ bounded-wait self-test

@@ -113,6 +113,36 @@ constexpr int kNormRows = 128;        // rows per norms item
 constexpr int kNormalizeCols = 8;     // columns per normalize item
 constexpr int kPart1Shifts = 256;     // shifts per part-1 block (a lane per shift)
 
+// Persistent batched engine.  One cooperative launch of `grid` CTAs (all
+// resident at once) works through `items` in list order: each CTA takes the
+// next index from *ticket, waits until the counters its item depends on reach
+// their targets, runs the item, and adds one to the item's own counter.  The
+// list is in a topological order of those dependencies, so the lowest
+// unfinished item can always run.  Waits are bounded: a wait that gives up
+// records kErrQueueTimeout in *err, and every other wait then stops at once,
+// so the launch always ends.
+enum QueueKind : int { qkNorms = 0, qkInit, qkDiag, qkPart1, qkGemm, qkFinal, qkNormalize };
+struct QueueItem {
+    BatchItem it;     // as in the batched kernels; qkInit: z = group of kQueueInitCols columns,
+                      // qkDiag: z = group of queue_diag_warps() 32-shift blocks,
+                      // qkFinal: z = group of kQueueFinalBlocks 32-shift blocks
+    int kind, ctr;    // what runs; the counter it completes
+    int dep0, tgt0;   // wait until ctr[dep0] >= tgt0 (dep0 < 0: none)
+    int dep1, tgt1;
+    int pad0, pad1;
+};
+constexpr int kQueueInitCols = 8;
+constexpr int kQueueFinalBlocks = 8;
+constexpr int kQueueThreads = 256;
+// Diagonal blocks one item runs (a warp each, v/y in shared memory) for tile
+// height up to bmax, and the shared memory of the persistent kernel.
+int queue_diag_warps(int bmax);
+size_t queue_smem_bytes(int bmax);
+// Largest grid that keeps every CTA resident (0 when the kernel cannot run).
+int queue_max_grid(int bmax);
+cudaError_t launch_queue(const DevProblem *probs, const QueueItem *items, int n_items, const CUtensorMap *maps,
+                         int *ctr, int *ticket, int *err, int bmax, int grid, cudaStream_t st);
+
 // Complex-conjugate shifts (hsr_cplx.cu).  The problem's S counts real
 // columns: pair p owns columns 2p (real part) and 2p+1 (imaginary part), and
 // P.wr holds the shifts interleaved the same way.

@@ -227,6 +227,28 @@ int hsr_batch_plan_execute(hsr_batch_plan *plan, void *stream);
 int hsr_batch_plan_info(const hsr_batch_plan *plan, int *tlsz, int *ticks, long *launches);
 void hsr_batch_plan_destroy(hsr_batch_plan *plan);
 
+/* Engines of a plan (no reference counterpart; the reference's equivalent is
+ * the dependency-driven OpenMP task DAG of shifted_Hessenberg_solve.c:95-313):
+ *   HSR_BATCH_ENGINE_TICKS  one CUDA graph of per-phase batched launches; all
+ *                           problems advance one stage per tick in lock step.
+ *   HSR_BATCH_ENGINE_QUEUE  one persistent cooperative launch (captured in a
+ *                           graph with the set-up memsets) that works through a
+ *                           device work queue of (problem, stage, block) items;
+ *                           an item starts as soon as the items of its own
+ *                           problem that it depends on have finished, tracked
+ *                           by per-problem counters with bounded waits.
+ * Both give bit-identical results.  set_engine builds the queue on first use;
+ * `stream` orders that set-up. */
+#define HSR_BATCH_ENGINE_TICKS 0
+#define HSR_BATCH_ENGINE_QUEUE 1
+int hsr_batch_plan_set_engine(hsr_batch_plan *plan, int engine, void *stream);
+/* Current engine, work items in the queue, persistent grid size, diagonal
+ * blocks per queue item (0 before the queue is built), and whether the
+ * persistent launch was captured in the plan's graph (1) or, where the
+ * runtime cannot capture a cooperative launch, is issued directly (0). */
+int hsr_batch_plan_queue_info(const hsr_batch_plan *plan, int *engine, long *items, int *grid,
+                              int *diag_warps, int *in_graph);
+
 /* Tile size for batches whose orders lie in [n_lo, n_hi]: the size that
  * hsr_autotune_batch measured fastest on this GPU for the sample whose order
  * range overlaps [n_lo, n_hi] the most, else a default. */

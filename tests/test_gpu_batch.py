@@ -154,3 +154,34 @@ def test_served_pinned_host_buffers(gpu_lib):
         assert np.all(ra["vr_full"][n:, :] == -7.0) and np.all(rb["vr_full"][n:, :] == -7.0)
         ref = hsr.inverse_iteration(H, wr, 32, 16)
         assert np.array_equal(ra["vr"], ref["vr"])
+
+
+@pytest.mark.parametrize("tlsz", [32, 64])
+def test_queue_engine_equals_ticks_and_alone(gpu_lib, tlsz):
+    """The persistent work-queue engine gives every problem exactly what the
+    tick graph and a lone solve give, on two executes in a row."""
+    import torch
+    import hsrq3in_gb300 as hsr
+    dev = torch.device("cuda", 0)
+    probs = _mixed(40, 21, 12, 330)
+    tens = [_dev_problem(torch, H, wr, dev) for H, wr in probs]
+    plan = hsr.BatchPlan(tens, tlsz=tlsz, engine="queue")
+    qi = plan.queue_info()
+    assert qi["engine"] == "queue" and qi["items"] > 0 and qi["grid"] > 0 and qi["diag_warps"] >= 1
+    for rep in range(2):
+        for _, _, dvr in tens:
+            dvr.fill_(float("nan"))
+        plan.execute()
+        torch.cuda.synchronize()
+        for (H, wr), (dH, dwr, dvr) in zip(probs, tens):
+            n = H.shape[0]
+            alone = hsr.inverse_iteration(H, wr, tlsz, 16)
+            assert np.array_equal(dwr.cpu().numpy(), alone["wr"])
+            assert np.array_equal(dvr[:, :n].cpu().numpy().T, alone["vr"]), (rep, n)
+    plan.set_engine("ticks")
+    for _, _, dvr in tens:
+        dvr.fill_(float("nan"))
+    plan.execute()
+    torch.cuda.synchronize()
+    H, wr = probs[5]
+    assert np.array_equal(tens[5][2][:, :H.shape[0]].cpu().numpy().T, hsr.inverse_iteration(H, wr, tlsz, 16)["vr"])

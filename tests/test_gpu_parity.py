@@ -277,3 +277,23 @@ def test_pinned_host_buffers_through_c_abi(gpu_lib, extra_h, extra_v):
 def hsr_cplx(H, mu, tlsz):
     import hsrq3in_gb300 as hsr
     return hsr.inverse_iteration_cplx(H, mu, tlsz, 16)
+
+
+@pytest.mark.parametrize("sc", ["8", "16", "32"])
+@pytest.mark.parametrize("n,tlsz,nrhs,seed", [
+    (300, 64, 300, 31),      # several tiles, all shifts
+    (203, 40, 77, 32),       # ragged first tile, ragged shift count
+    (520, 160, 1000, 33),    # the benchmark tile size, more shifts than rows (repeated)
+])
+def test_diag_forms_bitwise(gpu_lib, monkeypatch, sc, n, tlsz, nrhs, seed):
+    """The diagonal kernel's three forms -- 8, 16 or 32 shifts per CTA, chosen
+    by shift count -- give the oracle's result bit for bit."""
+    monkeypatch.setenv("HSR_DIAG_SHIFTS_PER_CTA", sc)
+    H, lam = G.real_spectrum(n, seed)
+    wr = G.perturbed_shifts(np.resize(lam, nrhs), seed + 1)
+    dev = _device(H, wr, tlsz)
+    orc = O.oracle_inverse_iteration(H, wr, tlsz, 16, intscale=1, variant="fma")
+    assert np.array_equal(dev["wr"], orc["wr"])
+    assert np.array_equal(dev["vr"], orc["vr"])
+    assert np.array_equal(dev["perturbed"], orc["perturbed"])
+    assert np.array_equal(dev["scale"], orc["colscale"])
