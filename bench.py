@@ -377,7 +377,7 @@ def run_gpu(args, H, wr, rank, world):
 
 SMALL_N = 1000
 SMALL_STEPS = 50
-SMALL_TLSZ = 160
+SMALL_TLSZ = 0          # 0: the plain-path autotuner's choice
 
 
 def run_plain_small(args, tlsz: int):
@@ -409,6 +409,14 @@ def run_plain_small(args, tlsz: int):
     stream = torch.cuda.Stream(device=dev)
     opt = _lib.Options(0, 0, -1, 0.0)
     steps = max(args.steps, SMALL_STEPS)
+    # Tile size: the plain-path autotuner on this problem (outside the timed
+    # region); its measured alternatives go into the line.
+    cands = (48, 64, 96, 128, 160, 200)
+    with torch.cuda.stream(stream):
+        tuned, tune_ms = hsr.autotune_plain(dHt, dwr, dX, candidates=cands, stream=stream)
+    torch.cuda.synchronize()
+    if tlsz == 0:
+        tlsz = tuned
 
     def step():
         rc = lib.hsr_inverse_iteration_device(n, dHt.data_ptr(), ldh, n, dwr.data_ptr(), tlsz, dX.data_ptr(), ldh,
@@ -456,6 +464,8 @@ def run_plain_small(args, tlsz: int):
                                   "order the sequential diagonal chain, not one kernel, sets the time)",
                         "peak_source": "FP64 DFMA stream measured in this run"},
            "kernel_ms_one_step": {k: round(float(v), 3) for k, v in zip(_lib.KERNEL_CLASSES, kms)},
+           "autotune": {"candidates": list(cands), "ms": [round(x, 3) for x in tune_ms], "best": tuned,
+                        "api": "hsr_autotune_plain"},
            "gpu_launches_per_step": launches / steps, "clocks": clk.summary()}
     # e2e through the drop-in entry point, pinned host buffers, flush between steps
     Hp = torch.from_numpy(np.asfortranarray(H).ravel(order="F")).pin_memory()

@@ -32,7 +32,7 @@ EXPORTS = [
     "hsr_hessenberg_device", "hsr_hessenberg_apply_q_device",
     "hsr_batch_plan_create", "hsr_batch_plan_execute", "hsr_batch_plan_info", "hsr_batch_plan_destroy",
     "hsr_batch_plan_set_engine", "hsr_batch_plan_queue_info",
-    "hsr_autotune_tlsz", "hsr_autotune_batch",
+    "hsr_autotune_tlsz", "hsr_autotune_batch", "hsr_autotune_plain", "hsr_autotune_plain_tlsz",
     "hsr_server_create", "hsr_server_replay", "hsr_server_destroy",
     "hsr_inverse_iteration_cplx_ex", "hsr_inverse_iteration_cplx_device", "hsr_inverse_iteration_mixed",
     "hsr_selftest_bounded_wait",
@@ -160,6 +160,11 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     lib.hsr_autotune_batch.restype = C.c_int
     lib.hsr_autotune_batch.argtypes = [C.c_int, C.POINTER(BatchProblem), C.POINTER(C.c_int), C.c_int,
                                        C.POINTER(C.c_double), C.c_void_p]
+    lib.hsr_autotune_plain.restype = C.c_int
+    lib.hsr_autotune_plain.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                       C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_double), C.c_void_p]
+    lib.hsr_autotune_plain_tlsz.restype = C.c_int
+    lib.hsr_autotune_plain_tlsz.argtypes = [C.c_int]
     lib.hsr_server_create.restype = C.c_int
     lib.hsr_server_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(ServerConfig)]
     lib.hsr_server_replay.restype = C.c_int

@@ -62,7 +62,8 @@ def inverse_iteration(H: np.ndarray, wr: np.ndarray, tlsz: int, rhs_tlsz: int = 
     n = H.shape[0]
     wr = np.array(wr, dtype=np.float64, copy=True)
     nrhs = wr.shape[0]
-    T = (n + tlsz - 1) // tlsz
+    tl = int(tlsz) if tlsz else lib.hsr_autotune_plain_tlsz(n)      # 0: the autotuned size
+    T = (n + tl - 1) // tl
     if rhs is not None:
         vr = np.array(rhs, dtype=np.float64, order="F", copy=True)
     else:
@@ -306,6 +307,22 @@ class BatchPlan:
             self.close()
         except Exception:
             pass
+
+
+def autotune_plain(dH, dwr, dvr, candidates=(64, 96, 128, 160, 200), stream=None):
+    """Time the plain device path on this problem for each candidate tile
+    size (dwr restored, dvr overwritten); records the fastest for this order
+    (used when tlsz=0 is passed) and returns (best, [ms per candidate])."""
+    lib = _lib.load()
+    n = dH.shape[0]
+    cand = (C.c_int * len(candidates))(*candidates)
+    ms = (C.c_double * len(candidates))()
+    best = lib.hsr_autotune_plain(n, dH.data_ptr(), dH.stride(0), dwr.numel(), dwr.data_ptr(), dvr.data_ptr(),
+                                  dvr.stride(0), cand, len(candidates), ms,
+                                  None if stream is None else C.c_void_p(stream.cuda_stream))
+    if best < 0:
+        raise HsrError(best)
+    return best, list(ms)
 
 
 def autotune_batch(problems, candidates=(32, 48, 64, 96, 128), stream=None):

@@ -17,6 +17,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <vector>
 
 namespace hsr {
@@ -240,6 +242,7 @@ struct Solver {
     cudaStream_t st;
     Workspace *w;
     CUtensorMap tmH, tmW[2], tmZ[2];
+    CUtensorMap tmWn[2], tmZn[2];   // 16-column boxes for launch_gemm_narrow
     double *eps3_dev;
     int *d_status;     // [S] per final column
     double *d_colnorm; // [S]
@@ -322,8 +325,12 @@ int run_pass(Solver &s, int mode, int its, int off, int cnt) {
             HSR_LAUNCH_C(kcPart1, M, launch_part1(P, J, M));
             HSR_CK(cudaEventRecord(w.ev_top, M));
             HSR_CK(cudaStreamWaitEvent(D, w.ev_top, 0));
-            HSR_LAUNCH_C(kcGemmTop, D,
-                         launch_gemm(P, J, s.fr[J - 1], s.fr[J], s.tmH, s.tmW[J & 1], s.tmZ[J & 1], D));
+            if (gemm_prefers_narrow(s.fr[J] - s.fr[J - 1], cc))
+                HSR_LAUNCH_C(kcGemmTop, D, launch_gemm_narrow(P, J, s.fr[J - 1], s.fr[J], s.tmH, s.tmWn[J & 1],
+                                                              s.tmZn[J & 1], D));
+            else
+                HSR_LAUNCH_C(kcGemmTop, D,
+                             launch_gemm(P, J, s.fr[J - 1], s.fr[J], s.tmH, s.tmW[J & 1], s.tmZ[J & 1], D));
             HSR_LAUNCH_C(kcDiag, D, launch_diag(Pn, J - 1, s.fr[J] - s.fr[J - 1], gs, D));
             HSR_CK(cudaEventRecord(w.ev_diag, D));
             if (s.fr[J - 1] > 0)
@@ -426,6 +433,12 @@ int solve_device(int n, const double *dH, long long ldh, int S, double *dwr, int
         !make_map(&s.tmZ[1], w.Zs.as<double>() + (size_t)tlsz * Sp, Sp, (unsigned long long)tlsz, Sp, kGemmBN,
                   kGemmKC))
         return HSR_ERR_CUDA;
+    for (int par = 0; par < 2; ++par)
+        if (!make_map(&s.tmWn[par], w.W.as<double>() + (size_t)par * tlsz * Sp, Sp, (unsigned long long)tlsz, Sp,
+                      kGemmBNNarrow, kGemmKC) ||
+            !make_map(&s.tmZn[par], w.Zs.as<double>() + (size_t)par * tlsz * Sp, Sp, (unsigned long long)tlsz, Sp,
+                      kGemmBNNarrow, kGemmKC))
+            return HSR_ERR_CUDA;
 
     // Norms and eps3.
     unsigned long long *bits = w.bits.as<unsigned long long>();
@@ -543,6 +556,30 @@ int solve_device(int n, const double *dH, long long ldh, int S, double *dwr, int
     return result;
 }
 
+// Tile sizes of the plain path recorded by hsr_autotune_plain, by order.
+std::mutex g_plain_tune_mu;
+std::map<int, int> g_plain_tune;
+
+// Default tile size by order, from sweeps of the plain path on GB300 (all
+// shifts): 64 at n = 1000 and 2048, 128 at n = 4096, 160 at n = 10^4.
+int plain_default_tlsz(int n) { return n <= 2560 ? 64 : (n <= 6144 ? 128 : 160); }
+
+// tlsz for order n: the tuned entry of the nearest order within a factor of
+// two, else the default.
+int plain_tlsz_for(int n) {
+    std::lock_guard<std::mutex> g(g_plain_tune_mu);
+    int best = 0;
+    double bd = 1e300;
+    for (auto &kv : g_plain_tune) {
+        const double d = std::fabs(std::log((double)kv.first / n));
+        if (d < bd) {
+            bd = d;
+            best = kv.second;
+        }
+    }
+    return (best > 0 && bd <= std::log(2.0)) ? best : plain_default_tlsz(n);
+}
+
 int check_args(int n, int ldH, int nrhs, int tlsz, int ldvr, const void *H, const void *wr, const void *vr) {
     if (n <= 0 || ldH < n || nrhs < 0 || tlsz <= 0 || (tlsz % 4) != 0 || ldvr < n || !H) return HSR_ERR_ARG;
     if (nrhs > 0 && (!wr || !vr)) return HSR_ERR_ARG;
@@ -602,6 +639,7 @@ int host_call(int n, const double *H, int ldH, int nrhs, double *wr, int tlsz, i
               int ldvr, const hsr_options *opt, hsr_column_info *info) {
     g_launches = 0;
     g_timing.reset();
+    if (tlsz == 0 && n > 0) tlsz = plain_tlsz_for(n);
     int rc = check_args(n, ldH, nrhs, tlsz, ldvr, H, wr, vr);
     if (rc) return rc;
     if (rhs_tlsz <= 0) return HSR_ERR_ARG;
@@ -1027,6 +1065,7 @@ int hsr_inverse_iteration_device(int n, const double *dH, int lddH, int nrhs, do
                                  int lddvr, const hsr_options *opt, void *stream, int *d_status, double *d_scale) {
     g_launches = 0;
     g_timing.reset();
+    if (tlsz == 0 && n > 0) tlsz = plain_tlsz_for(n);
     int rc = check_args(n, lddH, nrhs, tlsz, lddvr, dH, dwr, dvr);
     if (rc) return g_last_status = rc;
     if (nrhs == 0) return g_last_status = HSR_OK;
@@ -1231,6 +1270,67 @@ int hsr_selftest_bounded_wait(void *stream) {
     HSR_CK(cudaStreamSynchronize(st));
     return g_last_status = (errw & kErrWaitTimeout) ? HSR_ERR_DEVICE : HSR_OK;
 }
+
+int hsr_autotune_plain(int n, const double *dH, int lddH, int nrhs, double *dwr, double *dvr, int lddvr,
+                       const int *cand, int ncand, double *ms_out, void *stream) {
+    if (n <= 0 || nrhs <= 0 || !cand || ncand <= 0 || !dH || !dwr || !dvr) return g_last_status = HSR_ERR_ARG;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    double *wr0 = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto done = [&](int rc) {
+        if (wr0) cudaFree(wr0);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        return g_last_status = rc;
+    };
+    if (cudaMalloc(&wr0, (size_t)nrhs * 8) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+        cudaEventCreate(&e1) != cudaSuccess ||
+        cudaMemcpyAsync(wr0, dwr, (size_t)nrhs * 8, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+        return done(HSR_ERR_CUDA);
+    int best = 0;
+    double best_ms = 1e300;
+    for (int c = 0; c < ncand; ++c) {
+        double ms = 1e300;
+        if (cand[c] > 0 && cand[c] % 4 == 0) {
+            double tot = 0.0;
+            bool ok = true;
+            for (int rep = 0; rep < 3 && ok; ++rep) {
+                if (cudaMemcpyAsync(dwr, wr0, (size_t)nrhs * 8, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+                    cudaEventRecord(e0, st) != cudaSuccess)
+                    return done(HSR_ERR_CUDA);
+                const int rc = hsr_inverse_iteration_device(n, dH, lddH, nrhs, dwr, cand[c], dvr, lddvr, nullptr,
+                                                            stream, nullptr, nullptr);
+                if (rc < 0) {
+                    ok = false;
+                    break;
+                }
+                float t = 0.f;
+                if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                    cudaEventElapsedTime(&t, e0, e1) != cudaSuccess)
+                    return done(HSR_ERR_CUDA);
+                if (rep > 0) tot += t;      // the first run warms the workspace
+            }
+            if (ok) ms = tot / 2;
+        }
+        if (ms_out) ms_out[c] = ms;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = cand[c];
+        }
+    }
+    if (cudaMemcpyAsync(dwr, wr0, (size_t)nrhs * 8, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return done(HSR_ERR_CUDA);
+    if (best <= 0) return done(HSR_ERR_ARG);
+    {
+        std::lock_guard<std::mutex> g(g_plain_tune_mu);
+        g_plain_tune[n] = best;
+    }
+    done(HSR_OK);
+    return best;
+}
+
+int hsr_autotune_plain_tlsz(int n) { return n > 0 ? plain_tlsz_for(n) : HSR_ERR_ARG; }
 
 const char *hsr_version(void) { return "hsrq3in_gb300 0.1 (sm_103a, FP64 DFMA)"; }
 

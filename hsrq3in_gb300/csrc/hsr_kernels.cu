@@ -167,6 +167,7 @@ cudaError_t launch_init(const DevProblem &P, int mode, const double *eps3_dev, i
 constexpr int kDiagWarps = 4;     // single-problem path, v/y in global scratch
 constexpr int kDiagWarpsSmem = 8; // single-problem path, v/y in shared memory
 constexpr int kDiagWarpsB = 1;    // batched path
+constexpr int kDiagWarpsNarrow = 4;  // single-problem path, 8 or 16 shifts per CTA
 
 constexpr int kDiagBcast = 8;      // per-lane step results broadcast by warp 0
 // Staging buffers for columns of H: the pipelined multi-warp body keeps three
@@ -858,8 +859,11 @@ __host__ __device__ constexpr size_t diag_narrow_smem_bytes(int b, int nw) {
 template <int SC, int NW>
 __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int bx) {
     static_assert(32 % SC == 0 && SC >= 4 && SC < 32, "shifts per CTA");
+    static_assert(NW % 4 == 0, "whole sub-partitions");
     constexpr int RL = 32 / SC;                                               // rows per row-warp instruction
-    constexpr int NR = NW - 1;                                                // row warps
+    // Warps w = 0, 4, ... share sub-partition 0, whose FP64 unit the scalar
+    // chain (warp 0) needs to itself: rows go to the other warps only.
+    constexpr int NR = NW - NW / 4;                                           // row warps
     extern __shared__ double sm[];
     const int tid = threadIdx.x;
     const int lane = tid & 31;
@@ -867,6 +871,8 @@ __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int
     const int sh = lane % SC;                                                 // shift slot
     const int rs = lane / SC;                                                 // row slot (row warps)
     const bool store_lane = lane < SC;                                        // chain results are stored once
+    const bool row_warp = (wid & 3) != 0;
+    const int rw = wid - 1 - wid / 4;                                         // row-warp index, 0 .. NR-1
     const int k0 = bx * SC;
     const int k = k0 + sh;
     const bool act = k < P.S;
@@ -926,8 +932,8 @@ __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int
     // Maxima of |y(0:b-3)| and |v(0:b-3)| for the first step, by the row warps.
     {
         unsigned long long ym = 0, vm = 0;
-        if (wid > 0)
-            for (int i = (wid - 1) * RL + rs; i < b - 2; i += NR * RL) {
+        if (row_warp)
+            for (int i = rw * RL + rs; i < b - 2; i += NR * RL) {
                 ym = umax64(ym, abs_bits(Y(i)));
                 vm = umax64(vm, abs_bits(V(i)));
             }
@@ -1048,9 +1054,9 @@ __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int
                 chain12(j - 1, vn, yn);
             }
             if (j >= 3) stage_col(j - 3);                                     // for step j-2's chain
-        } else {
+        } else if (row_warp) {
             if (scaled) {
-                for (int i = j + 1 + (wid - 1) * RL + rs; i < b; i += NR * RL) {
+                for (int i = j + 1 + rw * RL + rs; i < b; i += NR * RL) {
                     double t = Y(i);
                     if (!is_one(s1)) t = s1 * t;
                     if (!is_one(s2)) t = s2 * t;
@@ -1060,7 +1066,7 @@ __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int
             }
             unsigned long long ymx = 0, vmx = 0;
             const int lim = j - 2;                                            // rows 0 .. j-3
-            int i = (wid - 1) * RL + rs;
+            int i = rw * RL + rs;
             constexpr int ST = NR * RL;                                       // row stride of one lane
             for (; i + 3 * ST < lim; i += 4 * ST) {
                 double hh[4], yy[4], vv[4];
@@ -1283,8 +1289,8 @@ int diag_shifts_per_cta(int S) {
 cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st) {
     const int grid = (P.S + 31) / 32;
     switch (diag_shifts_per_cta(P.S)) {
-    case 8: return launch_diag_narrow<8, kDiagWarpsSmem>(P, J, b, st);
-    case 16: return launch_diag_narrow<16, kDiagWarpsSmem>(P, J, b, st);
+    case 8: return launch_diag_narrow<8, kDiagWarpsNarrow>(P, J, b, st);
+    case 16: return launch_diag_narrow<16, kDiagWarpsNarrow>(P, J, b, st);
     default: break;
     }
     if (gscratch) {
@@ -1514,14 +1520,22 @@ cudaError_t launch_part1(const DevProblem &P, int J, cudaStream_t st) {
 // warp whose rows all lie outside [row_lo, row_hi) -- the partial blocks at
 // the ragged first tile and at unaligned tile starts -- skips the FMA loop:
 // masked lanes would cost the FP64 pipe as much as live ones.
-struct GemmSmem {
+// BN = 64 is the main tile.  BN = 16 serves the short GEMM over the rows of
+// the next diagonal tile when the 64-column tiles would leave most SMs idle:
+// that GEMM gates the next diagonal solve, and 16-column tiles spread its
+// sequential K loop over four times as many CTAs.  Every accumulator sums
+// the same products in the same order in both shapes.
+template <int BN>
+struct GemmSmemT {
     double A[kGemmStages][kGemmKC][kGemmBM];
-    double W[kGemmStages][kGemmKC][kGemmBN];
-    double Z[kGemmStages][kGemmKC][kGemmBN];
+    double W[kGemmStages][kGemmKC][BN];
+    double Z[kGemmStages][kGemmKC][BN];
     uint64_t full[kGemmStages];
 };
+using GemmSmem = GemmSmemT<kGemmBN>;
 
 size_t gemm_smem_bytes() { return sizeof(GemmSmem) + 128; }
+size_t gemm_narrow_smem_bytes() { return sizeof(GemmSmemT<kGemmBNNarrow>) + 128; }
 
 // Complex-shift epilogue: columns (2p, 2p+1) hold the real and imaginary
 // parts of pair p, the same thread owns both, and every scalar of the real
@@ -1596,21 +1610,25 @@ __device__ __forceinline__ void gemm_epilogue_cplx(const DevProblem &P, int J, i
     }
 }
 
-template <bool kCplx>
+template <bool kCplx, int BN = kGemmBN>
 __device__ __forceinline__ void gemm_body(const DevProblem &P, int J, int row_lo, int row_hi, int bx, int by,
                                           const CUtensorMap *tmH, const CUtensorMap *tmW,
                                           const CUtensorMap *tmZ) {
+    static_assert(BN == kGemmBN || (BN == kGemmBNNarrow && !kCplx), "tile widths");
+    // Threads per row of the tile (4 columns each) and rows per thread.
+    constexpr int TC = BN / 4, RPT = kGemmBM * TC / 256;
+    static_assert(RPT == 4 || RPT == 1, "thread tile");
     extern __shared__ unsigned char smraw[];
-    GemmSmem &sm = *reinterpret_cast<GemmSmem *>(
+    GemmSmemT<BN> &sm = *reinterpret_cast<GemmSmemT<BN> *>(
         (reinterpret_cast<uintptr_t>(smraw) + 127) & ~uintptr_t(127));
     const int tid = threadIdx.x;
     // Row blocks start at row_lo rounded down to 8, so the TMA x coordinate
     // is always 16-byte aligned; rows outside [row_lo, row_hi) are not stored.
     const int row0 = (row_lo & ~7) + bx * kGemmBM;
-    const int col0 = by * kGemmBN;
+    const int col0 = by * BN;
     const int l = P.fr[J], b = P.fr[J + 1] - l;
     const int nk = (b + kGemmKC - 1) / kGemmKC;
-    const uint32_t bytes = (uint32_t)((kGemmBM + 2 * kGemmBN) * kGemmKC * sizeof(double));
+    const uint32_t bytes = (uint32_t)((kGemmBM + 2 * BN) * kGemmKC * sizeof(double));
 
     if (tid == 0) {
         for (int s = 0; s < kGemmStages; ++s) mbar_init(&sm.full[s], 1);
@@ -1629,12 +1647,14 @@ __device__ __forceinline__ void gemm_body(const DevProblem &P, int J, int row_lo
     if (tid == 0)
         for (int s = 0; s < kGemmStages && s < nk; ++s) issue(s, s);
 
-    const int tc = tid & 15, tr = tid >> 4;
+    // Thread (tr, tc) owns rows RPT*tr .. RPT*tr+RPT-1 and columns 4*tc ..
+    // 4*tc+3; either way warp w owns rows 8w .. 8w+7.
+    const int tc = tid % TC, tr = tid / TC;
     const int wrow = row0 + 8 * (tid >> 5);
     const bool live = wrow + 8 > row_lo && wrow < row_hi;      // warp-uniform
-    double aw[4][4], az[4][4];
+    double aw[RPT][4], az[RPT][4];
 #pragma unroll
-    for (int r = 0; r < 4; ++r)
+    for (int r = 0; r < RPT; ++r)
 #pragma unroll
         for (int c = 0; c < 4; ++c) aw[r][c] = az[r][c] = 0.0;
 
@@ -1647,17 +1667,25 @@ __device__ __forceinline__ void gemm_body(const DevProblem &P, int J, int row_lo
         if (!__syncthreads_and(got)) { ok = false; break; }
         const int kmax = live ? min(kGemmKC, b - kc * kGemmKC) : 0;
         for (int kk = 0; kk < kmax; ++kk) {
-            const double2 a01 = *reinterpret_cast<const double2 *>(&sm.A[s][kk][4 * tr]);
-            const double2 a23 = *reinterpret_cast<const double2 *>(&sm.A[s][kk][4 * tr + 2]);
+            double a[RPT];
+            if constexpr (RPT == 4) {
+                const double2 a01 = *reinterpret_cast<const double2 *>(&sm.A[s][kk][4 * tr]);
+                const double2 a23 = *reinterpret_cast<const double2 *>(&sm.A[s][kk][4 * tr + 2]);
+                a[0] = a01.x;
+                a[1] = a01.y;
+                a[2] = a23.x;
+                a[3] = a23.y;
+            } else {
+                a[0] = sm.A[s][kk][tr];
+            }
             const double2 w01 = *reinterpret_cast<const double2 *>(&sm.W[s][kk][4 * tc]);
             const double2 w23 = *reinterpret_cast<const double2 *>(&sm.W[s][kk][4 * tc + 2]);
             const double2 z01 = *reinterpret_cast<const double2 *>(&sm.Z[s][kk][4 * tc]);
             const double2 z23 = *reinterpret_cast<const double2 *>(&sm.Z[s][kk][4 * tc + 2]);
-            const double a[4] = {a01.x, a01.y, a23.x, a23.y};
             const double w[4] = {w01.x, w01.y, w23.x, w23.y};
             const double z[4] = {z01.x, z01.y, z23.x, z23.y};
 #pragma unroll
-            for (int r = 0; r < 4; ++r)
+            for (int r = 0; r < RPT; ++r)
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
                     aw[r][c] = fma(a[r], w[c], aw[r][c]);
@@ -1684,20 +1712,28 @@ __device__ __forceinline__ void gemm_body(const DevProblem &P, int J, int row_lo
     // along the rows, and the per-tile maxima of |y| are reduced across the
     // warp before one atomic per (tile, column).
     constexpr int kEpiLd = kGemmBM + 2;                       // padded pitch: spreads the banks
-    static_assert(2 * kGemmBN * kEpiLd * sizeof(double) <= sizeof(sm.A) + sizeof(sm.W) + sizeof(sm.Z),
+    static_assert(2 * BN * kEpiLd * sizeof(double) <= sizeof(sm.A) + sizeof(sm.W) + sizeof(sm.Z),
                   "epilogue staging must fit the operand ring");
     __syncthreads();
     double *eaw = &sm.A[0][0][0];
-    double *eaz = eaw + kGemmBN * kEpiLd;
+    double *eaz = eaw + BN * kEpiLd;
     if (live) {
+        if constexpr (RPT == 4) {
 #pragma unroll
-        for (int c = 0; c < 4; ++c)
+            for (int c = 0; c < 4; ++c)
 #pragma unroll
-            for (int r = 0; r < 4; r += 2) {
-                const int at = (4 * tc + c) * kEpiLd + 4 * tr + r;
-                *reinterpret_cast<double2 *>(&eaw[at]) = make_double2(aw[r][c], aw[r + 1][c]);
-                *reinterpret_cast<double2 *>(&eaz[at]) = make_double2(az[r][c], az[r + 1][c]);
+                for (int r = 0; r < 4; r += 2) {
+                    const int at = (4 * tc + c) * kEpiLd + 4 * tr + r;
+                    *reinterpret_cast<double2 *>(&eaw[at]) = make_double2(aw[r][c], aw[r + 1][c]);
+                    *reinterpret_cast<double2 *>(&eaz[at]) = make_double2(az[r][c], az[r + 1][c]);
+                }
+        } else {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                eaw[(4 * tc + c) * kEpiLd + tr] = aw[0][c];
+                eaz[(4 * tc + c) * kEpiLd + tr] = az[0][c];
             }
+        }
     }
     __syncthreads();
     if constexpr (kCplx) {
@@ -1708,15 +1744,15 @@ __device__ __forceinline__ void gemm_body(const DevProblem &P, int J, int row_lo
     const size_t Spad = (size_t)P.Spad;
     unsigned long long *ynb = reinterpret_cast<unsigned long long *>(P.ynorm);
     const int lane = tid & 31;
-    const int er = tid & (kGemmBM - 1), cg = tid >> 6;       // row; 16-column group (warp-uniform)
+    const int er = tid & (kGemmBM - 1), cg = tid >> 6;       // row; BN/4-column group (warp-uniform)
     const int row = row0 + er;
     const bool rowok = row >= row_lo && row < row_hi;
     int I = P.T - 1 - (P.n - 1 - row) / P.tlsz;
     if (I < 0) I = 0;
     const int key = rowok ? I : -1;                           // tile of the row; rows are consecutive
     const double hl1 = rowok ? P.H[row + (size_t)(l - 1) * P.ldh] : 0.0;   // Part-1 column
-    for (int j = 0; j < kGemmBN / 4; ++j) {
-        const int cc = cg * (kGemmBN / 4) + j;
+    for (int j = 0; j < BN / 4; ++j) {
+        const int cc = cg * (BN / 4) + j;
         const int col = col0 + cc;
         if (col >= P.S) break;
         const double pik = P.pi[col], w0 = P.W[col], zl = P.zlast[col], mu = P.wr[col], yt = P.ytil[col];
@@ -1770,6 +1806,41 @@ k_gemm(DevProblem P, int J, int row_lo, int row_hi, const __grid_constant__ CUte
 }
 
 __global__ void __launch_bounds__(256, 2)
+k_gemm_n(DevProblem P, int J, int row_lo, int row_hi, const __grid_constant__ CUtensorMap tmH,
+         const __grid_constant__ CUtensorMap tmW, const __grid_constant__ CUtensorMap tmZ) {
+    gemm_body<false, kGemmBNNarrow>(P, J, row_lo, row_hi, blockIdx.x, blockIdx.y, &tmH, &tmW, &tmZ);
+}
+
+// The GEMM over [row_lo, row_hi) with 16-column tiles; tmW/tmZ must have a
+// 16 x 16 box.
+cudaError_t launch_gemm_narrow(const DevProblem &P, int J, int row_lo, int row_hi, const CUtensorMap &tmH,
+                               const CUtensorMap &tmW, const CUtensorMap &tmZ, cudaStream_t st) {
+    if (row_hi <= row_lo || P.S <= 0) return cudaSuccess;
+    static size_t configured = 0;
+    const size_t smem = gemm_narrow_smem_bytes();
+    const cudaError_t e = raise_smem_limit((const void *)k_gemm_n, &configured, smem);
+    if (e != cudaSuccess) return e;
+    const int span = row_hi - (row_lo & ~7);
+    dim3 g((span + kGemmBM - 1) / kGemmBM, (P.S + kGemmBNNarrow - 1) / kGemmBNNarrow);
+    k_gemm_n<<<g, 256, smem, st>>>(P, J, row_lo, row_hi, tmH, tmW, tmZ);
+    return cudaGetLastError();
+}
+
+// Whether the 16-column tiles should serve a GEMM over `rows` rows: when the
+// 64-column tiles would fill fewer than half of the SMs.
+bool gemm_prefers_narrow(int rows, int S) {
+    static const int sms = []() {
+        int dev = 0, n = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return 0;
+        return n;
+    }();
+    const long ctas = (long)((rows + kGemmBM - 1) / kGemmBM) * ((S + kGemmBN - 1) / kGemmBN);
+    return sms > 0 && 2 * ctas < sms;
+}
+
+__global__ void __launch_bounds__(256, 2)
 k_gemm_c(DevProblem P, int J, int row_lo, int row_hi, const __grid_constant__ CUtensorMap tmH,
          const __grid_constant__ CUtensorMap tmW, const __grid_constant__ CUtensorMap tmZ) {
     gemm_body<true>(P, J, row_lo, row_hi, blockIdx.x, blockIdx.y, &tmH, &tmW, &tmZ);
@@ -1811,8 +1882,18 @@ cudaError_t launch_gemm_c(const DevProblem &P, int J, int row_lo, int row_hi, co
 // three-accumulator 2-norm and the convergence test ||y|| > 0.1/sqrt(n)
 // (:33-40, :229-273).  Rows move through shared memory 32 at a time so that
 // the column-major block is read and written coalesced.
+// Per-warp staging of finalize_body_buf: a 32-row block of X (transposed)
+// and the rotations of those rows, each loaded coalesced with all its loads
+// in flight at once, so the sequential row loop reads shared memory only.
+struct FinalizeBuf {
+    double x[32][33];
+    double c[32][33];
+    double s[32][33];
+};
+
 __device__ __forceinline__ void finalize_body_buf(const DevProblem &P, int bx, double *colnorm, int *status,
-                                                  double *scale_out, double (*buf)[33]) {
+                                                  double *scale_out, FinalizeBuf &fb) {
+    double (*buf)[33] = fb.x;
     const int lane = threadIdx.x & 31;
     const int k0 = bx * 32;
     const int k = k0 + lane;
@@ -1837,6 +1918,11 @@ __device__ __forceinline__ void finalize_body_buf(const DevProblem &P, int bx, d
             const int kc = k0 + c;
             if (kc < P.S && lane < rows) buf[lane][c] = P.X[r0 + lane + (size_t)kc * P.ldx];
         }
+        for (int t = 0; t < rows; ++t) {
+            const size_t at = (size_t)(r0 + t) * Spad + k;
+            fb.c[t][lane] = act ? P.Cr[at] : 0.0;
+            fb.s[t][lane] = act ? P.Sr[at] : 0.0;
+        }
         __syncwarp();
         for (int t = 0; t < rows; ++t) {
             const int i = r0 + t;
@@ -1849,8 +1935,8 @@ __device__ __forceinline__ void finalize_body_buf(const DevProblem &P, int bx, d
                 continue;
             }
             const double tau2 = is_one(alpha) ? buf[t][lane] : alpha * buf[t][lane];
-            const double c = act ? P.Cr[(size_t)i * Spad + k] : 0.0;
-            const double s = act ? P.Sr[(size_t)i * Spad + k] : 0.0;
+            const double c = fb.c[t][lane];
+            const double s = fb.s[t][lane];
             const double out = fma(c, tau1, -(s * tau2));
             tau1 = fma(c, tau2, s * tau1);
             acc.add(out);
@@ -1879,8 +1965,8 @@ __device__ __forceinline__ void finalize_body_buf(const DevProblem &P, int bx, d
 
 __device__ __forceinline__ void finalize_body(const DevProblem &P, int bx, double *colnorm, int *status,
                                               double *scale_out) {
-    __shared__ double buf[32][33];
-    finalize_body_buf(P, bx, colnorm, status, scale_out, buf);
+    __shared__ FinalizeBuf fb;
+    finalize_body_buf(P, bx, colnorm, status, scale_out, fb);
 }
 
 __global__ void __launch_bounds__(32) k_finalize(DevProblem P, double *colnorm, int *status,
@@ -2121,7 +2207,7 @@ int queue_diag_warps(int bmax) {
 size_t queue_smem_bytes(int bmax) {
     size_t need = gemm_smem_bytes();
     const size_t diag = queue_diag_warps(bmax) * queue_diag_warp_bytes(bmax);
-    const size_t fin = (size_t)kQueueFinalBlocks * 32 * 33 * sizeof(double);
+    const size_t fin = (size_t)kQueueFinalBlocks * sizeof(FinalizeBuf);
     if (diag + 128 > need) need = diag + 128;     // + room to align the base to 128 bytes
     if (fin + 128 > need) need = fin + 128;
     return need;
@@ -2215,7 +2301,7 @@ __global__ void __launch_bounds__(kQueueThreads, 2) k_queue(const DevProblem *__
                 const int blk = it.z * kQueueFinalBlocks + wid;
                 if (wid < kQueueFinalBlocks && blk * 32 < P.S)
                     finalize_body_buf(P, blk, P.colnorm, P.status, P.scale,
-                                      reinterpret_cast<double(*)[33]>(smd + (size_t)wid * 32 * 33));
+                                      reinterpret_cast<FinalizeBuf *>(smd)[wid]);
                 break;
             }
             case qkNormalize: {

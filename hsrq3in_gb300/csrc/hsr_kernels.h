@@ -70,6 +70,8 @@ cudaError_t launch_norms(const DevProblem &P, unsigned long long *Hn_bits,
 cudaError_t launch_init(const DevProblem &P, int mode, const double *eps3_dev,
                         int its, cudaStream_t st);
 cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st);
+// Shifts per CTA the diagonal kernel uses for S shifts: 8, 16 or 32.
+int diag_shifts_per_cta(int S);
 size_t diag_smem_bytes(int b);
 // CTAs per SM of the diagonal kernels with v/y in shared memory (0: v/y do
 // not fit).  More CTAs than one resident wave -> v/y go to global scratch.
@@ -80,6 +82,12 @@ cudaError_t launch_part1(const DevProblem &P, int J, cudaStream_t st);
 cudaError_t launch_gemm(const DevProblem &P, int J, int row_lo, int row_hi, const CUtensorMap &tmH,
                         const CUtensorMap &tmW, const CUtensorMap &tmZ, cudaStream_t st);
 size_t gemm_smem_bytes();
+// The same GEMM with 16-column tiles (tmW/tmZ with a 16 x 16 box), for the
+// short GEMM that gates the next diagonal solve when 64-column tiles would
+// leave most SMs idle (gemm_prefers_narrow).
+cudaError_t launch_gemm_narrow(const DevProblem &P, int J, int row_lo, int row_hi, const CUtensorMap &tmH,
+                               const CUtensorMap &tmW, const CUtensorMap &tmZ, cudaStream_t st);
+bool gemm_prefers_narrow(int rows, int S);
 cudaError_t launch_finalize(const DevProblem &P, double *colnorm, int *status,
                             double *scale_out, cudaStream_t st);
 cudaError_t launch_normalize(const DevProblem &P, const double *colnorm,
@@ -132,7 +140,7 @@ struct QueueItem {
     int pad0, pad1;
 };
 constexpr int kQueueInitCols = 8;
-constexpr int kQueueFinalBlocks = 8;
+constexpr int kQueueFinalBlocks = 2;
 constexpr int kQueueThreads = 256;
 // Diagonal blocks one item runs (a warp each, v/y in shared memory) for tile
 // height up to bmax, and the shared memory of the persistent kernel.
@@ -167,6 +175,7 @@ cudaError_t launch_probe_dfma(double *out, int blocks, int iters, cudaStream_t s
 cudaError_t launch_probe_dmma(double *out, int blocks, int iters, cudaStream_t st);
 
 constexpr int kGemmBM = 64, kGemmBN = 64, kGemmKC = 16, kGemmStages = 3;
+constexpr int kGemmBNNarrow = 16;       // column tile of the narrow GEMM (launch_gemm_narrow)
 constexpr int kGemmTopFlag = 1 << 30;   // batched GEMM item: rows of tile J-1
 
 }  // namespace hsr

@@ -249,6 +249,19 @@ int hsr_batch_plan_set_engine(hsr_batch_plan *plan, int engine, void *stream);
 int hsr_batch_plan_queue_info(const hsr_batch_plan *plan, int *engine, long *items, int *grid,
                               int *diag_warps, int *in_graph);
 
+/* Plain-path tile size: times hsr_inverse_iteration_device on the caller's
+ * problem (device pointers; dwr is restored, dvr overwritten) for each
+ * candidate tlsz in `cand`, records the fastest for order n and returns it;
+ * ms_out[i] (optional) gets candidate i's time.  A tlsz of 0 passed to
+ * tiled_inverse_iteration, hsr_inverse_iteration_ex or
+ * hsr_inverse_iteration_device then selects the recorded size of the
+ * nearest tuned order within a factor of two (hsr_autotune_plain_tlsz), else
+ * a default by order.  The reference takes tlsz from its caller only
+ * (main.c:40-44); no reference counterpart. */
+int hsr_autotune_plain(int n, const double *dH, int lddH, int nrhs, double *dwr, double *dvr, int lddvr,
+                       const int *cand, int ncand, double *ms_out, void *stream);
+int hsr_autotune_plain_tlsz(int n);
+
 /* Tile size for batches whose orders lie in [n_lo, n_hi]: the size that
  * hsr_autotune_batch measured fastest on this GPU for the sample whose order
  * range overlaps [n_lo, n_hi] the most, else a default. */
@@ -324,8 +337,13 @@ void hsr_server_destroy(hsr_server *srv);
  * HSR_ERR_ARG before any work is enqueued.  The array is shared by all calls:
  * calls that overlap on the GPU race and must be serialised by the caller.
  * The first call on a device looks up the array's address on that device;
- * make that first call before any stream capture.  `status` (host, optional,
- * [nrhs]) receives 1 for converged columns. */
+ * make that first call before any stream capture.  Under CUDA's default lazy
+ * module loading that first call also loads the library's kernels and commits
+ * the array on the device, so make it before a pool takes the free memory (or
+ * set CUDA_MODULE_LOADING=EAGER).  The call returns after the solve has
+ * finished (it synchronises `stream`); after a failure it first waits for the
+ * work it had enqueued.  hsr_last_status() reports its status.  `status`
+ * (host, optional, [nrhs]) receives 1 for converged columns. */
 #define HSR_NOALLOC_MAX_N 256
 #define HSR_NOALLOC_MAX_NRHS 256
 #define HSR_NOALLOC_SCRATCH_BYTES (8u << 20)

@@ -297,3 +297,28 @@ def test_diag_forms_bitwise(gpu_lib, monkeypatch, sc, n, tlsz, nrhs, seed):
     assert np.array_equal(dev["vr"], orc["vr"])
     assert np.array_equal(dev["perturbed"], orc["perturbed"])
     assert np.array_equal(dev["scale"], orc["colscale"])
+
+
+def test_plain_autotune_and_tlsz_zero(gpu_lib):
+    """hsr_autotune_plain records the fastest candidate for the order, and
+    tlsz = 0 then solves with it: the same result bit for bit as passing that
+    tile size."""
+    import torch
+    import hsrq3in_gb300 as hsr
+    from hsrq3in_gb300 import _lib
+    n = 260
+    H, lam = G.real_spectrum(n, 41)
+    wr = G.perturbed_shifts(lam, 42)
+    dev = torch.device("cuda", 0)
+    ld = n + (n & 1)
+    dH = torch.zeros((n, ld), dtype=torch.float64, device=dev)
+    dH[:, :n] = torch.from_numpy(np.ascontiguousarray(H.T)).to(dev)
+    dwr = torch.from_numpy(wr.copy()).to(dev)
+    dX = torch.empty((n, ld), dtype=torch.float64, device=dev)
+    best, ms = hsr.autotune_plain(dH, dwr, dX, candidates=(32, 64, 96))
+    assert best in (32, 64, 96) and all(0 < t < 1e299 for t in ms)
+    assert np.array_equal(dwr.cpu().numpy(), wr)                 # restored
+    assert _lib.load().hsr_autotune_plain_tlsz(n) == best
+    a = hsr.inverse_iteration(H, wr, 0, 16)
+    b = hsr.inverse_iteration(H, wr, best, 16)
+    assert np.array_equal(a["vr"], b["vr"]) and np.array_equal(a["wr"], b["wr"])
