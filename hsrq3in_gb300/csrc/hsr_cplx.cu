@@ -62,7 +62,7 @@ __global__ void k_init_c(DevProblem P, int mode, const double *eps3_dev, int its
         xi[i] = 0.0;
     }
     if (blockIdx.x == 0) {
-        const double ub = mode == 1 ? fmax(fmax(eps3, tmp), fabs(tmp - eps3 / sq)) : eps3;
+        const double ub = mode == 1 ? fmax(fmax(eps3, tmp), absd(tmp - eps3 / sq)) : eps3;
         for (int I = threadIdx.x; I < P.T; I += blockDim.x) {
             P.beta[(size_t)I * P.Spad + k] = sc_one(P.is);
             P.beta[(size_t)I * P.Spad + k + 1] = sc_one(P.is);

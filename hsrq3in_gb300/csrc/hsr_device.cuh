@@ -28,6 +28,12 @@ constexpr double kOmegaInv = 1.e-300;
 // patterns equals the order of the magnitudes, so a max over them is an
 // integer-pipe max; NaN patterns map to 0 so that NaN never wins, matching
 // vector_infnorm (utils.h:75-85).
+// |x| by clearing the sign bit on the integer pipe: the same bits as fabs(x)
+// for every input (NaN included), without an FP64-pipe instruction, which on
+// this part costs as much issue time as a multiply.
+__device__ __forceinline__ double absd(double x) {
+    return __longlong_as_double(__double_as_longlong(x) & 0x7fffffffffffffffLL);
+}
 __device__ __forceinline__ unsigned long long abs_bits(double x) {
     unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
     return b > 0x7ff0000000000000ULL ? 0ULL : b;
@@ -58,32 +64,43 @@ __device__ __forceinline__ bool is_one(double a) { return ubits(a) == kOneBits; 
 __device__ __forceinline__ bool is_zero(double a) { return (ubits(a) << 1) == 0ULL; }
 __device__ __forceinline__ double neg(double a) { return __longlong_as_double((long long)(ubits(a) ^ 0x8000000000000000ULL)); }
 
+// ------------------------------------------------------- rare branches
+// Every FP64 instruction, taken or not, costs its sub-partition 64 issue
+// cycles on this part (a dependent chain and independent operations alike),
+// so the compiler must not evaluate a rarely taken branch speculatively and
+// select.  Rare branches therefore call non-inlined functions, which it
+// cannot evaluate ahead of the branch.  Each returns exactly the expression
+// the inline code would have computed.
+static __device__ __noinline__ double mul_rare(double a, double b) { return a * b; }
+static __device__ __noinline__ double add_rare(double a, double b) { return a + b; }
+// x scaled by a, skipping the multiplication when a == 1 (1*x == x bit for bit).
+__device__ __forceinline__ double scale_by(double a, double x) { return is_one(a) ? x : mul_rare(a, x); }
+
 // ------------------------------------------------ scaling-factor algebra
 // robust.c:24-121.  `is` selects base-2 exponents (INTSCALING) at run time.
 __device__ __forceinline__ double sc_one(bool is) { return is ? 0.0 : 1.0; }
+static __device__ __noinline__ double pow2_rare(double a) { return ldexp(1.0, (int)a); }
 __device__ __forceinline__ double sc_value(double a, bool is) {
-    if (is) return is_zero(a) ? 1.0 : ldexp(1.0, (int)a);
+    if (is) return is_zero(a) ? 1.0 : pow2_rare(a);
     return a;
 }
 __device__ __forceinline__ double sc_combine(double g, double phi, bool is) {
-    if (is) return is_zero(phi) ? g : phi + g;
-    return is_one(phi) ? g : phi * g;
+    if (is) return is_zero(phi) ? g : add_rare(phi, g);
+    return is_one(phi) ? g : mul_rare(phi, g);
 }
 __device__ __forceinline__ double sc_upscale(double amin, double a, bool is) {
     return is ? ldexp(1.0, (int)(amin - a)) : amin / a;
 }
 __device__ __forceinline__ double sc_min(double a, double b, bool is) { return is ? (a < b ? a : b) : fmin(a, b); }
+static __device__ __noinline__ double sc_min_rare(double a, double b, bool is) { return sc_min(a, b, is); }
 
 // ------------------------------------------------- robust scalar kernels
 // protect_real_division (robust.c:144-166).  Shortcut: with t normal and
 // exponent(b) <= exponent(t) + 989, |b| < 2^990 |t| <= fl(|t| Omega), so
 // neither branch rescales.
-__device__ __forceinline__ double protect_real_division(double b, double t) {
-    const unsigned long long mb = mag(b), mt = mag(t);
-    if (mt >= pow2_bits(-1022) && mt <= kInfBits && mb <= kInfBits && (mb >> 52) < (mt >> 52) + 990)
-        return 1.0;
+static __device__ __noinline__ double protect_real_division_full(double b, double t) {
     double scale = 1.0;
-    const double at = fabs(t), ab = fabs(b);
+    const double at = absd(t), ab = absd(b);
     if (at < kOmegaInv) {
         if (ab > at * kOmega) scale = (at * kOmega) / ab;
     } else {
@@ -91,20 +108,27 @@ __device__ __forceinline__ double protect_real_division(double b, double t) {
     }
     return scale;
 }
+__device__ __forceinline__ double protect_real_division(double b, double t) {
+    const unsigned long long mb = mag(b), mt = mag(t);
+    if (mt >= pow2_bits(-1022) && mt <= kInfBits && mb <= kInfBits && (mb >> 52) < (mt >> 52) + 990)
+        return 1.0;
+    return protect_real_division_full(b, t);
+}
 // protect_sum (robust.c:175-185).  Shortcut: |x|, |y| < 2^995 gives
 // Omega - |y| > 2^995 > |x|.
-__device__ __forceinline__ double protect_sum(double x, double y) {
-    if (mag(x) < pow2_bits(995) && mag(y) < pow2_bits(995)) return 1.0;
+static __device__ __noinline__ double protect_sum_full(double x, double y) {
     double scale = 1.0;
     if ((x > 0 && y > 0) || (x < 0 && y < 0))
-        if (fabs(x) > kOmega - fabs(y)) scale = 0.5;
+        if (absd(x) > kOmega - absd(y)) scale = 0.5;
     return scale;
+}
+__device__ __forceinline__ double protect_sum(double x, double y) {
+    if (mag(x) < pow2_bits(995) && mag(y) < pow2_bits(995)) return 1.0;
+    return protect_sum_full(x, y);
 }
 // protect_update (robust.c:220-262), for t, x, y >= 0.  Shortcut: t, x <
 // 2^497 and y < 2^995 give t*x < 2^994 < Omega - y and t < (Omega - y)/x.
-__device__ __forceinline__ double protect_update(double tnorm, double xnorm, double ynorm, bool is) {
-    if (mag(tnorm) < pow2_bits(497) && mag(xnorm) < pow2_bits(497) && mag(ynorm) < pow2_bits(995))
-        return sc_one(is);
+static __device__ __noinline__ double protect_update_full(double tnorm, double xnorm, double ynorm, bool is) {
     double scale = 1.0;
     if (xnorm <= 1.0) {
         if (tnorm * xnorm > kOmega - ynorm) scale = 0.5;
@@ -113,28 +137,40 @@ __device__ __forceinline__ double protect_update(double tnorm, double xnorm, dou
     }
     return is ? (double)ilogb(scale) : scale;
 }
+__device__ __forceinline__ double protect_update(double tnorm, double xnorm, double ynorm, bool is) {
+    if (mag(tnorm) < pow2_bits(497) && mag(xnorm) < pow2_bits(497) && mag(ynorm) < pow2_bits(995))
+        return sc_one(is);
+    return protect_update_full(tnorm, xnorm, ynorm, is);
+}
 // protect_double_update (robust.c:270-285)
 __device__ __forceinline__ double protect_double_update(double t1, double x1, double t2, double x2,
                                                         double y, bool is) {
     const double a1 = protect_update(t1, x1, y, is);
     const double a2 = protect_update(t2, x2, y, is);
     if (ubits(a1) == ubits(a2)) return a1;
-    return is ? (a1 < a2 ? a1 : a2) : fmin(a1, a2);
+    return sc_min_rare(a1, a2, is);
+}
+// Rare parts of solve_1x1: the rescaled difference and the scaling factor.
+static __device__ __noinline__ double solve_1x1_scaled_diff(double s, double t, double lambda) {
+    return (s * t) - (s * lambda);
+}
+static __device__ __noinline__ double solve_1x1_scale(double alpha, double s, bool is) {
+    return is ? (double)ilogb(alpha / s) : alpha / s;
 }
 // solve_1x1_real_system (robust.c:422-479); returns 1 if |t-lambda| < smin.
 __device__ __forceinline__ int solve_1x1(double smin, double t, double lambda, double &x,
                                          double &scale, bool is) {
     int info = 0;
     const double s = protect_sum(t, neg(lambda));
-    double csr = is_one(s) ? t - lambda : (s * t) - (s * lambda);
-    if (mag(csr) < ubits(smin)) {          // fabs(csr) < smin, smin > 0
+    double csr = is_one(s) ? t - lambda : solve_1x1_scaled_diff(s, t, lambda);
+    if (mag(csr) < ubits(smin)) {          // absd(csr) < smin, smin > 0
         csr = smin;
         info = 1;
     }
     const double alpha = protect_real_division(x, csr);
-    x = is_one(alpha) ? x / csr : (alpha * x) / csr;
+    x = scale_by(alpha, x) / csr;
     if (is_one(alpha) && is_one(s)) scale = sc_one(is);
-    else scale = is ? (double)ilogb(alpha / s) : alpha / s;
+    else scale = solve_1x1_scale(alpha, s, is);
     return info;
 }
 
@@ -156,15 +192,15 @@ __device__ __forceinline__ void givens(double f, double g, double &c, double &s)
         c = 0.0; sv = copysign(1.0, g);
     } else if (mf > kRtminBits && mf < kRtmaxBits && mg > kRtminBits && mg < kRtmaxBits) {
         const double d = sqrt(f * f + g * g);
-        c = fabs(f) / d;
+        c = absd(f) / d;
         const double r = copysign(d, f);
         sv = g / r;
     } else {
-        const double f1 = fabs(f), g1 = fabs(g);
+        const double f1 = absd(f), g1 = absd(g);
         const double u = fmin(safmax, fmax(safmin, fmax(f1, g1)));
         const double fs = f / u, gs = g / u;
         const double d = sqrt(fs * fs + gs * gs);
-        c = fabs(fs) / d;
+        c = absd(fs) / d;
         const double r = copysign(d, f);
         sv = gs / r;
     }
@@ -179,14 +215,21 @@ constexpr double kTbig = 0x1p+486;
 constexpr double kSsml = 0x1p+537;
 constexpr double kSbig = 0x1p-538;
 
+// Scaled square accumulation of the rare big and small ranges (not inlined,
+// so the common middle range evaluates one fma).
+static __device__ __noinline__ double nrm3_scaled_sq(double ax, double sc, double acc) {
+    const double t = ax * sc;
+    return fma(t, t, acc);
+}
+
 struct Nrm3 {
     double asml, amed, abig;
     __device__ __forceinline__ void init() { asml = amed = abig = 0.0; }
     __device__ __forceinline__ void add(double x) {
-        const double ax = fabs(x);
+        const double ax = absd(x);
         const unsigned long long m = mag(x);
-        if (m > pow2_bits(486) && m <= kInfBits) { const double t = ax * kSbig; abig = fma(t, t, abig); }
-        else if (m < pow2_bits(-511)) { const double t = ax * kSsml; asml = fma(t, t, asml); }
+        if (m > pow2_bits(486) && m <= kInfBits) abig = nrm3_scaled_sq(ax, kSbig, abig);
+        else if (m < pow2_bits(-511)) asml = nrm3_scaled_sq(ax, kSsml, asml);
         else amed = fma(ax, ax, amed);
     }
     __device__ __forceinline__ double finish() const {
@@ -220,7 +263,7 @@ struct dcplx {
 };
 __device__ __forceinline__ dcplx cmk(double re, double im) { return dcplx{re, im}; }
 // LAPACK's CABS1: |Re z| + |Im z|, an upper bound of |z| and of each part.
-__device__ __forceinline__ double cabs1(dcplx z) { return fabs(z.re) + fabs(z.im); }
+__device__ __forceinline__ double cabs1(dcplx z) { return absd(z.re) + absd(z.im); }
 __device__ __forceinline__ dcplx cmul(dcplx a, dcplx b) {           // a b
     return cmk(fma(a.re, b.re, -(a.im * b.im)), fma(a.re, b.im, a.im * b.re));
 }
@@ -253,10 +296,10 @@ __device__ __forceinline__ dcplx crot_next(double c, dcplx s, dcplx t1, dcplx t2
 __device__ __forceinline__ double protect_mul(double tnorm, double xnorm) {
     if (mag(tnorm) < pow2_bits(497) && mag(xnorm) < pow2_bits(497)) return 1.0;
     double scale = 1.0;
-    if (fabs(xnorm) <= 1.0) {
-        if (fabs(tnorm) * fabs(xnorm) > kOmega) scale = 0.5;
+    if (absd(xnorm) <= 1.0) {
+        if (absd(tnorm) * absd(xnorm) > kOmega) scale = 0.5;
     } else {
-        if (fabs(tnorm) > kOmega / fabs(xnorm)) scale = 0.5 / fabs(xnorm);
+        if (absd(tnorm) > kOmega / absd(xnorm)) scale = 0.5 / absd(xnorm);
     }
     return scale;
 }
@@ -274,14 +317,14 @@ __device__ __forceinline__ void c_dladiv2(double a, double b, double c, double d
             double s = protect_sum(a, br);
             res = (s * a) + (s * br);
             alpha = s * alpha;
-            s = protect_mul(fabs(t), fabs(res));
+            s = protect_mul(absd(t), absd(res));
             res = (s * res) * t;
             alpha = s * alpha;
         } else {
             // a t + (b t) r
-            const double s1 = protect_mul(fabs(t), fabs(a));
+            const double s1 = protect_mul(absd(t), absd(a));
             double tmp1 = (s1 * a) * t;
-            const double s2 = protect_mul(fabs(t), fabs(b));
+            const double s2 = protect_mul(absd(t), absd(b));
             double tmp2 = (s2 * b) * t;
             tmp2 = tmp2 * r;
             const double smin = fmin(s1, s2);
@@ -297,14 +340,14 @@ __device__ __forceinline__ void c_dladiv2(double a, double b, double c, double d
         const double s1 = protect_real_division(b, c);
         alpha = s1 * alpha;
         double tmp = (s1 * b) / c;
-        const double s2 = protect_mul(fabs(d), fabs(tmp));
+        const double s2 = protect_mul(absd(d), absd(tmp));
         alpha = s2 * alpha;
         tmp = d * (s2 * tmp);
         a = (s1 * s2) * a;
         double s = protect_sum(a, tmp);
         alpha = s * alpha;
         tmp = (s * a) + (s * tmp);
-        s = protect_mul(fabs(tmp), fabs(t));
+        s = protect_mul(absd(tmp), absd(t));
         alpha = s * alpha;
         res = (s * tmp) * t;
     }
@@ -333,7 +376,7 @@ __device__ __forceinline__ void c_dladiv1(double a, double b, double c, double d
 }
 __device__ __forceinline__ void c_dladiv(double a, double b, double c, double d, double &xr, double &xi,
                                          double &scale) {
-    if (fabs(d) < fabs(c)) {
+    if (absd(d) < absd(c)) {
         c_dladiv1(a, b, c, d, xr, xi, scale);
     } else {
         c_dladiv1(b, a, d, c, xr, xi, scale);
@@ -348,7 +391,7 @@ __device__ __forceinline__ int csolve_1x1(double smin, double tr, double ti, dou
     const double s = fmin(protect_sum(tr, -lr), protect_sum(ti, -li));
     double csr = (s * tr) - (s * lr);
     double csi = (s * ti) - (s * li);
-    if (fabs(csr) + fabs(csi) < smin) {
+    if (absd(csr) + absd(csi) < smin) {
         csr = smin;
         csi = 0.0;
         info = 1;
@@ -380,8 +423,8 @@ __device__ __forceinline__ void cgivens(dcplx f, double g, double &c, dcplx &sg)
         sg = cmk(-copysign(1.0, g), 0.0);
         return;
     }
-    const int ef = exp_clamped(fmax(fabs(f.re), fabs(f.im)));
-    const int eg = exp_clamped(fabs(g));
+    const int ef = exp_clamped(fmax(absd(f.re), absd(f.im)));
+    const int eg = exp_clamped(absd(g));
     const int e = ef > eg ? ef : eg;
     const double uf = pow2d(-ef);
     const double fsr = f.re * uf, fsi = f.im * uf;

@@ -58,7 +58,7 @@ __global__ void k_tile_rowsums(DevProblem P, unsigned long long *Hn_bits,
     const int c0 = P.fr[J], c1 = P.fr[J + 1];
     double sum = 0.0;
     const double *row = P.H + i;
-    for (int c = c0; c < c1; ++c) sum += fabs(row[(size_t)c * P.ldh]);
+    for (int c = c0; c < c1; ++c) sum += absd(row[(size_t)c * P.ldh]);
     if (sum != sum) atomicOr(nan_flag, 1 << 1);
     atomicMax(&Hn_bits[I + (size_t)J * T], (unsigned long long)__double_as_longlong(sum));
     if (J > I) {
@@ -72,7 +72,7 @@ __global__ void k_full_rowsums(DevProblem P, unsigned long long *hinf_bits, int 
     if (i >= P.n) return;
     double sum = 0.0;
     const double *row = P.H + i;
-    for (int c = 0; c < P.n; ++c) sum += fabs(row[(size_t)c * P.ldh]);
+    for (int c = 0; c < P.n; ++c) sum += absd(row[(size_t)c * P.ldh]);
     if (sum != sum) atomicOr(nan_flag, 1);
     atomicMax(hinf_bits, (unsigned long long)__double_as_longlong(sum));
 }
@@ -113,7 +113,7 @@ __global__ void k_init(DevProblem P, int mode, const double *eps3_dev, int its) 
         }
     }
     if (blockIdx.x == 0) {
-        const double ub = fmax(fmax(eps3, tmp), fabs(tmp - eps3 / sq));
+        const double ub = fmax(fmax(eps3, tmp), absd(tmp - eps3 / sq));
         for (int I = threadIdx.x; I < P.T; I += blockDim.x) {
             P.beta[(size_t)I * P.Spad + k] = sc_one(P.is);
             if (mode == 0) P.ynorm[(size_t)I * P.Spad + k] = eps3;
@@ -235,7 +235,7 @@ __device__ __forceinline__ void diag_body_1w(const DevProblem &P, int J, int bx,
     }
 
     const double mu = act ? P.wr[k] : 0.0;
-    const double smin = fmax(DBL_EPSILON / 2 * fabs(mu), P.smlnum);
+    const double smin = fmax(DBL_EPSILON / 2 * absd(mu), P.smlnum);
     const double Hnorm = P.Hn[J + (size_t)J * P.T];
     double beta = act ? P.beta[(size_t)J * Spad + k] : sc_one(is);
     int pert = 0;
@@ -291,29 +291,29 @@ __device__ __forceinline__ void diag_body_1w(const DevProblem &P, int J, int bx,
             beta = sc_combine(beta, phi, is);
             a1 = sc_value(phi, is);
             if (!is_one(a1)) {
-                yjm1 = a1 * yjm1;
-                ymax = abs_bits(a1 * from_bits(ymax));
+                yjm1 = mul_rare(a1, yjm1);
+                ymax = abs_bits(mul_rare(a1, from_bits(ymax)));
             }
             // y(j-1) (solve-task.c:84-90).
-            phi = protect_double_update(fabs(vjm1), fabs(yj), fabs(hdiag), fabs(yj), fabs(yjm1), is);
+            phi = protect_double_update(absd(vjm1), absd(yj), absd(hdiag), absd(yj), absd(yjm1), is);
             a2 = sc_value(phi, is);
             if (!is_one(a2)) {
-                yj = a2 * yj;
-                yjm1 = a2 * yjm1;
-                ymax = abs_bits(a2 * from_bits(ymax));
+                yj = mul_rare(a2, yj);
+                yjm1 = mul_rare(a2, yjm1);
+                ymax = abs_bits(mul_rare(a2, from_bits(ymax)));
             }
             beta = sc_combine(beta, phi, is);
             yc = yj * c;
             ys = yj * s;
             yjm1 = fma(ys, hdiag, fma(-yc, vjm1, yjm1));
             // y(0:j-2) (solve-task.c:92-100).
-            phi = protect_double_update(from_bits(vmax), fabs(yj), Hnorm, fabs(yj), from_bits(ymax), is);
+            phi = protect_double_update(from_bits(vmax), absd(yj), Hnorm, absd(yj), from_bits(ymax), is);
             a3 = sc_value(phi, is);
             if (!is_one(a3)) {
-                yj = a3 * yj;
-                yjm1 = a3 * yjm1;
-                yc = yj * c;
-                ys = yj * s;
+                yj = mul_rare(a3, yj);
+                yjm1 = mul_rare(a3, yjm1);
+                yc = mul_rare(yj, c);
+                ys = mul_rare(yj, s);
             }
             beta = sc_combine(beta, phi, is);
         }
@@ -322,9 +322,9 @@ __device__ __forceinline__ void diag_body_1w(const DevProblem &P, int J, int bx,
             // Rare: the whole-vector scale() also reaches the solved rows j+1 .. b-1.
             for (int i = j + 1; i < b; ++i) {
                 double t = Y(i);
-                if (!is_one(a1)) t = a1 * t;
-                if (!is_one(a2)) t = a2 * t;
-                if (!is_one(a3)) t = a3 * t;
+                t = scale_by(a1, t);
+                t = scale_by(a2, t);
+                t = scale_by(a3, t);
                 Y(i) = t;
             }
         }
@@ -344,9 +344,9 @@ __device__ __forceinline__ void diag_body_1w(const DevProblem &P, int J, int bx,
             if (scaled) {
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    if (!is_one(a1)) yy[q] = a1 * yy[q];
-                    if (!is_one(a2)) yy[q] = a2 * yy[q];
-                    if (!is_one(a3)) yy[q] = a3 * yy[q];
+                    yy[q] = scale_by(a1, yy[q]);
+                    yy[q] = scale_by(a2, yy[q]);
+                    yy[q] = scale_by(a3, yy[q]);
                 }
             }
 #pragma unroll
@@ -369,9 +369,9 @@ __device__ __forceinline__ void diag_body_1w(const DevProblem &P, int J, int bx,
             const double h = hcol[i];
             double yi = Y(i), vi = V(i);
             if (scaled) {
-                if (!is_one(a1)) yi = a1 * yi;
-                if (!is_one(a2)) yi = a2 * yi;
-                if (!is_one(a3)) yi = a3 * yi;
+                yi = scale_by(a1, yi);
+                yi = scale_by(a2, yi);
+                yi = scale_by(a3, yi);
             }
             yi = fma(ys, h, fma(-yc, vi, yi));
             vi = fma(c, h, s * vi);
@@ -534,7 +534,7 @@ __device__ __forceinline__ void diag_body_pipe(const DevProblem &P, int J, int b
     }
 
     const double mu = act ? P.wr[k] : 0.0;
-    const double smin = fmax(DBL_EPSILON / 2 * fabs(mu), P.smlnum);
+    const double smin = fmax(DBL_EPSILON / 2 * absd(mu), P.smlnum);
     const double Hnorm = P.Hn[J + (size_t)J * P.T];
     double beta = act ? P.beta[(size_t)J * Spad + k] : sc_one(is);
     int pert = 0;
@@ -588,12 +588,12 @@ __device__ __forceinline__ void diag_body_pipe(const DevProblem &P, int J, int b
         pert |= solve_1x1(smin, c * vj, s * hsub, yj, phi, is);
         beta = sc_combine(beta, phi, is);
         a1 = sc_value(phi, is);
-        if (!is_one(a1)) yjm1 = a1 * yjm1;
-        phi = protect_double_update(fabs(vjm1), fabs(yj), fabs(hdiag), fabs(yj), fabs(yjm1), is);
+        yjm1 = scale_by(a1, yjm1);
+        phi = protect_double_update(absd(vjm1), absd(yj), absd(hdiag), absd(yj), absd(yjm1), is);
         a2 = sc_value(phi, is);
         if (!is_one(a2)) {
-            yj = a2 * yj;
-            yjm1 = a2 * yjm1;
+            yj = mul_rare(a2, yj);
+            yjm1 = mul_rare(a2, yjm1);
         }
         beta = sc_combine(beta, phi, is);
         yc = yj * c;
@@ -612,15 +612,15 @@ __device__ __forceinline__ void diag_body_pipe(const DevProblem &P, int J, int b
             vmb = umax64(vmb, PM(w, 1));
         }
         double ymax = from_bits(ymb);
-        if (!is_one(a1)) ymax = from_bits(abs_bits(a1 * ymax));
-        if (!is_one(a2)) ymax = from_bits(abs_bits(a2 * ymax));
-        const double phi = protect_double_update(from_bits(vmb), fabs(yj), Hnorm, fabs(yj), ymax, is);
+        if (!is_one(a1)) ymax = from_bits(abs_bits(mul_rare(a1, ymax)));
+        if (!is_one(a2)) ymax = from_bits(abs_bits(mul_rare(a2, ymax)));
+        const double phi = protect_double_update(from_bits(vmb), absd(yj), Hnorm, absd(yj), ymax, is);
         a3 = sc_value(phi, is);
         if (!is_one(a3)) {
-            yj = a3 * yj;
-            yjm1 = a3 * yjm1;
-            yc = yj * c;
-            ys = yj * s;
+            yj = mul_rare(a3, yj);
+            yjm1 = mul_rare(a3, yjm1);
+            yc = mul_rare(yj, c);
+            ys = mul_rare(yj, s);
         }
         beta = sc_combine(beta, phi, is);
         BC(0) = c;
@@ -661,9 +661,9 @@ __device__ __forceinline__ void diag_body_pipe(const DevProblem &P, int J, int b
                 double yi = Y(j - 2);
                 const double vi = V(j - 2);
                 if (scaled) {
-                    if (!is_one(s1)) yi = s1 * yi;
-                    if (!is_one(s2)) yi = s2 * yi;
-                    if (!is_one(s3)) yi = s3 * yi;
+                    yi = scale_by(s1, yi);
+                    yi = scale_by(s2, yi);
+                    yi = scale_by(s3, yi);
                 }
                 yn = fma(sc_ys, h, fma(-sc_yc, vi, yi));
                 vn = fma(sc_c, h, sc_s * vi);
@@ -680,9 +680,9 @@ __device__ __forceinline__ void diag_body_pipe(const DevProblem &P, int J, int b
             if (scaled) {
                 for (int i = j + 1 + ((wid - 1 - (j + 1)) % (NW - 1) + (NW - 1)) % (NW - 1); i < b; i += NW - 1) {
                     double t = Y(i);
-                    if (!is_one(s1)) t = s1 * t;
-                    if (!is_one(s2)) t = s2 * t;
-                    if (!is_one(s3)) t = s3 * t;
+                    t = scale_by(s1, t);
+                    t = scale_by(s2, t);
+                    t = scale_by(s3, t);
                     Y(i) = t;
                 }
             }
@@ -700,9 +700,9 @@ __device__ __forceinline__ void diag_body_pipe(const DevProblem &P, int J, int b
                 if (scaled) {
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
-                        if (!is_one(s1)) yy[q] = s1 * yy[q];
-                        if (!is_one(s2)) yy[q] = s2 * yy[q];
-                        if (!is_one(s3)) yy[q] = s3 * yy[q];
+                        yy[q] = scale_by(s1, yy[q]);
+                        yy[q] = scale_by(s2, yy[q]);
+                        yy[q] = scale_by(s3, yy[q]);
                     }
                 }
 #pragma unroll
@@ -723,9 +723,9 @@ __device__ __forceinline__ void diag_body_pipe(const DevProblem &P, int J, int b
                 const double h = hcol[i];
                 double yi = Y(i), vi = V(i);
                 if (scaled) {
-                    if (!is_one(s1)) yi = s1 * yi;
-                    if (!is_one(s2)) yi = s2 * yi;
-                    if (!is_one(s3)) yi = s3 * yi;
+                    yi = scale_by(s1, yi);
+                    yi = scale_by(s2, yi);
+                    yi = scale_by(s3, yi);
                 }
                 yi = fma(sc_ys, h, fma(-sc_yc, vi, yi));
                 vi = fma(sc_c, h, sc_s * vi);
@@ -904,7 +904,7 @@ __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int
     }
 
     const double mu = act ? P.wr[k] : 0.0;
-    const double smin = fmax(DBL_EPSILON / 2 * fabs(mu), P.smlnum);
+    const double smin = fmax(DBL_EPSILON / 2 * absd(mu), P.smlnum);
     const double Hnorm = P.Hn[J + (size_t)J * P.T];
     double beta = act ? P.beta[(size_t)J * Spad + k] : sc_one(is);
     int pert = 0;
@@ -965,12 +965,12 @@ __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int
         pert |= solve_1x1(smin, c * vj, s * hsub, yj, phi, is);
         beta = sc_combine(beta, phi, is);
         a1 = sc_value(phi, is);
-        if (!is_one(a1)) yjm1 = a1 * yjm1;
-        phi = protect_double_update(fabs(vjm1), fabs(yj), fabs(hdiag), fabs(yj), fabs(yjm1), is);
+        yjm1 = scale_by(a1, yjm1);
+        phi = protect_double_update(absd(vjm1), absd(yj), absd(hdiag), absd(yj), absd(yjm1), is);
         a2 = sc_value(phi, is);
         if (!is_one(a2)) {
-            yj = a2 * yj;
-            yjm1 = a2 * yjm1;
+            yj = mul_rare(a2, yj);
+            yjm1 = mul_rare(a2, yjm1);
         }
         beta = sc_combine(beta, phi, is);
         yc = yj * c;
@@ -986,15 +986,15 @@ __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int
             vmb = umax64(vmb, PM(w, 1));
         }
         double ymax = from_bits(ymb);
-        if (!is_one(a1)) ymax = from_bits(abs_bits(a1 * ymax));
-        if (!is_one(a2)) ymax = from_bits(abs_bits(a2 * ymax));
-        const double phi = protect_double_update(from_bits(vmb), fabs(yj), Hnorm, fabs(yj), ymax, is);
+        if (!is_one(a1)) ymax = from_bits(abs_bits(mul_rare(a1, ymax)));
+        if (!is_one(a2)) ymax = from_bits(abs_bits(mul_rare(a2, ymax)));
+        const double phi = protect_double_update(from_bits(vmb), absd(yj), Hnorm, absd(yj), ymax, is);
         a3 = sc_value(phi, is);
         if (!is_one(a3)) {
-            yj = a3 * yj;
-            yjm1 = a3 * yjm1;
-            yc = yj * c;
-            ys = yj * s;
+            yj = mul_rare(a3, yj);
+            yjm1 = mul_rare(a3, yjm1);
+            yc = mul_rare(yj, c);
+            ys = mul_rare(yj, s);
         }
         beta = sc_combine(beta, phi, is);
         if (store_lane) {
@@ -1036,9 +1036,9 @@ __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int
                 double yi = Y(j - 2);
                 const double vi = V(j - 2);
                 if (scaled) {
-                    if (!is_one(s1)) yi = s1 * yi;
-                    if (!is_one(s2)) yi = s2 * yi;
-                    if (!is_one(s3)) yi = s3 * yi;
+                    yi = scale_by(s1, yi);
+                    yi = scale_by(s2, yi);
+                    yi = scale_by(s3, yi);
                 }
                 yn = fma(sc_ys, h, fma(-sc_yc, vi, yi));
                 vn = fma(sc_c, h, sc_s * vi);
@@ -1058,9 +1058,9 @@ __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int
             if (scaled) {
                 for (int i = j + 1 + rw * RL + rs; i < b; i += NR * RL) {
                     double t = Y(i);
-                    if (!is_one(s1)) t = s1 * t;
-                    if (!is_one(s2)) t = s2 * t;
-                    if (!is_one(s3)) t = s3 * t;
+                    t = scale_by(s1, t);
+                    t = scale_by(s2, t);
+                    t = scale_by(s3, t);
                     Y(i) = t;
                 }
             }
@@ -1079,9 +1079,9 @@ __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int
                 if (scaled) {
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
-                        if (!is_one(s1)) yy[q] = s1 * yy[q];
-                        if (!is_one(s2)) yy[q] = s2 * yy[q];
-                        if (!is_one(s3)) yy[q] = s3 * yy[q];
+                        yy[q] = scale_by(s1, yy[q]);
+                        yy[q] = scale_by(s2, yy[q]);
+                        yy[q] = scale_by(s3, yy[q]);
                     }
                 }
 #pragma unroll
@@ -1102,9 +1102,9 @@ __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int
                 const double h = hcol[i];
                 double yi = Y(i), vi = V(i);
                 if (scaled) {
-                    if (!is_one(s1)) yi = s1 * yi;
-                    if (!is_one(s2)) yi = s2 * yi;
-                    if (!is_one(s3)) yi = s3 * yi;
+                    yi = scale_by(s1, yi);
+                    yi = scale_by(s2, yi);
+                    yi = scale_by(s3, yi);
                 }
                 yi = fma(sc_ys, h, fma(-sc_yc, vi, yi));
                 vi = fma(sc_c, h, sc_s * vi);
@@ -1382,7 +1382,7 @@ __device__ __noinline__ void part1_full(const DevProblem &P, int J, int I, int k
         ytilde = -s0 * x0;
     }
     const double hnrm = P.hn[I + (size_t)J * T];
-    const double alpha = protect_update(fmax(hnrm, fabs(mu)), fabs(ytilde), Yn, is);
+    const double alpha = protect_update(fmax(hnrm, absd(mu)), absd(ytilde), Yn, is);
     const double a = sc_value(alpha, is);
     unsigned long long mx = 0;
     if (!is_one(a)) {
@@ -1931,10 +1931,10 @@ __device__ __forceinline__ void finalize_body_buf(const DevProblem &P, int bx, d
                 alpha = act ? sc_upscale(smin, P.beta[(size_t)I * Spad + k], is) : 1.0;
             }
             if (i == 0) {
-                tau1 = is_one(alpha) ? buf[0][lane] : alpha * buf[0][lane];
+                tau1 = scale_by(alpha, buf[0][lane]);
                 continue;
             }
-            const double tau2 = is_one(alpha) ? buf[t][lane] : alpha * buf[t][lane];
+            const double tau2 = scale_by(alpha, buf[t][lane]);
             const double c = fb.c[t][lane];
             const double s = fb.s[t][lane];
             const double out = fma(c, tau1, -(s * tau2));
@@ -2036,7 +2036,7 @@ __device__ __forceinline__ void norms_rows(const DevProblem &P, int rb) {
         const int c0 = P.fr[J], c1 = P.fr[J + 1];
         double tsum = 0.0;
         for (int c = c0; c < c1; ++c) {
-            const double a = fabs(row[(size_t)c * P.ldh]);
+            const double a = absd(row[(size_t)c * P.ldh]);
             full += a;
             tsum += a;
         }
