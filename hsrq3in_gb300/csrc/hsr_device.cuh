@@ -92,6 +92,9 @@ __device__ __forceinline__ double sc_upscale(double amin, double a, bool is) {
     return is ? ldexp(1.0, (int)(amin - a)) : amin / a;
 }
 __device__ __forceinline__ double sc_min(double a, double b, bool is) { return is ? (a < b ? a : b) : fmin(a, b); }
+// The upscaling at a tile boundary of the back-transform (once per tile, not
+// per row): out of line so the per-row loop evaluates none of it.
+static __device__ __noinline__ double sc_upscale_rare(double amin, double a, bool is) { return sc_upscale(amin, a, is); }
 static __device__ __noinline__ double sc_min_rare(double a, double b, bool is) { return sc_min(a, b, is); }
 
 // ------------------------------------------------- robust scalar kernels
@@ -181,9 +184,24 @@ __device__ __forceinline__ int solve_1x1(double smin, double t, double lambda, d
 // (correctly rounded), as bit patterns.
 constexpr unsigned long long kRtminBits = 0x2000000000000000ULL;
 constexpr unsigned long long kRtmaxBits = 0x5fd6a09e667f3bcdULL;
-__device__ __forceinline__ void givens(double f, double g, double &c, double &s) {
+// The safe-scaled branch of the rotation (operands near underflow or
+// overflow), out of line: rarely taken.  Returns (c, s before negation).
+struct RotCS {
+    double c, sv;
+};
+static __device__ __noinline__ RotCS givens_scaled(double f, double g) {
     const double safmin = 2.2250738585072014e-308;   // 2^-1022
     const double safmax = 1.0 / safmin;               // 2^1022
+    const double f1 = absd(f), g1 = absd(g);
+    const double u = fmin(safmax, fmax(safmin, fmax(f1, g1)));
+    const double fs = f / u, gs = g / u;
+    const double d = sqrt(fs * fs + gs * gs);
+    RotCS r;
+    r.c = absd(fs) / d;
+    r.sv = gs / copysign(d, f);
+    return r;
+}
+__device__ __forceinline__ void givens(double f, double g, double &c, double &s) {
     const unsigned long long mf = mag(f), mg = mag(g);
     double sv;
     if (is_zero(g)) {
@@ -196,13 +214,9 @@ __device__ __forceinline__ void givens(double f, double g, double &c, double &s)
         const double r = copysign(d, f);
         sv = g / r;
     } else {
-        const double f1 = absd(f), g1 = absd(g);
-        const double u = fmin(safmax, fmax(safmin, fmax(f1, g1)));
-        const double fs = f / u, gs = g / u;
-        const double d = sqrt(fs * fs + gs * gs);
-        c = absd(fs) / d;
-        const double r = copysign(d, f);
-        sv = gs / r;
+        const RotCS r = givens_scaled(f, g);
+        c = r.c;
+        sv = r.sv;
     }
     s = neg(sv);
 }

@@ -1928,7 +1928,7 @@ __device__ __forceinline__ void finalize_body_buf(const DevProblem &P, int bx, d
             const int i = r0 + t;
             if (i == P.fr[I + 1]) {
                 ++I;
-                alpha = act ? sc_upscale(smin, P.beta[(size_t)I * Spad + k], is) : 1.0;
+                alpha = act ? sc_upscale_rare(smin, P.beta[(size_t)I * Spad + k], is) : 1.0;
             }
             if (i == 0) {
                 tau1 = scale_by(alpha, buf[0][lane]);
