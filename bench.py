@@ -413,7 +413,8 @@ def run_plain_small(args, tlsz: int):
     # region); its measured alternatives go into the line.
     cands = (48, 64, 96, 128, 160, 200)
     with torch.cuda.stream(stream):
-        tuned, tune_ms = hsr.autotune_plain(dHt, dwr, dX, candidates=cands, stream=stream)
+        tuned, tune_ms, tuned_sc, sc_ms = hsr.autotune_plain(dHt, dwr, dX, candidates=cands, stream=stream,
+                                                              detail=True)
     torch.cuda.synchronize()
     if tlsz == 0:
         tlsz = tuned
@@ -465,6 +466,8 @@ def run_plain_small(args, tlsz: int):
                         "peak_source": "FP64 DFMA stream measured in this run"},
            "kernel_ms_one_step": {k: round(float(v), 3) for k, v in zip(_lib.KERNEL_CLASSES, kms)},
            "autotune": {"candidates": list(cands), "ms": [round(x, 3) for x in tune_ms], "best": tuned,
+                        "shifts_per_cta": {"candidates": [8, 16, 32], "ms": [round(x, 3) for x in sc_ms],
+                                           "best": tuned_sc},
                         "api": "hsr_autotune_plain"},
            "gpu_launches_per_step": launches / steps, "clocks": clk.summary()}
     # e2e through the drop-in entry point, pinned host buffers, flush between steps

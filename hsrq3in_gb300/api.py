@@ -309,19 +309,25 @@ class BatchPlan:
             pass
 
 
-def autotune_plain(dH, dwr, dvr, candidates=(64, 96, 128, 160, 200), stream=None):
+def autotune_plain(dH, dwr, dvr, candidates=(64, 96, 128, 160, 200), stream=None, detail=False):
     """Time the plain device path on this problem for each candidate tile
-    size (dwr restored, dvr overwritten); records the fastest for this order
-    (used when tlsz=0 is passed) and returns (best, [ms per candidate])."""
+    size, then 8/16/32 shifts per diagonal CTA at the fastest (dwr restored,
+    dvr overwritten); records both (used when tlsz=0 is passed) and returns
+    (best tlsz, [ms per candidate]), plus (shifts per CTA, [ms for 8, 16,
+    32]) when detail is set."""
     lib = _lib.load()
     n = dH.shape[0]
     cand = (C.c_int * len(candidates))(*candidates)
     ms = (C.c_double * len(candidates))()
+    sc = C.c_int()
+    scms = (C.c_double * 3)()
     best = lib.hsr_autotune_plain(n, dH.data_ptr(), dH.stride(0), dwr.numel(), dwr.data_ptr(), dvr.data_ptr(),
-                                  dvr.stride(0), cand, len(candidates), ms,
+                                  dvr.stride(0), cand, len(candidates), ms, C.byref(sc), scms,
                                   None if stream is None else C.c_void_p(stream.cuda_stream))
     if best < 0:
         raise HsrError(best)
+    if detail:
+        return best, list(ms), sc.value, list(scms)
     return best, list(ms)
 
 

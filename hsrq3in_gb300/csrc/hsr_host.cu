@@ -1272,12 +1272,14 @@ int hsr_selftest_bounded_wait(void *stream) {
 }
 
 int hsr_autotune_plain(int n, const double *dH, int lddH, int nrhs, double *dwr, double *dvr, int lddvr,
-                       const int *cand, int ncand, double *ms_out, void *stream) {
+                       const int *cand, int ncand, double *ms_out, int *shifts_per_cta, double *spc_ms,
+                       void *stream) {
     if (n <= 0 || nrhs <= 0 || !cand || ncand <= 0 || !dH || !dwr || !dvr) return g_last_status = HSR_ERR_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     double *wr0 = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     auto done = [&](int rc) {
+        set_diag_shifts_trial(0);
         if (wr0) cudaFree(wr0);
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
@@ -1287,45 +1289,64 @@ int hsr_autotune_plain(int n, const double *dH, int lddH, int nrhs, double *dwr,
         cudaEventCreate(&e1) != cudaSuccess ||
         cudaMemcpyAsync(wr0, dwr, (size_t)nrhs * 8, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
         return done(HSR_ERR_CUDA);
+    // Mean of two timed solves after one warm-up; 1e300 when the solve fails.
+    auto time_one = [&](int tl, double *ms) -> int {
+        double tot = 0.0;
+        for (int rep = 0; rep < 3; ++rep) {
+            if (cudaMemcpyAsync(dwr, wr0, (size_t)nrhs * 8, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+                cudaEventRecord(e0, st) != cudaSuccess)
+                return HSR_ERR_CUDA;
+            const int rc = hsr_inverse_iteration_device(n, dH, lddH, nrhs, dwr, tl, dvr, lddvr, nullptr, stream,
+                                                        nullptr, nullptr);
+            if (rc < 0) {
+                *ms = 1e300;
+                return HSR_OK;
+            }
+            float t = 0.f;
+            if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                cudaEventElapsedTime(&t, e0, e1) != cudaSuccess)
+                return HSR_ERR_CUDA;
+            if (rep > 0) tot += t;      // the first run warms the workspace
+        }
+        *ms = tot / 2;
+        return HSR_OK;
+    };
     int best = 0;
     double best_ms = 1e300;
     for (int c = 0; c < ncand; ++c) {
         double ms = 1e300;
-        if (cand[c] > 0 && cand[c] % 4 == 0) {
-            double tot = 0.0;
-            bool ok = true;
-            for (int rep = 0; rep < 3 && ok; ++rep) {
-                if (cudaMemcpyAsync(dwr, wr0, (size_t)nrhs * 8, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
-                    cudaEventRecord(e0, st) != cudaSuccess)
-                    return done(HSR_ERR_CUDA);
-                const int rc = hsr_inverse_iteration_device(n, dH, lddH, nrhs, dwr, cand[c], dvr, lddvr, nullptr,
-                                                            stream, nullptr, nullptr);
-                if (rc < 0) {
-                    ok = false;
-                    break;
-                }
-                float t = 0.f;
-                if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
-                    cudaEventElapsedTime(&t, e0, e1) != cudaSuccess)
-                    return done(HSR_ERR_CUDA);
-                if (rep > 0) tot += t;      // the first run warms the workspace
-            }
-            if (ok) ms = tot / 2;
-        }
+        if (cand[c] > 0 && cand[c] % 4 == 0 && time_one(cand[c], &ms) != HSR_OK) return done(HSR_ERR_CUDA);
         if (ms_out) ms_out[c] = ms;
         if (ms < best_ms) {
             best_ms = ms;
             best = cand[c];
         }
     }
+    if (best <= 0) return done(HSR_ERR_ARG);
+    // Shifts per diagonal CTA (8, 16, 32) at the chosen tile size.
+    int best_sc = 0;
+    double best_sc_ms = 1e300;
+    const int scs[3] = {8, 16, 32};
+    for (int i = 0; i < 3; ++i) {
+        set_diag_shifts_trial(scs[i]);
+        double ms = 1e300;
+        if (time_one(best, &ms) != HSR_OK) return done(HSR_ERR_CUDA);
+        if (spc_ms) spc_ms[i] = ms;
+        if (ms < best_sc_ms) {
+            best_sc_ms = ms;
+            best_sc = scs[i];
+        }
+    }
+    set_diag_shifts_trial(0);
     if (cudaMemcpyAsync(dwr, wr0, (size_t)nrhs * 8, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
         return done(HSR_ERR_CUDA);
-    if (best <= 0) return done(HSR_ERR_ARG);
     {
         std::lock_guard<std::mutex> g(g_plain_tune_mu);
         g_plain_tune[n] = best;
     }
+    if (best_sc) record_diag_shifts(nrhs, best_sc);
+    if (shifts_per_cta) *shifts_per_cta = best_sc;
     done(HSR_OK);
     return best;
 }

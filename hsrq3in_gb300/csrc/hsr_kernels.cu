@@ -25,7 +25,9 @@
 #include "hsr_kernels.h"
 
 #include <cfloat>
+#include <cmath>
 #include <cstdlib>
+#include <map>
 #include <mutex>
 
 namespace hsr {
@@ -1268,10 +1270,39 @@ cudaError_t launch_diag_narrow(const DevProblem &P, int J, int b, cudaStream_t s
 // cover the GPU; fewer when they would leave most SMs idle -- 16 below half
 // the SMs, 8 below a quarter.  HSR_DIAG_SHIFTS_PER_CTA (8, 16 or 32)
 // overrides the choice for tuning; every choice gives the same result.
+// Shifts per CTA recorded by the plain-path autotuner, by shift count, and a
+// per-thread trial value the autotuner sets while it times the candidates.
+namespace {
+std::mutex g_spc_mu;
+std::map<int, int> g_spc_tuned;
+thread_local int t_spc_trial = 0;
+}  // namespace
+
+void set_diag_shifts_trial(int sc) { t_spc_trial = sc; }
+void record_diag_shifts(int S, int sc) {
+    std::lock_guard<std::mutex> g(g_spc_mu);
+    g_spc_tuned[S] = sc;
+}
+
 int diag_shifts_per_cta(int S) {
     const char *env = getenv("HSR_DIAG_SHIFTS_PER_CTA");   // read per launch: tests switch it
     const int forced = env ? atoi(env) : 0;
     if (forced == 8 || forced == 16 || forced == 32) return forced;
+    if (t_spc_trial) return t_spc_trial;
+    {
+        // The tuned entry of the nearest shift count within a factor of two.
+        std::lock_guard<std::mutex> g(g_spc_mu);
+        int best = 0;
+        double bd = 1e300;
+        for (auto &kv : g_spc_tuned) {
+            const double d = std::fabs(std::log((double)kv.first / S));
+            if (d < bd) {
+                bd = d;
+                best = kv.second;
+            }
+        }
+        if (best && bd <= std::log(2.0)) return best;
+    }
     static const int sms = []() {
         int dev = 0, n = 0;
         if (cudaGetDevice(&dev) != cudaSuccess ||

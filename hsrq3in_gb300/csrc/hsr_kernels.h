@@ -70,8 +70,13 @@ cudaError_t launch_norms(const DevProblem &P, unsigned long long *Hn_bits,
 cudaError_t launch_init(const DevProblem &P, int mode, const double *eps3_dev,
                         int its, cudaStream_t st);
 cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st);
-// Shifts per CTA the diagonal kernel uses for S shifts: 8, 16 or 32.
+// Shifts per CTA the diagonal kernel uses for S shifts: 8, 16 or 32 -- the
+// HSR_DIAG_SHIFTS_PER_CTA override, else this thread's autotuning trial, else
+// the tuned entry of the nearest shift count (record_diag_shifts), else a rule
+// by how many SMs the 32-shift CTAs would fill.
 int diag_shifts_per_cta(int S);
+void set_diag_shifts_trial(int sc);      // 0 ends the trial
+void record_diag_shifts(int S, int sc);
 size_t diag_smem_bytes(int b);
 // CTAs per SM of the diagonal kernels with v/y in shared memory (0: v/y do
 // not fit).  More CTAs than one resident wave -> v/y go to global scratch.

@@ -249,17 +249,22 @@ int hsr_batch_plan_set_engine(hsr_batch_plan *plan, int engine, void *stream);
 int hsr_batch_plan_queue_info(const hsr_batch_plan *plan, int *engine, long *items, int *grid,
                               int *diag_warps, int *in_graph);
 
-/* Plain-path tile size: times hsr_inverse_iteration_device on the caller's
+/* Plain-path autotuner: times hsr_inverse_iteration_device on the caller's
  * problem (device pointers; dwr is restored, dvr overwritten) for each
- * candidate tlsz in `cand`, records the fastest for order n and returns it;
- * ms_out[i] (optional) gets candidate i's time.  A tlsz of 0 passed to
- * tiled_inverse_iteration, hsr_inverse_iteration_ex or
- * hsr_inverse_iteration_device then selects the recorded size of the
- * nearest tuned order within a factor of two (hsr_autotune_plain_tlsz), else
- * a default by order.  The reference takes tlsz from its caller only
- * (main.c:40-44); no reference counterpart. */
+ * candidate tlsz in `cand` (ms_out[i], optional, gets candidate i's time),
+ * then, at the fastest tlsz, for 8, 16 and 32 shifts per diagonal CTA
+ * (spc_ms[0..2], optional).  It records the fastest tlsz for order n and the
+ * fastest shifts per CTA for nrhs shifts (*shifts_per_cta, optional), and
+ * returns the tlsz.  A tlsz of 0 passed to tiled_inverse_iteration,
+ * hsr_inverse_iteration_ex or hsr_inverse_iteration_device then selects the
+ * recorded size of the nearest tuned order within a factor of two
+ * (hsr_autotune_plain_tlsz), else a default by order; the diagonal kernel
+ * likewise uses the recorded shifts per CTA of the nearest tuned shift count.
+ * The reference takes tlsz from its caller only (main.c:40-44); no reference
+ * counterpart. */
 int hsr_autotune_plain(int n, const double *dH, int lddH, int nrhs, double *dwr, double *dvr, int lddvr,
-                       const int *cand, int ncand, double *ms_out, void *stream);
+                       const int *cand, int ncand, double *ms_out, int *shifts_per_cta, double *spc_ms,
+                       void *stream);
 int hsr_autotune_plain_tlsz(int n);
 
 /* Tile size for batches whose orders lie in [n_lo, n_hi]: the size that

@@ -315,8 +315,9 @@ def test_plain_autotune_and_tlsz_zero(gpu_lib):
     dH[:, :n] = torch.from_numpy(np.ascontiguousarray(H.T)).to(dev)
     dwr = torch.from_numpy(wr.copy()).to(dev)
     dX = torch.empty((n, ld), dtype=torch.float64, device=dev)
-    best, ms = hsr.autotune_plain(dH, dwr, dX, candidates=(32, 64, 96))
+    best, ms, sc, sc_ms = hsr.autotune_plain(dH, dwr, dX, candidates=(32, 64, 96), detail=True)
     assert best in (32, 64, 96) and all(0 < t < 1e299 for t in ms)
+    assert sc in (8, 16, 32) and all(0 < t < 1e299 for t in sc_ms)
     assert np.array_equal(dwr.cpu().numpy(), wr)                 # restored
     assert _lib.load().hsr_autotune_plain_tlsz(n) == best
     a = hsr.inverse_iteration(H, wr, 0, 16)
