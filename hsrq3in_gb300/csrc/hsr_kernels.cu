@@ -169,7 +169,11 @@ cudaError_t launch_init(const DevProblem &P, int mode, const double *eps3_dev, i
 constexpr int kDiagWarps = 4;     // single-problem path, v/y in global scratch
 constexpr int kDiagWarpsSmem = 8; // single-problem path, v/y in shared memory
 constexpr int kDiagWarpsB = 1;    // batched path
-constexpr int kDiagWarpsNarrow = 4;  // single-problem path, 8 or 16 shifts per CTA
+// Single-problem path, 8 or 16 shifts per CTA: three warps (the chain and
+// two row warps) need 3 x 32 x 120 registers, which fit beside the two
+// 256-thread CTAs of the concurrent GEMM on one SM (a fourth warp would not,
+// and the diagonal CTA would wait for a GEMM CTA to finish).
+constexpr int kDiagWarpsNarrow = 3;
 
 constexpr int kDiagBcast = 8;      // per-lane step results broadcast by warp 0
 // Staging buffers for columns of H: the pipelined multi-warp body keeps three
@@ -861,11 +865,11 @@ __host__ __device__ constexpr size_t diag_narrow_smem_bytes(int b, int nw) {
 template <int SC, int NW>
 __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int bx) {
     static_assert(32 % SC == 0 && SC >= 4 && SC < 32, "shifts per CTA");
-    static_assert(NW % 4 == 0, "whole sub-partitions");
+    static_assert(NW >= 2, "a chain warp and at least one row warp");
     constexpr int RL = 32 / SC;                                               // rows per row-warp instruction
     // Warps w = 0, 4, ... share sub-partition 0, whose FP64 unit the scalar
     // chain (warp 0) needs to itself: rows go to the other warps only.
-    constexpr int NR = NW - NW / 4;                                           // row warps
+    constexpr int NR = NW - (NW + 3) / 4;                                     // row warps
     extern __shared__ double sm[];
     const int tid = threadIdx.x;
     const int lane = tid & 31;
