@@ -61,6 +61,12 @@ struct Timing {
         if (!enabled) return;
         cudaEventRecord(next(), st);
     }
+    // Forget the last begin/end pair (a launch that did not happen).
+    void drop_last() {
+        if (!enabled || cls.empty()) return;
+        cls.pop_back();
+        used -= 2;
+    }
     void resolve() {
         if (!enabled) return;
         for (size_t i = 0; i < cls.size(); ++i) {
@@ -325,13 +331,25 @@ int run_pass(Solver &s, int mode, int its, int off, int cnt) {
             HSR_LAUNCH_C(kcPart1, M, launch_part1(P, J, M));
             HSR_CK(cudaEventRecord(w.ev_top, M));
             HSR_CK(cudaStreamWaitEvent(D, w.ev_top, 0));
-            if (gemm_prefers_narrow(s.fr[J] - s.fr[J - 1], cc))
+            cudaError_t fe = cudaSuccess;
+            ++g_launches;
+            g_timing.begin(kcDiag, D);
+            const bool fused = launch_diag_fused(Pn, P, J - 1, s.fr[J] - s.fr[J - 1], D, &fe);
+            g_timing.end(D);
+            if (!fused) {
+                --g_launches;
+                g_timing.drop_last();
+            }
+            HSR_CK(fe);
+            if (fused) {
+                // Few shifts: the top GEMM ran inside the diagonal CTAs.
+            } else if (gemm_prefers_narrow(s.fr[J] - s.fr[J - 1], cc))
                 HSR_LAUNCH_C(kcGemmTop, D, launch_gemm_narrow(P, J, s.fr[J - 1], s.fr[J], s.tmH, s.tmWn[J & 1],
                                                               s.tmZn[J & 1], D));
             else
                 HSR_LAUNCH_C(kcGemmTop, D,
                              launch_gemm(P, J, s.fr[J - 1], s.fr[J], s.tmH, s.tmW[J & 1], s.tmZ[J & 1], D));
-            HSR_LAUNCH_C(kcDiag, D, launch_diag(Pn, J - 1, s.fr[J] - s.fr[J - 1], gs, D));
+            if (!fused) HSR_LAUNCH_C(kcDiag, D, launch_diag(Pn, J - 1, s.fr[J] - s.fr[J - 1], gs, D));
             HSR_CK(cudaEventRecord(w.ev_diag, D));
             if (s.fr[J - 1] > 0)
                 HSR_LAUNCH_C(kcGemm, M, launch_gemm(P, J, 0, s.fr[J - 1], s.tmH, s.tmW[J & 1], s.tmZ[J & 1], M));

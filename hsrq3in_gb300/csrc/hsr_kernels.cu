@@ -847,6 +847,46 @@ __device__ __forceinline__ void diag_body_pipe(const DevProblem &P, int J, int b
 }
 
 
+// One element (row, col) of the real GEMM epilogue of the stage whose
+// diagonal tile starts at row l (height b): the crossover column advanced by
+// pi and the accumulated H W (aw), Part 1 applied where flagged, the tile
+// update with the accumulated H Zs (az) or, for protected columns, with the
+// rescaled Ytilde2 (update-task.c:233-243), in place in R and X.  I is the
+// row's tile and hl1 = H(row, l-1).  Returns |y| as bits for the tile's norm
+// bound.
+__device__ __forceinline__ unsigned long long gemm_epilogue_elem(const DevProblem &P, int l, int b, int row, int I,
+                                                                 int col, double hl1, double aw, double az) {
+    const size_t Spad = (size_t)P.Spad;
+    const double pik = P.pi[col], w0 = P.W[col], zl = P.zlast[col], mu = P.wr[col], yt = P.ytil[col];
+    const size_t ir = row + (size_t)col * P.ldr;
+    const size_t ix = row + (size_t)col * P.ldx;
+    const double rold = P.R[ir];
+    double rnew = fma(pik, rold, aw);
+    if (row == l - 1) rnew = fma(-mu, w0, rnew);
+    P.R[ir] = rnew;
+    double yv = P.X[ix];
+    const unsigned char fl = P.slow[(size_t)I * Spad + col];
+    if (fl & 2) {
+        // Part 1 (update-task.c:134-139): y -= (H(i, l-1) - mu [i == l-1]) ytilde.
+        yv = fma(-hl1, yt, yv);
+        if (row == l - 1) yv = fma(mu, yt, yv);
+    }
+    if (fl & 1) {
+        // Protected path: rescaled Ytilde2 of this (tile, shift).
+        const double *zs = P.Zslow + (size_t)I * P.tlsz * Spad + col;
+        const double *hr = P.H + row + (size_t)l * P.ldh;
+        double acc = 0.0;
+        for (int q = 0; q < b - 1; ++q) acc = fma(hr[(size_t)q * P.ldh], zs[(size_t)q * Spad], acc);
+        yv = yv - acc;
+        yv = fma(-rold, zs[(size_t)(b - 1) * Spad], yv);
+    } else {
+        yv = yv - az;
+        yv = fma(-rold, zl, yv);
+    }
+    P.X[ix] = yv;
+    return abs_bits(yv);
+}
+
 // Narrow form of the pipelined body for solves with few shifts: SC (< 32)
 // shifts per CTA, so that a small shift count still spreads over many SMs.
 // The scalar chain of each step runs on warp 0, lane s (and its duplicates
@@ -1225,6 +1265,67 @@ __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int
 #undef BC
 }
 
+// The GEMM of stage J+1 over the rows of tile J, for the CTA's own columns
+// k0 .. k0+SC-1 (Pg: the descriptor with stage J+1's operands).  Each
+// thread takes (row, column) elements -- the lanes of a warp cover 32/SC rows
+// x SC columns, so they share the loads of H -- and sums k = 0 .. b-1 in
+// order with fma, as gemm_body does, then applies the same epilogue
+// (gemm_epilogue_elem).  The result is bit-identical to the top GEMM launch
+// it replaces, and the tile's rows are ready in this CTA without waiting for
+// another kernel.
+template <int SC, int NW>
+__device__ __forceinline__ void top_rows_fused(const DevProblem &Pg, int J, int k0) {
+    const int Js = J + 1;                                   // the stage whose GEMM this is
+    const int l = Pg.fr[Js], b = Pg.fr[Js + 1] - l;
+    const int r_lo = Pg.fr[J], rows = l - r_lo;
+    const size_t Spad = (size_t)Pg.Spad;
+    unsigned long long *ynb = reinterpret_cast<unsigned long long *>(Pg.ynorm);
+    for (int e = threadIdx.x; e < rows * SC; e += 32 * NW) {
+        const int rr = e / SC, col = k0 + (e - rr * SC);
+        if (col >= Pg.S) continue;
+        const int row = r_lo + rr;
+        const double *hrow = Pg.H + row + (size_t)(l - 1) * Pg.ldh;
+        double aw = 0.0, az = 0.0;
+        int k = 0;
+        for (; k + 3 < b; k += 4) {
+            double a[4], w[4], z[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                a[q] = hrow[(size_t)(k + q) * Pg.ldh];
+                w[q] = Pg.W[(size_t)(k + q) * Spad + col];
+                z[q] = Pg.Zs[(size_t)(k + q) * Spad + col];
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                aw = fma(a[q], w[q], aw);
+                az = fma(a[q], z[q], az);
+            }
+        }
+        for (; k < b; ++k) {
+            const double a = hrow[(size_t)k * Pg.ldh];
+            aw = fma(a, Pg.W[(size_t)k * Spad + col], aw);
+            az = fma(a, Pg.Zs[(size_t)k * Spad + col], az);
+        }
+        const double hl1 = Pg.H[row + (size_t)(l - 1) * Pg.ldh];
+        const unsigned long long m = gemm_epilogue_elem(Pg, l, b, row, J, col, hl1, aw, az);
+        atomicMax(&ynb[(size_t)J * Spad + col], m);
+    }
+}
+
+// Fused form: the GEMM of stage J+1 over this tile's rows (top_rows_fused),
+// then the diagonal solve of tile J, in one CTA.
+template <int SC, int NW>
+__global__ void __launch_bounds__(32 * NW) k_diag_nf(DevProblem P, DevProblem Pg, int J) {
+    const int b = P.fr[J + 1] - P.fr[J];
+    if (diag_narrow_smem_bytes<SC>(b, NW) > dynamic_smem_bytes()) {
+        if (threadIdx.x == 0) atomicOr(P.err, kErrShape);
+        return;
+    }
+    top_rows_fused<SC, NW>(Pg, J, blockIdx.x * SC);
+    __syncthreads();                     // this CTA's rows of tile J are final
+    diag_body_narrow<SC, NW>(P, J, blockIdx.x);
+}
+
 template <int SC, int NW>
 __global__ void __launch_bounds__(32 * NW) k_diag_n(DevProblem P, int J) {
     const int b = P.fr[J + 1] - P.fr[J];
@@ -1270,10 +1371,30 @@ cudaError_t launch_diag_narrow(const DevProblem &P, int J, int b, cudaStream_t s
     return cudaGetLastError();
 }
 
-// Shifts per diagonal CTA: 32 (a lane per shift) while the 32-shift CTAs
-// cover the GPU; fewer when they would leave most SMs idle -- 16 below half
-// the SMs, 8 below a quarter.  HSR_DIAG_SHIFTS_PER_CTA (8, 16 or 32)
-// overrides the choice for tuning; every choice gives the same result.
+template <int SC, int NW>
+cudaError_t launch_diag_narrow_fused(const DevProblem &P, const DevProblem &Pg, int J, int b, cudaStream_t st) {
+    static size_t configured = 0;
+    const size_t smem = diag_narrow_smem_bytes<SC>(b, NW);
+    const cudaError_t e = raise_smem_limit((const void *)k_diag_nf<SC, NW>, &configured, smem);
+    if (e != cudaSuccess) return e;
+    k_diag_nf<SC, NW><<<(P.S + SC - 1) / SC, 32 * NW, smem, st>>>(P, Pg, J);
+    return cudaGetLastError();
+}
+
+// Tile J's diagonal solve preceded by stage J+1's GEMM over tile J's rows,
+// in one launch, when the narrow forms apply; false (nothing launched) when
+// the wide form is used and the caller runs the two launches.
+bool launch_diag_fused(const DevProblem &P, const DevProblem &Pg, int J, int b, cudaStream_t st,
+                       cudaError_t *err) {
+    const char *env = getenv("HSR_FUSED_TOP");          // 0: separate launches, for comparison
+    if (env && env[0] == '0') return false;
+    switch (diag_shifts_per_cta(P.S)) {
+    case 8: *err = launch_diag_narrow_fused<8, kDiagWarpsNarrow>(P, Pg, J, b, st); return true;
+    case 16: *err = launch_diag_narrow_fused<16, kDiagWarpsNarrow>(P, Pg, J, b, st); return true;
+    default: return false;
+    }
+}
+
 // Shifts per CTA recorded by the plain-path autotuner, by shift count, and a
 // per-thread trial value the autotuner sets while it times the candidates.
 namespace {
@@ -1288,6 +1409,12 @@ void record_diag_shifts(int S, int sc) {
     g_spc_tuned[S] = sc;
 }
 
+// Shifts per diagonal CTA.  HSR_DIAG_SHIFTS_PER_CTA (8, 16 or 32) first,
+// then the autotuner's trial value, then its recorded choice for the nearest
+// shift count within a factor of two; otherwise 32 (a lane per shift) while
+// the 32-shift CTAs cover the GPU, fewer when they would leave most SMs idle
+// -- 16 below half the SMs, 8 below a quarter.  Every choice gives the same
+// result bit for bit.
 int diag_shifts_per_cta(int S) {
     const char *env = getenv("HSR_DIAG_SHIFTS_PER_CTA");   // read per launch: tests switch it
     const int forced = env ? atoi(env) : 0;
@@ -1790,37 +1917,8 @@ __device__ __forceinline__ void gemm_body(const DevProblem &P, int J, int row_lo
         const int cc = cg * (BN / 4) + j;
         const int col = col0 + cc;
         if (col >= P.S) break;
-        const double pik = P.pi[col], w0 = P.W[col], zl = P.zlast[col], mu = P.wr[col], yt = P.ytil[col];
-        unsigned long long m = 0;
-        if (rowok) {
-            const size_t ir = row + (size_t)col * P.ldr;
-            const size_t ix = row + (size_t)col * P.ldx;
-            const double rold = P.R[ir];
-            double rnew = fma(pik, rold, eaw[cc * kEpiLd + er]);
-            if (row == l - 1) rnew = fma(-mu, w0, rnew);
-            P.R[ir] = rnew;
-            double yv = P.X[ix];
-            const unsigned char fl = P.slow[(size_t)I * Spad + col];
-            if (fl & 2) {
-                // Part 1 (update-task.c:134-139): y -= (H(i, l-1) - mu [i == l-1]) ytilde.
-                yv = fma(-hl1, yt, yv);
-                if (row == l - 1) yv = fma(mu, yt, yv);
-            }
-            if (fl & 1) {
-                // Protected path: rescaled Ytilde2 of this (tile, shift).
-                const double *zs = P.Zslow + (size_t)I * P.tlsz * Spad + col;
-                const double *hr = P.H + row + (size_t)l * P.ldh;
-                double acc = 0.0;
-                for (int q = 0; q < b - 1; ++q) acc = fma(hr[(size_t)q * P.ldh], zs[(size_t)q * Spad], acc);
-                yv = yv - acc;
-                yv = fma(-rold, zs[(size_t)(b - 1) * Spad], yv);
-            } else {
-                yv = yv - eaz[cc * kEpiLd + er];
-                yv = fma(-rold, zl, yv);
-            }
-            P.X[ix] = yv;
-            m = abs_bits(yv);
-        }
+        unsigned long long m =
+            rowok ? gemm_epilogue_elem(P, l, b, row, I, col, hl1, eaw[cc * kEpiLd + er], eaz[cc * kEpiLd + er]) : 0;
         // Segmented max over runs of lanes in the same tile (inclusive scan);
         // the last lane of each run holds its maximum.
 #pragma unroll

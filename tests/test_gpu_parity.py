@@ -279,16 +279,19 @@ def hsr_cplx(H, mu, tlsz):
     return hsr.inverse_iteration_cplx(H, mu, tlsz, 16)
 
 
+@pytest.mark.parametrize("fused", ["1", "0"])
 @pytest.mark.parametrize("sc", ["8", "16", "32"])
 @pytest.mark.parametrize("n,tlsz,nrhs,seed", [
     (300, 64, 300, 31),      # several tiles, all shifts
     (203, 40, 77, 32),       # ragged first tile, ragged shift count
     (520, 160, 1000, 33),    # the benchmark tile size, more shifts than rows (repeated)
 ])
-def test_diag_forms_bitwise(gpu_lib, monkeypatch, sc, n, tlsz, nrhs, seed):
+def test_diag_forms_bitwise(gpu_lib, monkeypatch, sc, n, tlsz, nrhs, seed, fused):
     """The diagonal kernel's three forms -- 8, 16 or 32 shifts per CTA, chosen
-    by shift count -- give the oracle's result bit for bit."""
+    by shift count -- with the top GEMM fused into the narrow forms or run as
+    its own launch, give the oracle's result bit for bit."""
     monkeypatch.setenv("HSR_DIAG_SHIFTS_PER_CTA", sc)
+    monkeypatch.setenv("HSR_FUSED_TOP", fused)
     H, lam = G.real_spectrum(n, seed)
     wr = G.perturbed_shifts(np.resize(lam, nrhs), seed + 1)
     dev = _device(H, wr, tlsz)
