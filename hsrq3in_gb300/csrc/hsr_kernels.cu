@@ -44,6 +44,24 @@ cudaError_t raise_smem_limit(const void *func, size_t *configured, size_t smem) 
     return e;
 }
 
+// Ask for the largest shared-memory carveout for a kernel of the plain
+// path's look-ahead.  The GEMM of the rows above (two 74 KB CTAs per SM) and
+// the diagonal kernel of the next tile run at the same time; an SM set up
+// with a small carveout for whichever CTA arrived first could not take the
+// other kernel's CTAs beside it.  HSR_CARVEOUT=0 leaves the default.
+cudaError_t prefer_max_shared(const void *func, bool *done) {
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    if (*done) return cudaSuccess;
+    const char *env = getenv("HSR_CARVEOUT");
+    const cudaError_t e = (env && env[0] == '0')
+                              ? cudaSuccess
+                              : cudaFuncSetAttribute(func, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                     (int)cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess) *done = true;
+    return e;
+}
+
 // --------------------------------------------------------------- norms
 // Row sums of |H| accumulated column by column in order, as LAPACK dlange
 // 'I' does (utils.c:155-174): per (row, tile J >= tile(row)) for the tile
@@ -1266,16 +1284,117 @@ __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int
 }
 
 // The GEMM of stage J+1 over the rows of tile J, for the CTA's own columns
-// k0 .. k0+SC-1 (Pg: the descriptor with stage J+1's operands).  Each
-// thread takes (row, column) elements -- the lanes of a warp cover 32/SC rows
-// x SC columns, so they share the loads of H -- and sums k = 0 .. b-1 in
-// order with fma, as gemm_body does, then applies the same epilogue
-// (gemm_epilogue_elem).  The result is bit-identical to the top GEMM launch
-// it replaces, and the tile's rows are ready in this CTA without waiting for
-// another kernel.
+// k0 .. k0+SC-1 (Pg: the descriptor with stage J+1's operands).  Every
+// (row, column) element sums k = 0 .. b-1 in order with fma, as gemm_body
+// does, then goes through the same epilogue (gemm_epilogue_elem), so the
+// result is bit-identical to the top GEMM launch it replaces and the tile's
+// rows are ready in this CTA without waiting for another kernel.
+//
+// Staged form: the H block (rows x b) and the CTA's columns of W and Zs move
+// through shared memory in chunks of kTopChunk k-columns, double-buffered
+// with cp.async (every request of a chunk in flight at once), so the FP64
+// sums read shared memory instead of paying a global-load latency every few
+// fmas.  Thread t takes column t % SC and rows g, g + G, ..., g + (EB-1) G
+// (g = t / SC, G = threads / SC), its sums in registers across the chunks;
+// a pass covers G * EB rows (72 with 8 shifts per CTA), a taller tile takes
+// more passes.  The two buffers, (rows + 2 SC) x kTopChunk doubles each, are
+// 10 KB at tlsz 64 -- no more than the diagonal solve's own shared memory,
+// which reuses them afterwards, so the CTA still fits beside two GEMM CTAs
+// on one SM.  Taller tiles use the global form.
+constexpr int kTopChunk = 8, kTopRowsPerThread = 6;
+constexpr size_t kTopStagedMaxBytes = 16 * 1024;
+template <int SC>
+__host__ __device__ constexpr size_t top_staged_bytes(int rows) {
+    return 2 * ((size_t)rows + 2 * SC) * kTopChunk * sizeof(double);
+}
+
 template <int SC, int NW>
-__device__ __forceinline__ void top_rows_fused(const DevProblem &Pg, int J, int k0) {
+__device__ __forceinline__ void top_rows_staged(const DevProblem &Pg, int J, int k0, double *sm) {
+    constexpr int NT = 32 * NW, G = NT / SC, EB = kTopRowsPerThread;
     const int Js = J + 1;                                   // the stage whose GEMM this is
+    const int l = Pg.fr[Js], b = Pg.fr[Js + 1] - l;
+    const int r_lo = Pg.fr[J], rows = l - r_lo;
+    const size_t Spad = (size_t)Pg.Spad;
+    const size_t bufd = ((size_t)rows + 2 * SC) * kTopChunk;  // doubles per buffer
+    // Buffer layout: hs[kk][rows] = H(r_lo + r, l - 1 + k), then ws[kk][SC], zs[kk][SC].
+    auto stage = [&](int ch) {
+        double *hs = sm + (size_t)(ch & 1) * bufd;
+        double *ws = hs + (size_t)kTopChunk * rows;
+        double *zs = ws + kTopChunk * SC;
+        const int kb = ch * kTopChunk, kn = min(kTopChunk, b - kb);
+        for (int idx = threadIdx.x; idx < kn * rows; idx += NT) {
+            const int kk = idx / rows, r = idx - kk * rows;
+            cp_async8(hs + idx, Pg.H + (r_lo + r) + (size_t)(l - 1 + kb + kk) * Pg.ldh);
+        }
+        for (int idx = threadIdx.x; idx < kn * SC; idx += NT) {
+            const int kk = idx / SC, c = idx - kk * SC;
+            const int col = k0 + c;
+            if (col < Pg.S) {
+                cp_async8(ws + idx, Pg.W + (size_t)(kb + kk) * Spad + col);
+                cp_async8(zs + idx, Pg.Zs + (size_t)(kb + kk) * Spad + col);
+            } else {
+                ws[idx] = 0.0;
+                zs[idx] = 0.0;
+            }
+        }
+        cp_async_commit();
+    };
+
+    const int c = threadIdx.x % SC, g = threadIdx.x / SC;
+    const int col = k0 + c;
+    const int nch = (b + kTopChunk - 1) / kTopChunk;
+    unsigned long long m = 0;
+    for (int p0 = 0; p0 < rows; p0 += G * EB) {
+        int ri[EB];
+#pragma unroll
+        for (int e = 0; e < EB; ++e) ri[e] = min(p0 + g + e * G, rows - 1);   // rows past the tile: computed, dropped
+        double aw[EB], az[EB], hl1[EB];
+#pragma unroll
+        for (int e = 0; e < EB; ++e) aw[e] = az[e] = hl1[e] = 0.0;
+        stage(0);
+        for (int ch = 0; ch < nch; ++ch) {
+            if (ch + 1 < nch) {
+                stage(ch + 1);
+                cp_async_wait_one();
+            } else {
+                cp_async_wait_all();
+            }
+            __syncthreads();                                    // chunk ch in shared memory
+            const double *hs = sm + (size_t)(ch & 1) * bufd;
+            const double *ws = hs + (size_t)kTopChunk * rows;
+            const double *zs = ws + kTopChunk * SC;
+            if (ch == 0) {
+#pragma unroll
+                for (int e = 0; e < EB; ++e) hl1[e] = hs[ri[e]];  // H(row, l-1), the epilogue's operand
+            }
+            const int kn = min(kTopChunk, b - ch * kTopChunk);
+            for (int kk = 0; kk < kn; ++kk) {
+                const double w = ws[kk * SC + c], z = zs[kk * SC + c];
+                const double *hk = hs + (size_t)kk * rows;
+#pragma unroll
+                for (int e = 0; e < EB; ++e) {
+                    const double a = hk[ri[e]];
+                    aw[e] = fma(a, w, aw[e]);
+                    az[e] = fma(a, z, az[e]);
+                }
+            }
+            __syncthreads();                                    // buffer ch & 1 free for chunk ch + 2
+        }
+        if (col < Pg.S) {
+#pragma unroll
+            for (int e = 0; e < EB; ++e)
+                if (p0 + g + e * G < rows)
+                    m = umax64(m, gemm_epilogue_elem(Pg, l, b, r_lo + ri[e], J, col, hl1[e], aw[e], az[e]));
+        }
+    }
+    if (col < Pg.S && m) atomicMax(reinterpret_cast<unsigned long long *>(Pg.ynorm) + (size_t)J * Spad + col, m);
+}
+
+// Fallback for blocks too large to stage: the same sums with operands read
+// from global memory.
+template <int SC, int NW>
+__device__ __forceinline__ void top_rows_global(const DevProblem &Pg, int J, int k0) {
+    const int Js = J + 1;
     const int l = Pg.fr[Js], b = Pg.fr[Js + 1] - l;
     const int r_lo = Pg.fr[J], rows = l - r_lo;
     const size_t Spad = (size_t)Pg.Spad;
@@ -1312,17 +1431,23 @@ __device__ __forceinline__ void top_rows_fused(const DevProblem &Pg, int J, int 
     }
 }
 
-// Fused form: the GEMM of stage J+1 over this tile's rows (top_rows_fused),
-// then the diagonal solve of tile J, in one CTA.
+// Fused form: the GEMM of stage J+1 over this tile's rows (staged when the
+// launch gave it the shared memory, else from global memory), then the
+// diagonal solve of tile J, in one CTA.
 template <int SC, int NW>
 __global__ void __launch_bounds__(32 * NW) k_diag_nf(DevProblem P, DevProblem Pg, int J) {
     const int b = P.fr[J + 1] - P.fr[J];
-    if (diag_narrow_smem_bytes<SC>(b, NW) > dynamic_smem_bytes()) {
+    const size_t have = dynamic_smem_bytes();
+    if (diag_narrow_smem_bytes<SC>(b, NW) > have) {
         if (threadIdx.x == 0) atomicOr(P.err, kErrShape);
         return;
     }
-    top_rows_fused<SC, NW>(Pg, J, blockIdx.x * SC);
-    __syncthreads();                     // this CTA's rows of tile J are final
+    extern __shared__ double sm[];
+    if (top_staged_bytes<SC>(b) <= have)
+        top_rows_staged<SC, NW>(Pg, J, blockIdx.x * SC, sm);
+    else
+        top_rows_global<SC, NW>(Pg, J, blockIdx.x * SC);
+    __syncthreads();                     // this CTA's rows of tile J are final; shared memory free
     diag_body_narrow<SC, NW>(P, J, blockIdx.x);
 }
 
@@ -1358,24 +1483,34 @@ __global__ void __launch_bounds__(32 * NW) k_diag(DevProblem P, int J, double *g
 template <int NW>
 cudaError_t diag_smem_attr(size_t smem) {
     static size_t configured = 0;
+    static bool carve = false;
+    const cudaError_t e = prefer_max_shared((const void *)k_diag<NW>, &carve);
+    if (e != cudaSuccess) return e;
     return raise_smem_limit((const void *)k_diag<NW>, &configured, smem);
 }
 
 template <int SC, int NW>
 cudaError_t launch_diag_narrow(const DevProblem &P, int J, int b, cudaStream_t st) {
     static size_t configured = 0;
+    static bool carve = false;
     const size_t smem = diag_narrow_smem_bytes<SC>(b, NW);
-    const cudaError_t e = raise_smem_limit((const void *)k_diag_n<SC, NW>, &configured, smem);
+    cudaError_t e = prefer_max_shared((const void *)k_diag_n<SC, NW>, &carve);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_diag_n<SC, NW>, &configured, smem);
     if (e != cudaSuccess) return e;
     k_diag_n<SC, NW><<<(P.S + SC - 1) / SC, 32 * NW, smem, st>>>(P, J);
     return cudaGetLastError();
 }
 
 template <int SC, int NW>
-cudaError_t launch_diag_narrow_fused(const DevProblem &P, const DevProblem &Pg, int J, int b, cudaStream_t st) {
+cudaError_t launch_diag_narrow_fused(const DevProblem &P, const DevProblem &Pg, int J, int b, int bs,
+                                     cudaStream_t st) {
     static size_t configured = 0;
-    const size_t smem = diag_narrow_smem_bytes<SC>(b, NW);
-    const cudaError_t e = raise_smem_limit((const void *)k_diag_nf<SC, NW>, &configured, smem);
+    size_t smem = diag_narrow_smem_bytes<SC>(b, NW);
+    const size_t top = top_staged_bytes<SC>(b);
+    if (top <= kTopStagedMaxBytes && top > smem) smem = top;
+    static bool carve = false;
+    cudaError_t e = prefer_max_shared((const void *)k_diag_nf<SC, NW>, &carve);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_diag_nf<SC, NW>, &configured, smem);
     if (e != cudaSuccess) return e;
     k_diag_nf<SC, NW><<<(P.S + SC - 1) / SC, 32 * NW, smem, st>>>(P, Pg, J);
     return cudaGetLastError();
@@ -1384,13 +1519,13 @@ cudaError_t launch_diag_narrow_fused(const DevProblem &P, const DevProblem &Pg, 
 // Tile J's diagonal solve preceded by stage J+1's GEMM over tile J's rows,
 // in one launch, when the narrow forms apply; false (nothing launched) when
 // the wide form is used and the caller runs the two launches.
-bool launch_diag_fused(const DevProblem &P, const DevProblem &Pg, int J, int b, cudaStream_t st,
+bool launch_diag_fused(const DevProblem &P, const DevProblem &Pg, int J, int b, int bs, cudaStream_t st,
                        cudaError_t *err) {
     const char *env = getenv("HSR_FUSED_TOP");          // 0: separate launches, for comparison
     if (env && env[0] == '0') return false;
     switch (diag_shifts_per_cta(P.S)) {
-    case 8: *err = launch_diag_narrow_fused<8, kDiagWarpsNarrow>(P, Pg, J, b, st); return true;
-    case 16: *err = launch_diag_narrow_fused<16, kDiagWarpsNarrow>(P, Pg, J, b, st); return true;
+    case 8: *err = launch_diag_narrow_fused<8, kDiagWarpsNarrow>(P, Pg, J, b, bs, st); return true;
+    case 16: *err = launch_diag_narrow_fused<16, kDiagWarpsNarrow>(P, Pg, J, b, bs, st); return true;
     default: return false;
     }
 }
@@ -1950,8 +2085,10 @@ cudaError_t launch_gemm_narrow(const DevProblem &P, int J, int row_lo, int row_h
                                const CUtensorMap &tmW, const CUtensorMap &tmZ, cudaStream_t st) {
     if (row_hi <= row_lo || P.S <= 0) return cudaSuccess;
     static size_t configured = 0;
+    static bool carve = false;
     const size_t smem = gemm_narrow_smem_bytes();
-    const cudaError_t e = raise_smem_limit((const void *)k_gemm_n, &configured, smem);
+    cudaError_t e = prefer_max_shared((const void *)k_gemm_n, &carve);
+    if (e == cudaSuccess) e = raise_smem_limit((const void *)k_gemm_n, &configured, smem);
     if (e != cudaSuccess) return e;
     const int span = row_hi - (row_lo & ~7);
     dim3 g((span + kGemmBM - 1) / kGemmBM, (P.S + kGemmBNNarrow - 1) / kGemmBNNarrow);
@@ -1982,9 +2119,11 @@ k_gemm_c(DevProblem P, int J, int row_lo, int row_hi, const __grid_constant__ CU
 cudaError_t launch_gemm(const DevProblem &P, int J, int row_lo, int row_hi, const CUtensorMap &tmH,
                         const CUtensorMap &tmW, const CUtensorMap &tmZ, cudaStream_t st) {
     static size_t configured = 0;
+    static bool carve = false;
     const size_t smem = gemm_smem_bytes();
     {
-        const cudaError_t e = raise_smem_limit((const void *)k_gemm, &configured, smem);
+        cudaError_t e = prefer_max_shared((const void *)k_gemm, &carve);
+        if (e == cudaSuccess) e = raise_smem_limit((const void *)k_gemm, &configured, smem);
         if (e != cudaSuccess) return e;
     }
     if (row_hi <= row_lo) return cudaSuccess;
@@ -2102,14 +2241,114 @@ __device__ __forceinline__ void finalize_body(const DevProblem &P, int bx, doubl
     finalize_body_buf(P, bx, colnorm, status, scale_out, fb);
 }
 
+// The plain path's form of finalize_body_buf: the next 32-row block's X,
+// rotations and sines are brought in with cp.async while the current block's
+// rows are processed, so the sequential row loop never waits on a load (two
+// FinalizeBuf in dynamic shared memory).  The arithmetic and its order are
+// those of finalize_body_buf.
+__device__ __forceinline__ void finalize_body_db(const DevProblem &P, int bx, double *colnorm, int *status,
+                                                 double *scale_out, FinalizeBuf *fbs) {
+    const int lane = threadIdx.x & 31;
+    const int k0 = bx * 32;
+    const int k = k0 + lane;
+    const bool act = k < P.S;
+    const bool is = P.is != 0;
+    const size_t Spad = (size_t)P.Spad;
+    const int n = P.n;
+
+    auto stage = [&](int r0, FinalizeBuf &fb) {
+        const int rows = min(32, n - r0);
+        for (int c = 0; c < 32; ++c) {
+            const int kc = k0 + c;
+            if (kc < P.S && lane < rows) cp_async8(&fb.x[lane][c], P.X + r0 + lane + (size_t)kc * P.ldx);
+        }
+        for (int t = 0; t < rows; ++t) {
+            const size_t at = (size_t)(r0 + t) * Spad + k;
+            if (act) {
+                cp_async8(&fb.c[t][lane], P.Cr + at);
+                cp_async8(&fb.s[t][lane], P.Sr + at);
+            } else {
+                fb.c[t][lane] = 0.0;
+                fb.s[t][lane] = 0.0;
+            }
+        }
+        cp_async_commit();
+    };
+
+    double smin = act ? P.beta[k] : sc_one(is);
+    for (int I = 1; I < P.T; ++I)
+        if (act) smin = sc_min(smin, P.beta[(size_t)I * Spad + k], is);
+
+    Nrm3 acc;
+    acc.init();
+    double tau1 = 0.0;
+    int I = 0;
+    double alpha = act ? sc_upscale(smin, P.beta[k], is) : 1.0;
+    stage(0, fbs[0]);
+    for (int r0 = 0, blk = 0; r0 < n; r0 += 32, ++blk) {
+        const int rows = min(32, n - r0);
+        FinalizeBuf &fb = fbs[blk & 1];
+        double (*buf)[33] = fb.x;
+        if (r0 + 32 < n) {
+            stage(r0 + 32, fbs[(blk + 1) & 1]);
+            cp_async_wait_one();
+        } else {
+            cp_async_wait_all();
+        }
+        __syncwarp();
+        for (int t = 0; t < rows; ++t) {
+            const int i = r0 + t;
+            if (i == P.fr[I + 1]) {
+                ++I;
+                alpha = act ? sc_upscale_rare(smin, P.beta[(size_t)I * Spad + k], is) : 1.0;
+            }
+            if (i == 0) {
+                tau1 = scale_by(alpha, buf[0][lane]);
+                continue;
+            }
+            const double tau2 = scale_by(alpha, buf[t][lane]);
+            const double c = fb.c[t][lane];
+            const double s = fb.s[t][lane];
+            const double out = fma(c, tau1, -(s * tau2));
+            tau1 = fma(c, tau2, s * tau1);
+            acc.add(out);
+            if (t == 0) {
+                if (act) P.X[(i - 1) + (size_t)k * P.ldx] = out;
+            } else {
+                buf[t - 1][lane] = out;
+            }
+        }
+        __syncwarp();
+        // rows r0 .. r0+rows-2 hold outputs; row r0-1 was written directly.
+        for (int c = 0; c < 32; ++c) {
+            const int kc = k0 + c;
+            if (kc < P.S && lane < rows - 1) P.X[r0 + lane + (size_t)kc * P.ldx] = buf[lane][c];
+        }
+        __syncwarp();                                          // this buffer is restaged two blocks on
+    }
+    if (act) {
+        P.X[(n - 1) + (size_t)k * P.ldx] = tau1;
+        acc.add(tau1);
+        const double ynrm = acc.finish();
+        colnorm[k] = ynrm;
+        status[k] = (ynrm > 0.1 / sqrt((double)n)) ? 1 : 0;
+        if (scale_out) scale_out[k] = smin;
+    }
+}
+
 __global__ void __launch_bounds__(32) k_finalize(DevProblem P, double *colnorm, int *status,
                                                  double *scale_out) {
-    finalize_body(P, blockIdx.x, colnorm, status, scale_out);
+    extern __shared__ double fsm[];
+    finalize_body_db(P, blockIdx.x, colnorm, status, scale_out, reinterpret_cast<FinalizeBuf *>(fsm));
 }
 
 cudaError_t launch_finalize(const DevProblem &P, double *colnorm, int *status, double *scale_out,
                             cudaStream_t st) {
-    k_finalize<<<(P.S + 31) / 32, 32, 0, st>>>(P, colnorm, status, scale_out);
+    static size_t configured = 0;
+    const size_t smem = 2 * sizeof(FinalizeBuf);
+    const cudaError_t e = raise_smem_limit((const void *)k_finalize, &configured, smem);
+    if (e != cudaSuccess) return e;
+    k_finalize<<<(P.S + 31) / 32, 32, smem, st>>>(P, colnorm, status, scale_out);
     return cudaGetLastError();
 }
 
