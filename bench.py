@@ -43,12 +43,14 @@ sys.path.insert(0, HERE)
 
 METRIC = "FP64 eigenvectors/s at n=10k"
 UNIT = "eigenvectors/s"
-# DRAM bytes per algorithmic FMA of k_gemm, from one ncu capture of the
-# n=4096, S=4096, tlsz=200 case (stage 10 rest launch: 183.61 MB of
-# dram__bytes_read+write for 1696*399*4096 FMAs).
-# Traffic and FMAs both grow with rows x shifts, so the ratio scales the
-# capture to the launches of this workload.
-GEMM_DRAM_BYTES_PER_FMA = (127.772928e6 + 54.166528e6) / (1696 * 399 * 4096)
+# DRAM bytes per algorithmic FMA of k_gemm, from one ncu capture of this
+# workload (n=10000, S=10000, tlsz=160; the launch over the 8080 rows above
+# tile 51: 1342.60 MB of dram__bytes_read and 1237.79 MB of
+# dram__bytes_write for 8080*319*10000 FMAs; the launch over 7920 rows gives
+# the same ratio within 0.1%).  The traffic is the read and write of R and
+# X over the rows above, so it grows with rows x shifts as the FMAs do, and
+# the ratio gives each launch's traffic.
+GEMM_DRAM_BYTES_PER_FMA = (1342.602752e6 + 1237.791744e6) / (8080 * 319 * 10000)
 
 
 def parse():
@@ -317,7 +319,7 @@ def run_gpu(args, H, wr, rank, world):
     roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": (achieved / peak) if achieved else None,
             "traffic": (GEMM_DRAM_BYTES_PER_FMA * gemm_fma / max(kl[3], 1)) if GEMM_DRAM_BYTES_PER_FMA else None,
-            "traffic_note": "DRAM bytes per launch, scaled from the n=4096 ncu capture by algorithmic FMAs",
+            "traffic_note": "DRAM bytes per launch: bytes per FMA from an ncu capture of this workload (n=10000, tlsz=160) times this run's FMAs per launch",
             "kernel": "k_gemm (crossover propagation + tile update, DFMA; the launches over the rows above "
                       "the next diagonal tile, which share the GPU with that tile's GEMM and diagonal solve)",
             "peak_source": "FP64 DFMA stream measured in this run (MEASURED_PEAKS.json has no FP64 figure)",

@@ -2241,114 +2241,145 @@ __device__ __forceinline__ void finalize_body(const DevProblem &P, int bx, doubl
     finalize_body_buf(P, bx, colnorm, status, scale_out, fb);
 }
 
-// The plain path's form of finalize_body_buf: the next 32-row block's X,
-// rotations and sines are brought in with cp.async while the current block's
-// rows are processed, so the sequential row loop never waits on a load (two
-// FinalizeBuf in dynamic shared memory).  The arithmetic and its order are
-// those of finalize_body_buf.
-__device__ __forceinline__ void finalize_body_db(const DevProblem &P, int bx, double *colnorm, int *status,
-                                                 double *scale_out, FinalizeBuf *fbs) {
+// The plain path's form of finalize_body_buf, on two warps for the same 32
+// shifts.  Warp 0 runs only the per-row recurrence (the back-transform
+// rotation of each row, reading X, the cosines and the sines from shared
+// memory) and leaves each row's result in an output buffer.  Warp 1 brings
+// the next 32-row block in with cp.async, and for the block warp 0 finished
+// one step earlier adds the results to the three-accumulator norm in row
+// order and writes them back to X.  The two warps meet at one barrier per
+// block, with double-buffered inputs and outputs.  Every value sees the
+// operations of finalize_body_buf in the same order, so the result is the
+// same bit for bit; the recurrence's warp no longer carries the loads, the
+// norm and the stores between one row's rotation and the next.
+struct FinalizeWs {
+    double x[2][32][33];                 // X rows of the block, [row][shift]
+    double c[2][32][33];                 // cosines, [row][shift]
+    double s[2][32][33];                 // sines, [row][shift]
+    double o[2][32][33];                 // results: o[t] is row r0 - 1 + t
+    double tail[32];                     // the last row's result, for warp 1
+};
+
+__device__ __forceinline__ void finalize_body_ws(const DevProblem &P, int bx, double *colnorm, int *status,
+                                                 double *scale_out, FinalizeWs &fw) {
     const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
     const int k0 = bx * 32;
     const int k = k0 + lane;
     const bool act = k < P.S;
     const bool is = P.is != 0;
     const size_t Spad = (size_t)P.Spad;
     const int n = P.n;
+    const int nb = (n + 31) / 32;
 
-    auto stage = [&](int r0, FinalizeBuf &fb) {
-        const int rows = min(32, n - r0);
+    auto stage = [&](int blk) {                                // warp 1
+        const int r0 = blk * 32, rows = min(32, n - r0), q = blk & 1;
         for (int c = 0; c < 32; ++c) {
             const int kc = k0 + c;
-            if (kc < P.S && lane < rows) cp_async8(&fb.x[lane][c], P.X + r0 + lane + (size_t)kc * P.ldx);
+            if (kc < P.S && lane < rows) cp_async8(&fw.x[q][lane][c], P.X + r0 + lane + (size_t)kc * P.ldx);
         }
         for (int t = 0; t < rows; ++t) {
             const size_t at = (size_t)(r0 + t) * Spad + k;
             if (act) {
-                cp_async8(&fb.c[t][lane], P.Cr + at);
-                cp_async8(&fb.s[t][lane], P.Sr + at);
+                cp_async8(&fw.c[q][t][lane], P.Cr + at);
+                cp_async8(&fw.s[q][t][lane], P.Sr + at);
             } else {
-                fb.c[t][lane] = 0.0;
-                fb.s[t][lane] = 0.0;
+                fw.c[q][t][lane] = 0.0;
+                fw.s[q][t][lane] = 0.0;
             }
         }
         cp_async_commit();
+        cp_async_wait_all();
     };
 
-    double smin = act ? P.beta[k] : sc_one(is);
-    for (int I = 1; I < P.T; ++I)
-        if (act) smin = sc_min(smin, P.beta[(size_t)I * Spad + k], is);
-
+    // Warp 0: the recurrence.
+    double tau1 = 0.0, alpha = 1.0, smin = 0.0;
+    int I = 0, nbound = 0;
+    if (wid == 0) {
+        smin = act ? P.beta[k] : sc_one(is);
+        for (int J = 1; J < P.T; ++J)
+            if (act) smin = sc_min(smin, P.beta[(size_t)J * Spad + k], is);
+        alpha = act ? sc_upscale(smin, P.beta[k], is) : 1.0;
+        nbound = P.fr[1];
+    }
+    // Warp 1: the norm.
     Nrm3 acc;
     acc.init();
-    double tau1 = 0.0;
-    int I = 0;
-    double alpha = act ? sc_upscale(smin, P.beta[k], is) : 1.0;
-    stage(0, fbs[0]);
-    for (int r0 = 0, blk = 0; r0 < n; r0 += 32, ++blk) {
-        const int rows = min(32, n - r0);
-        FinalizeBuf &fb = fbs[blk & 1];
-        double (*buf)[33] = fb.x;
-        if (r0 + 32 < n) {
-            stage(r0 + 32, fbs[(blk + 1) & 1]);
-            cp_async_wait_one();
-        } else {
-            cp_async_wait_all();
-        }
-        __syncwarp();
-        for (int t = 0; t < rows; ++t) {
-            const int i = r0 + t;
-            if (i == P.fr[I + 1]) {
-                ++I;
-                alpha = act ? sc_upscale_rare(smin, P.beta[(size_t)I * Spad + k], is) : 1.0;
-            }
-            if (i == 0) {
-                tau1 = scale_by(alpha, buf[0][lane]);
-                continue;
-            }
-            const double tau2 = scale_by(alpha, buf[t][lane]);
-            const double c = fb.c[t][lane];
-            const double s = fb.s[t][lane];
-            const double out = fma(c, tau1, -(s * tau2));
-            tau1 = fma(c, tau2, s * tau1);
-            acc.add(out);
-            if (t == 0) {
-                if (act) P.X[(i - 1) + (size_t)k * P.ldx] = out;
-            } else {
-                buf[t - 1][lane] = out;
+
+    if (wid == 1) stage(0);
+    __syncthreads();                                           // block 0 in
+    for (int blk = 0; blk <= nb; ++blk) {
+        if (wid == 0 && blk < nb) {
+            const int r0 = blk * 32, rows = min(32, n - r0), q = blk & 1;
+            double (*xb)[33] = fw.x[q];
+            double (*cb)[33] = fw.c[q];
+            double (*sb)[33] = fw.s[q];
+            double (*ob)[33] = fw.o[q];
+            for (int t = 0; t < rows; ++t) {
+                const int i = r0 + t;
+                if (i == nbound) {                             // tile boundary: the next tile's upscaling
+                    ++I;
+                    nbound = P.fr[I + 1];
+                    alpha = act ? sc_upscale_rare(smin, P.beta[(size_t)I * Spad + k], is) : 1.0;
+                }
+                if (i == 0) {
+                    tau1 = scale_by(alpha, xb[0][lane]);
+                    continue;
+                }
+                const double tau2 = scale_by(alpha, xb[t][lane]);
+                const double c = cb[t][lane];
+                const double s = sb[t][lane];
+                ob[t][lane] = fma(c, tau1, -(s * tau2));       // row i - 1
+                tau1 = fma(c, tau2, s * tau1);
             }
         }
-        __syncwarp();
-        // rows r0 .. r0+rows-2 hold outputs; row r0-1 was written directly.
-        for (int c = 0; c < 32; ++c) {
-            const int kc = k0 + c;
-            if (kc < P.S && lane < rows - 1) P.X[r0 + lane + (size_t)kc * P.ldx] = buf[lane][c];
+        if (wid == 1) {
+            if (blk >= 1) {
+                // Results of block blk-1: rows r0-1 .. r0+rows-2 (row -1 does not exist).
+                const int p = blk - 1, r0 = p * 32, rows = min(32, n - r0), q = p & 1;
+                double (*ob)[33] = fw.o[q];
+                for (int t = (r0 == 0 ? 1 : 0); t < rows; ++t) acc.add(ob[t][lane]);
+                __syncwarp();
+                const int lo = r0 == 0 ? 1 : 0;
+                for (int c = 0; c < 32; ++c) {
+                    const int kc = k0 + c;
+                    if (kc < P.S && lane >= lo && lane < rows)
+                        P.X[(r0 - 1 + lane) + (size_t)kc * P.ldx] = ob[lane][c];
+                }
+            }
+            if (blk + 1 < nb) stage(blk + 1);
         }
-        __syncwarp();                                          // this buffer is restaged two blocks on
+        __syncthreads();
     }
-    if (act) {
-        P.X[(n - 1) + (size_t)k * P.ldx] = tau1;
-        acc.add(tau1);
+    if (wid == 0) {
+        fw.tail[lane] = tau1;
+        if (act) {
+            P.X[(n - 1) + (size_t)k * P.ldx] = tau1;
+            if (scale_out) scale_out[k] = smin;
+        }
+    }
+    __syncthreads();
+    if (wid == 1 && act) {
+        acc.add(fw.tail[lane]);
         const double ynrm = acc.finish();
         colnorm[k] = ynrm;
         status[k] = (ynrm > 0.1 / sqrt((double)n)) ? 1 : 0;
-        if (scale_out) scale_out[k] = smin;
     }
 }
 
-__global__ void __launch_bounds__(32) k_finalize(DevProblem P, double *colnorm, int *status,
+__global__ void __launch_bounds__(64) k_finalize(DevProblem P, double *colnorm, int *status,
                                                  double *scale_out) {
     extern __shared__ double fsm[];
-    finalize_body_db(P, blockIdx.x, colnorm, status, scale_out, reinterpret_cast<FinalizeBuf *>(fsm));
+    finalize_body_ws(P, blockIdx.x, colnorm, status, scale_out, *reinterpret_cast<FinalizeWs *>(fsm));
 }
 
 cudaError_t launch_finalize(const DevProblem &P, double *colnorm, int *status, double *scale_out,
                             cudaStream_t st) {
     static size_t configured = 0;
-    const size_t smem = 2 * sizeof(FinalizeBuf);
+    const size_t smem = sizeof(FinalizeWs);
     const cudaError_t e = raise_smem_limit((const void *)k_finalize, &configured, smem);
     if (e != cudaSuccess) return e;
-    k_finalize<<<(P.S + 31) / 32, 32, smem, st>>>(P, colnorm, status, scale_out);
+    k_finalize<<<(P.S + 31) / 32, 64, smem, st>>>(P, colnorm, status, scale_out);
     return cudaGetLastError();
 }
 
