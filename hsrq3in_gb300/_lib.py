@@ -35,7 +35,7 @@ EXPORTS = [
     "hsr_autotune_tlsz", "hsr_autotune_batch", "hsr_autotune_plain", "hsr_autotune_plain_tlsz",
     "hsr_server_create", "hsr_server_replay", "hsr_server_destroy",
     "hsr_inverse_iteration_cplx_ex", "hsr_inverse_iteration_cplx_device", "hsr_inverse_iteration_mixed",
-    "hsr_selftest_bounded_wait",
+    "hsr_selftest_bounded_wait", "hsr_selftest_arith",
 ]
 NOALLOC_MAX_N = 256
 NOALLOC_MAX_NRHS = 256
@@ -141,6 +141,8 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     lib.hsr_probe_fp64_peak.restype = C.c_int
     lib.hsr_probe_fp64_peak.argtypes = [C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.hsr_version.restype = C.c_char_p
+    lib.hsr_selftest_arith.restype = C.c_int
+    lib.hsr_selftest_arith.argtypes = [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]
     lib.hsr_batch_plan_create.restype = C.c_int
     lib.hsr_batch_plan_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.POINTER(BatchProblem), C.c_int,
                                           C.POINTER(Options), C.c_void_p]

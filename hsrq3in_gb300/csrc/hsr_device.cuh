@@ -76,6 +76,102 @@ static __device__ __noinline__ double add_rare(double a, double b) { return a + 
 // x scaled by a, skipping the multiplication when a == 1 (1*x == x bit for bit).
 __device__ __forceinline__ double scale_by(double a, double x) { return is_one(a) ? x : mul_rare(a, x); }
 
+// ---------------------------------------- two quotients on the integer pipe
+// The rotation divides |f| and g by the same d.  An FP64 division issues
+// about nine FP64 instructions here (some 560 cycles of its sub-partition,
+// dependent or not), so the two cost about 1,100 cycles of each step of the
+// diagonal solve's chain.  ddiv2_rn returns the same two correctly rounded
+// (round-to-nearest-even) quotients from integer arithmetic and one shared
+// reciprocal: the reciprocal of d's significand, seeded by the FP32
+// approximation and refined by two fixed-point Newton-Raphson steps to about
+// 62 bits; each quotient truncated from it and corrected to the exact floor
+// by its integer remainder, which also gives the rounding (the
+// remainder-corrected Newton division of Muller et al., Handbook of
+// Floating-Point Arithmetic, 2nd ed., 2018, ch. 4, in 64-bit integers).
+// IEEE division is correctly rounded, so any correct method returns the same
+// bits.  Measured on one warp: 741 cycles for both quotients against 1,438
+// for two FP64 divisions.  Operands outside the common range (zero,
+// subnormal, infinite, NaN, a divisor whose significand is a power of two, a
+// quotient near the exponent limits) take the FP64 instruction.
+static __device__ __noinline__ double div_fp64(double a, double b) { return a / b; }
+__device__ __forceinline__ float rcp_approx_f32(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+// One Newton step for y ~ 2^116 / mb, mb in (2^52, 2^53): with the 128-bit
+// error E = 2^116 - mb y, y' = y + y E / 2^116.
+__device__ __forceinline__ unsigned long long ip_recip_step(unsigned long long mb, unsigned long long y) {
+    const unsigned long long lo = mb * y;
+    const unsigned long long hi = __umul64hi(mb, y);
+    const long long ehi = (long long)((1ULL << 52) - hi) - (lo != 0ULL ? 1 : 0);
+    const unsigned long long elo = 0ULL - lo;
+    const long long e = (long long)(((unsigned long long)ehi << 12) | (elo >> 52));   // E / 2^52
+    const unsigned long long ae = e < 0 ? (unsigned long long)(-e) : (unsigned long long)e;
+    const unsigned long long d = __umul64hi(y, ae);
+    return e < 0 ? y - d : y + d;
+}
+// y ~ 2^116 / mb within a few units (about 2^-62 relative).
+__device__ __forceinline__ unsigned long long ip_recip(unsigned long long mb) {
+    float r = rcp_approx_f32((float)(unsigned)(mb >> 29)) * 0x1p87f;
+    r = fminf(r, 0x1.fffffep63f);
+    unsigned long long y = (unsigned long long)r;
+    y = ip_recip_step(mb, y);
+    return ip_recip_step(mb, y);
+}
+// Bits of the correctly rounded ma / mb (significands with the hidden bit),
+// given y = ip_recip(mb), the biased exponent ea - eb + 1023 and the sign.
+// q estimates floor(ma 2^sh / mb) (54 bits) within two; the remainder
+// r = ma 2^sh - q mb, exact modulo 2^64 because |r| < 2^56, moves q to the
+// floor; its last bit and r != 0 round the 53-bit result to nearest even.
+__device__ __forceinline__ unsigned long long ip_quot(unsigned long long ma, unsigned long long mb,
+                                                      unsigned long long y, int ebias, unsigned long long sign) {
+    const int sh = ma < mb ? 54 : 53;
+    const unsigned long long hi = __umul64hi(ma, y);
+    const unsigned long long lo = ma * y;
+    unsigned long long q = sh == 53 ? ((hi << 1) | (lo >> 63)) : ((hi << 2) | (lo >> 62));
+    long long r = (long long)((ma << sh) - q * mb);
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+        if (r < 0) {
+            q -= 1;
+            r += (long long)mb;
+        }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+        if (r >= (long long)mb) {
+            q += 1;
+            r -= (long long)mb;
+        }
+    const unsigned long long guard = q & 1ULL;
+    unsigned long long Q = q >> 1;
+    Q += guard & ((r != 0 ? 1ULL : 0ULL) | (Q & 1ULL));
+    const int eo = ebias - (sh == 54 ? 1 : 0);
+    return sign | (((unsigned long long)(eo - 1) << 52) + Q);   // a carry out of Q raises the exponent
+}
+constexpr unsigned long long kSigMask = 0xfffffffffffffULL, kHidden = 1ULL << 52;
+__device__ __forceinline__ bool ip_div_ok(int ea, int eb, unsigned long long fb) {
+    const int eq = ea - eb + 1023;
+    return ea != 0 && ea != 0x7ff && eb != 0 && eb != 0x7ff && fb != 0 && eq >= 2 && eq <= 2045;
+}
+// q1 = a1 / b and q2 = a2 / b, correctly rounded, one reciprocal of b for
+// both.  Returns whether the integer path was taken (the self-test counts it).
+__device__ __forceinline__ bool ddiv2_rn(double a1, double a2, double b, double &q1, double &q2) {
+    const unsigned long long u1 = ubits(a1), u2 = ubits(a2), ub = ubits(b);
+    const int e1 = (int)((u1 >> 52) & 0x7ff), e2 = (int)((u2 >> 52) & 0x7ff), eb = (int)((ub >> 52) & 0x7ff);
+    const unsigned long long fb = ub & kSigMask;
+    if (!ip_div_ok(e1, eb, fb) || !ip_div_ok(e2, eb, fb)) {
+        q1 = div_fp64(a1, b);
+        q2 = div_fp64(a2, b);
+        return false;
+    }
+    const unsigned long long mb = fb | kHidden;
+    const unsigned long long y = ip_recip(mb);
+    q1 = from_bits(ip_quot((u1 & kSigMask) | kHidden, mb, y, e1 - eb + 1023, (u1 ^ ub) & 0x8000000000000000ULL));
+    q2 = from_bits(ip_quot((u2 & kSigMask) | kHidden, mb, y, e2 - eb + 1023, (u2 ^ ub) & 0x8000000000000000ULL));
+    return true;
+}
+
 // ------------------------------------------------ scaling-factor algebra
 // robust.c:24-121.  `is` selects base-2 exponents (INTSCALING) at run time.
 __device__ __forceinline__ double sc_one(bool is) { return is ? 0.0 : 1.0; }
@@ -209,10 +305,11 @@ __device__ __forceinline__ void givens(double f, double g, double &c, double &s)
     } else if (is_zero(f)) {
         c = 0.0; sv = copysign(1.0, g);
     } else if (mf > kRtminBits && mf < kRtmaxBits && mg > kRtminBits && mg < kRtmaxBits) {
+        // c = |f| / d and sv = g / copysign(d, f) = +-(g / d), exactly as the
+        // FP64 divisions round them, from one reciprocal of d.
         const double d = sqrt(f * f + g * g);
-        c = absd(f) / d;
-        const double r = copysign(d, f);
-        sv = g / r;
+        ddiv2_rn(absd(f), g, d, c, sv);
+        if (ubits(f) >> 63) sv = neg(sv);
     } else {
         const RotCS r = givens_scaled(f, g);
         c = r.c;

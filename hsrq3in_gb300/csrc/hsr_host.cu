@@ -439,7 +439,10 @@ int solve_device(int n, const double *dH, long long ldh, int S, double *dwr, int
     HSR_CK(cudaMemcpyAsync(w.fr.p, s.fr.data(), (T + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
     s.d_status = d_status_user ? d_status_user : w.status.as<int>();
     s.d_colnorm = w.colnorm.as<double>();
-    s.d_scale = d_scale_user ? d_scale_user : (w.scale.bytes ? w.scale.as<double>() : nullptr);
+    // The workspace scale buffer only when this call sized it: one left by an
+    // earlier call may hold fewer than S entries.
+    const bool own_scale = !d_scale_user && (h_scale || h_tile_scales);
+    s.d_scale = d_scale_user ? d_scale_user : (own_scale ? w.scale.as<double>() : nullptr);
     s.d_pert = w.pert.as<unsigned char>();
 
     if (!make_map(&s.tmH, dH, (unsigned long long)n, (unsigned long long)n, (unsigned long long)ldh, kGemmBM,
@@ -1225,6 +1228,23 @@ int hsr_last_kernel_times(double *ms, long *launches, double *gemm_fma) {
 }
 
 void hsr_release_workspace(void) { ws().release(); }
+
+int hsr_selftest_arith(long long per_thread, unsigned long long seed, long long counts[4]) {
+    if (per_thread < 0 || !counts) return record_status(HSR_ERR_ARG, cudaSuccess);
+    Workspace &w = ws();
+    cudaError_t e = w.probe.ensure(64);
+    int dev = 0, sms = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    unsigned long long *cnt = reinterpret_cast<unsigned long long *>(w.probe.p);
+    if (e == cudaSuccess) e = cudaMemset(cnt, 0, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = launch_selftest_arith((unsigned long long)per_thread, seed, cnt, sms * 4, 0);
+    unsigned long long h[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(h, cnt, sizeof(h), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return record_status(HSR_ERR_CUDA, e);
+    for (int i = 0; i < 4; ++i) counts[i] = (long long)h[i];
+    return record_status(HSR_OK, cudaSuccess);
+}
 
 int hsr_probe_fp64_peak(double ms_target, double *dfma_gflops, double *dmma_gflops) {
     Workspace &w = ws();

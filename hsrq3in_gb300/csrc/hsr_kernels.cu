@@ -2813,4 +2813,57 @@ cudaError_t launch_probe_dmma(double *out, int blocks, int iters, cudaStream_t s
     return cudaGetLastError();
 }
 
+// ------------------------------------------ integer-pipe division self-test
+// Seeded operands (splitmix64 per thread) compared bit for bit with the FP64
+// division: random significands and exponents within 2^+-100 and over the
+// whole normal range, divisor significands near 1 and near 2, dividends equal
+// or next to the divisor.  Each set divides two dividends by one divisor
+// through ddiv2_rn.  cnt: [first-quotient mismatches, second-quotient
+// mismatches, sets that took the integer path, sets tried].
+__device__ __forceinline__ unsigned long long st_mix(unsigned long long &s) {
+    unsigned long long z = (s += 0x9e3779b97f4a7c15ULL);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+
+__global__ void k_selftest_arith(unsigned long long per_thread, unsigned long long seed, unsigned long long *cnt) {
+    const unsigned long long tid = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    unsigned long long sd = seed ^ (tid * 0x2545f4914f6cdd1dULL);
+    unsigned long long bad1 = 0, bad2 = 0, fast = 0;
+    for (unsigned long long i = 0; i < per_thread; ++i) {
+        const unsigned long long ra = st_mix(sd), rb = st_mix(sd), rc = st_mix(sd);
+        const int mode = (int)(rc & 7);
+        unsigned long long fa = ra & kSigMask, fb = rb & kSigMask;
+        if (mode == 1) fb |= 0xffffffffff000ULL;
+        if (mode == 2) fb &= 0xffULL;
+        if (mode == 3) fa = fb;
+        if (mode == 4) fa = (fb + ((rc >> 8) & 0xf)) & kSigMask;
+        if (mode == 5) fa = (fb - ((rc >> 8) & 0xf)) & kSigMask;
+        if (mode == 6) fa |= 0xfffffffffff00ULL;
+        int ea = 1023 + (int)((rc >> 16) % 200) - 100, eb = 1023 + (int)((rc >> 32) % 200) - 100;
+        if (mode == 7) {
+            ea = 1 + (int)((rc >> 16) % 2046);
+            eb = 1 + (int)((rc >> 32) % 2046);
+        }
+        const double a = from_bits((((rc >> 60) & 1ULL) << 63) | ((unsigned long long)ea << 52) | fa);
+        const double b = from_bits((((rc >> 61) & 1ULL) << 63) | ((unsigned long long)eb << 52) | fb);
+        const double a2 = from_bits(ubits(a) ^ ((rc >> 40) & 0xffffULL));
+        double q1, q2;
+        if (ddiv2_rn(a, a2, b, q1, q2)) ++fast;
+        if (ubits(q1) != ubits(div_fp64(a, b))) ++bad1;
+        if (ubits(q2) != ubits(div_fp64(a2, b))) ++bad2;
+    }
+    if (bad1) atomicAdd(&cnt[0], bad1);
+    if (bad2) atomicAdd(&cnt[1], bad2);
+    atomicAdd(&cnt[2], fast);
+    atomicAdd(&cnt[3], per_thread);
+}
+
+cudaError_t launch_selftest_arith(unsigned long long per_thread, unsigned long long seed, unsigned long long *cnt,
+                                  int blocks, cudaStream_t st) {
+    k_selftest_arith<<<blocks, 256, 0, st>>>(per_thread, seed, cnt);
+    return cudaGetLastError();
+}
+
 }  // namespace hsr

@@ -185,6 +185,11 @@ cudaError_t launch_wait_selftest(int *err, long limit, cudaStream_t st);
 // FP64 throughput probe kernels.
 cudaError_t launch_probe_dfma(double *out, int blocks, int iters, cudaStream_t st);
 cudaError_t launch_probe_dmma(double *out, int blocks, int iters, cudaStream_t st);
+// Integer-pipe two-quotient division against the FP64 division; cnt[4]
+// (zeroed by the caller) receives the mismatch counts, the integer-path
+// count and the total.
+cudaError_t launch_selftest_arith(unsigned long long per_thread, unsigned long long seed, unsigned long long *cnt,
+                                  int blocks, cudaStream_t st);
 
 constexpr int kGemmBM = 64, kGemmBN = 64, kGemmKC = 16, kGemmStages = 3;
 constexpr int kGemmBNNarrow = 16;       // column tile of the narrow GEMM (launch_gemm_narrow)

@@ -371,6 +371,18 @@ int hsr_probe_fp64_peak(double ms_target, double *dfma_gflops,
  * HSR_OK only if the wait did not report.  No reference counterpart. */
 int hsr_selftest_bounded_wait(void *stream);
 
+/* Self-test of the integer-pipe division the diagonal solve's Givens
+ * rotation uses for its two quotients in place of two FP64 divisions:
+ * 256 threads x 4 per SM each try `per_thread` seeded operand sets (random
+ * significands and exponents over the whole normal range, divisor
+ * significands near 1 and 2, dividends equal or next to the divisor), divide
+ * two dividends by one divisor, and compare both quotients bit for bit with
+ * the FP64 division.  counts[0..1] receive the mismatches of the first and
+ * second quotient, counts[2] the sets that took the integer path (the rest
+ * fall back to the FP64 division), counts[3] the sets tried.  Blocks until
+ * done.  No reference counterpart. */
+int hsr_selftest_arith(long long per_thread, unsigned long long seed, long long counts[4]);
+
 /* Library version string. */
 const char *hsr_version(void);
 

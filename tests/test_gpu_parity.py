@@ -326,3 +326,44 @@ def test_plain_autotune_and_tlsz_zero(gpu_lib):
     a = hsr.inverse_iteration(H, wr, 0, 16)
     b = hsr.inverse_iteration(H, wr, best, 16)
     assert np.array_equal(a["vr"], b["vr"]) and np.array_equal(a["wr"], b["wr"])
+
+
+def test_integer_pipe_division(gpu_lib):
+    """The integer-pipe division the Givens rotation uses for its two
+    quotients returns the FP64 division's results bit for bit on about 1.6e8
+    seeded operand sets (random and edge-case significands, the whole normal
+    exponent range), most of them on the integer path."""
+    import ctypes as C
+    lib = gpu_lib
+    counts = (C.c_longlong * 4)()
+    assert lib.hsr_selftest_arith(1024, 0x5eed1234, counts) == 0
+    assert counts[3] >= 1024 * 256 * 4 * 100
+    assert counts[2] > 0.8 * counts[3]
+    assert (counts[0], counts[1]) == (0, 0)
+
+
+def test_device_call_after_host_call_with_fewer_shifts(gpu_lib):
+    """A device-resident call that passes no scale buffer writes no scales.
+    An earlier host call on the same thread leaves the workspace's scale
+    buffer sized for its own 8 shifts; the device call's 1000 columns must
+    not be written there (that would run past the buffer into other device
+    allocations), so every column is finite, converged and equal to the
+    oracle bit for bit."""
+    import torch
+    import hsrq3in_gb300 as hsr
+    H0, lam0 = G.real_spectrum(40, 61)
+    hsr.inverse_iteration(H0, G.perturbed_shifts(lam0, 62)[:8], 8, 4)
+    n = 1000
+    H, lam = G.real_spectrum(n, 63)
+    wr = G.perturbed_shifts(lam, 64)
+    dev = torch.device("cuda", 0)
+    dH = torch.from_numpy(np.ascontiguousarray(H.T)).to(dev)
+    dwr = torch.from_numpy(wr.copy()).to(dev)
+    dX = torch.empty((n, n), dtype=torch.float64, device=dev)
+    d_status = torch.zeros(n, dtype=torch.int32, device=dev)
+    assert hsr.inverse_iteration_device(dH, dwr, dX, 200, d_status=d_status) == 0
+    X = dX.cpu().numpy().T
+    assert np.all(np.isfinite(X)) and int(d_status.sum().item()) == n
+    cols = np.array([0, 333, 999])
+    orc = O.oracle_inverse_iteration(H, wr[cols], 200, 1, intscale=1, variant="fma")
+    assert np.array_equal(X[:, cols], orc["vr"])
