@@ -334,7 +334,7 @@ int run_pass(Solver &s, int mode, int its, int off, int cnt) {
             cudaError_t fe = cudaSuccess;
             ++g_launches;
             g_timing.begin(kcDiag, D);
-            const bool fused = launch_diag_fused(Pn, P, J - 1, s.fr[J] - s.fr[J - 1], bj, D, &fe);
+            const bool fused = launch_diag_fused(Pn, P, J - 1, s.fr[J] - s.fr[J - 1], D, &fe);
             g_timing.end(D);
             if (!fused) {
                 --g_launches;

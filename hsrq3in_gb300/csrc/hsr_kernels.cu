@@ -1300,9 +1300,8 @@ __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int
 // more passes.  The two buffers, (rows + 2 SC) x kTopChunk doubles each, are
 // 10 KB at tlsz 64 -- no more than the diagonal solve's own shared memory,
 // which reuses them afterwards, so the CTA still fits beside two GEMM CTAs
-// on one SM.  Taller tiles use the global form.
+// on one SM; from 16 rows on they are no larger than the diagonal solve's.
 constexpr int kTopChunk = 8, kTopRowsPerThread = 6;
-constexpr size_t kTopStagedMaxBytes = 16 * 1024;
 template <int SC>
 __host__ __device__ constexpr size_t top_staged_bytes(int rows) {
     return 2 * ((size_t)rows + 2 * SC) * kTopChunk * sizeof(double);
@@ -1390,63 +1389,20 @@ __device__ __forceinline__ void top_rows_staged(const DevProblem &Pg, int J, int
     if (col < Pg.S && m) atomicMax(reinterpret_cast<unsigned long long *>(Pg.ynorm) + (size_t)J * Spad + col, m);
 }
 
-// Fallback for blocks too large to stage: the same sums with operands read
-// from global memory.
-template <int SC, int NW>
-__device__ __forceinline__ void top_rows_global(const DevProblem &Pg, int J, int k0) {
-    const int Js = J + 1;
-    const int l = Pg.fr[Js], b = Pg.fr[Js + 1] - l;
-    const int r_lo = Pg.fr[J], rows = l - r_lo;
-    const size_t Spad = (size_t)Pg.Spad;
-    unsigned long long *ynb = reinterpret_cast<unsigned long long *>(Pg.ynorm);
-    for (int e = threadIdx.x; e < rows * SC; e += 32 * NW) {
-        const int rr = e / SC, col = k0 + (e - rr * SC);
-        if (col >= Pg.S) continue;
-        const int row = r_lo + rr;
-        const double *hrow = Pg.H + row + (size_t)(l - 1) * Pg.ldh;
-        double aw = 0.0, az = 0.0;
-        int k = 0;
-        for (; k + 3 < b; k += 4) {
-            double a[4], w[4], z[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                a[q] = hrow[(size_t)(k + q) * Pg.ldh];
-                w[q] = Pg.W[(size_t)(k + q) * Spad + col];
-                z[q] = Pg.Zs[(size_t)(k + q) * Spad + col];
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                aw = fma(a[q], w[q], aw);
-                az = fma(a[q], z[q], az);
-            }
-        }
-        for (; k < b; ++k) {
-            const double a = hrow[(size_t)k * Pg.ldh];
-            aw = fma(a, Pg.W[(size_t)k * Spad + col], aw);
-            az = fma(a, Pg.Zs[(size_t)k * Spad + col], az);
-        }
-        const double hl1 = Pg.H[row + (size_t)(l - 1) * Pg.ldh];
-        const unsigned long long m = gemm_epilogue_elem(Pg, l, b, row, J, col, hl1, aw, az);
-        atomicMax(&ynb[(size_t)J * Spad + col], m);
-    }
-}
-
-// Fused form: the GEMM of stage J+1 over this tile's rows (staged when the
-// launch gave it the shared memory, else from global memory), then the
-// diagonal solve of tile J, in one CTA.
+// Fused form: the GEMM of stage J+1 over this tile's rows (top_rows_staged),
+// then the diagonal solve of tile J, in one CTA.  The launch gives the larger
+// of the two shared-memory footprints; a launch given less records a shape
+// error and touches nothing.
 template <int SC, int NW>
 __global__ void __launch_bounds__(32 * NW) k_diag_nf(DevProblem P, DevProblem Pg, int J) {
     const int b = P.fr[J + 1] - P.fr[J];
     const size_t have = dynamic_smem_bytes();
-    if (diag_narrow_smem_bytes<SC>(b, NW) > have) {
+    if (diag_narrow_smem_bytes<SC>(b, NW) > have || top_staged_bytes<SC>(b) > have) {
         if (threadIdx.x == 0) atomicOr(P.err, kErrShape);
         return;
     }
     extern __shared__ double sm[];
-    if (top_staged_bytes<SC>(b) <= have)
-        top_rows_staged<SC, NW>(Pg, J, blockIdx.x * SC, sm);
-    else
-        top_rows_global<SC, NW>(Pg, J, blockIdx.x * SC);
+    top_rows_staged<SC, NW>(Pg, J, blockIdx.x * SC, sm);
     __syncthreads();                     // this CTA's rows of tile J are final; shared memory free
     diag_body_narrow<SC, NW>(P, J, blockIdx.x);
 }
@@ -1502,12 +1458,9 @@ cudaError_t launch_diag_narrow(const DevProblem &P, int J, int b, cudaStream_t s
 }
 
 template <int SC, int NW>
-cudaError_t launch_diag_narrow_fused(const DevProblem &P, const DevProblem &Pg, int J, int b, int bs,
-                                     cudaStream_t st) {
+cudaError_t launch_diag_narrow_fused(const DevProblem &P, const DevProblem &Pg, int J, int b, cudaStream_t st) {
     static size_t configured = 0;
-    size_t smem = diag_narrow_smem_bytes<SC>(b, NW);
-    const size_t top = top_staged_bytes<SC>(b);
-    if (top <= kTopStagedMaxBytes && top > smem) smem = top;
+    const size_t smem = std::max(diag_narrow_smem_bytes<SC>(b, NW), top_staged_bytes<SC>(b));
     static bool carve = false;
     cudaError_t e = prefer_max_shared((const void *)k_diag_nf<SC, NW>, &carve);
     if (e == cudaSuccess) e = raise_smem_limit((const void *)k_diag_nf<SC, NW>, &configured, smem);
@@ -1519,13 +1472,13 @@ cudaError_t launch_diag_narrow_fused(const DevProblem &P, const DevProblem &Pg, 
 // Tile J's diagonal solve preceded by stage J+1's GEMM over tile J's rows,
 // in one launch, when the narrow forms apply; false (nothing launched) when
 // the wide form is used and the caller runs the two launches.
-bool launch_diag_fused(const DevProblem &P, const DevProblem &Pg, int J, int b, int bs, cudaStream_t st,
+bool launch_diag_fused(const DevProblem &P, const DevProblem &Pg, int J, int b, cudaStream_t st,
                        cudaError_t *err) {
     const char *env = getenv("HSR_FUSED_TOP");          // 0: separate launches, for comparison
     if (env && env[0] == '0') return false;
     switch (diag_shifts_per_cta(P.S)) {
-    case 8: *err = launch_diag_narrow_fused<8, kDiagWarpsNarrow>(P, Pg, J, b, bs, st); return true;
-    case 16: *err = launch_diag_narrow_fused<16, kDiagWarpsNarrow>(P, Pg, J, b, bs, st); return true;
+    case 8: *err = launch_diag_narrow_fused<8, kDiagWarpsNarrow>(P, Pg, J, b, st); return true;
+    case 16: *err = launch_diag_narrow_fused<16, kDiagWarpsNarrow>(P, Pg, J, b, st); return true;
     default: return false;
     }
 }

@@ -72,10 +72,9 @@ cudaError_t launch_init(const DevProblem &P, int mode, const double *eps3_dev,
 cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cudaStream_t st);
 // Few shifts: tile J's diagonal solve preceded, in the same CTAs, by the GEMM
 // of stage J+1 over tile J's rows (Pg: the descriptor with stage J+1's
-// operands; b: tile J's height, bs: stage J+1's width).  Returns false,
-// launching nothing, where the wide diagonal form applies; otherwise *err
-// holds the launch status.
-bool launch_diag_fused(const DevProblem &P, const DevProblem &Pg, int J, int b, int bs, cudaStream_t st,
+// operands; b: tile J's height).  Returns false, launching nothing, where
+// the wide diagonal form applies; otherwise *err holds the launch status.
+bool launch_diag_fused(const DevProblem &P, const DevProblem &Pg, int J, int b, cudaStream_t st,
                        cudaError_t *err);
 // Shifts per CTA the diagonal kernel uses for S shifts: 8, 16 or 32 -- the
 // HSR_DIAG_SHIFTS_PER_CTA override, else this thread's autotuning trial, else
