@@ -415,8 +415,8 @@ def run_plain_small(args, tlsz: int):
     # region); its measured alternatives go into the line.
     cands = (48, 64, 96, 128, 160, 200)
     with torch.cuda.stream(stream):
-        tuned, tune_ms, tuned_sc, sc_ms = hsr.autotune_plain(dHt, dwr, dX, candidates=cands, stream=stream,
-                                                              detail=True)
+        tuned, tune_ms, tuned_sc, sc_ms, tuned_fused, fused_ms = hsr.autotune_plain(
+            dHt, dwr, dX, candidates=cands, stream=stream, detail=True)
     torch.cuda.synchronize()
     if tlsz == 0:
         tlsz = tuned
@@ -470,6 +470,9 @@ def run_plain_small(args, tlsz: int):
            "autotune": {"candidates": list(cands), "ms": [round(x, 3) for x in tune_ms], "best": tuned,
                         "shifts_per_cta": {"candidates": [8, 16, 32], "ms": [round(x, 3) for x in sc_ms],
                                            "best": tuned_sc},
+                        "top_gemm": {"candidates": ["separate launch", "inside the diagonal CTAs"],
+                                     "ms": [round(x, 3) for x in fused_ms],
+                                     "best": "inside the diagonal CTAs" if tuned_fused else "separate launch"},
                         "api": "hsr_autotune_plain"},
            "gpu_launches_per_step": launches / steps, "clocks": clk.summary()}
     # e2e through the drop-in entry point, pinned host buffers, flush between steps

@@ -165,7 +165,8 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     lib.hsr_autotune_plain.restype = C.c_int
     lib.hsr_autotune_plain.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                        C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int),
-                                       C.POINTER(C.c_double), C.c_void_p]
+                                       C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                       C.c_void_p]
     lib.hsr_autotune_plain_tlsz.restype = C.c_int
     lib.hsr_autotune_plain_tlsz.argtypes = [C.c_int]
     lib.hsr_server_create.restype = C.c_int

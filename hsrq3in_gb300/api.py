@@ -311,23 +311,27 @@ class BatchPlan:
 
 def autotune_plain(dH, dwr, dvr, candidates=(64, 96, 128, 160, 200), stream=None, detail=False):
     """Time the plain device path on this problem for each candidate tile
-    size, then 8/16/32 shifts per diagonal CTA at the fastest (dwr restored,
-    dvr overwritten); records both (used when tlsz=0 is passed) and returns
-    (best tlsz, [ms per candidate]), plus (shifts per CTA, [ms for 8, 16,
-    32]) when detail is set."""
+    size, then 8/16/32 shifts per diagonal CTA at the fastest, then (with 8
+    or 16) the top GEMM of each tile's rows inside the diagonal CTAs or as
+    its own launch (dwr restored, dvr overwritten); records all three (used
+    when tlsz=0 is passed) and returns (best tlsz, [ms per candidate]), plus
+    (shifts per CTA, [ms for 8, 16, 32], fused (bool), [ms separate, ms
+    fused]) when detail is set (-1 ms where the form does not apply)."""
     lib = _lib.load()
     n = dH.shape[0]
     cand = (C.c_int * len(candidates))(*candidates)
     ms = (C.c_double * len(candidates))()
     sc = C.c_int()
     scms = (C.c_double * 3)()
+    fz = C.c_int()
+    fzms = (C.c_double * 2)()
     best = lib.hsr_autotune_plain(n, dH.data_ptr(), dH.stride(0), dwr.numel(), dwr.data_ptr(), dvr.data_ptr(),
-                                  dvr.stride(0), cand, len(candidates), ms, C.byref(sc), scms,
+                                  dvr.stride(0), cand, len(candidates), ms, C.byref(sc), scms, C.byref(fz), fzms,
                                   None if stream is None else C.c_void_p(stream.cuda_stream))
     if best < 0:
         raise HsrError(best)
     if detail:
-        return best, list(ms), sc.value, list(scms)
+        return best, list(ms), sc.value, list(scms), bool(fz.value), list(fzms)
     return best, list(ms)
 
 

@@ -1311,13 +1311,14 @@ int hsr_selftest_bounded_wait(void *stream) {
 
 int hsr_autotune_plain(int n, const double *dH, int lddH, int nrhs, double *dwr, double *dvr, int lddvr,
                        const int *cand, int ncand, double *ms_out, int *shifts_per_cta, double *spc_ms,
-                       void *stream) {
+                       int *top_fused, double *fused_ms, void *stream) {
     if (n <= 0 || nrhs <= 0 || !cand || ncand <= 0 || !dH || !dwr || !dvr) return g_last_status = HSR_ERR_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     double *wr0 = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     auto done = [&](int rc) {
         set_diag_shifts_trial(0);
+        set_fused_top_trial(-1);
         if (wr0) cudaFree(wr0);
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
@@ -1375,7 +1376,21 @@ int hsr_autotune_plain(int n, const double *dH, int lddH, int nrhs, double *dwr,
             best_sc = scs[i];
         }
     }
+    // With narrow diagonal CTAs: the top GEMM of each tile's rows inside
+    // them or as its own launch ([separate, fused]); -1 where it does not
+    // apply (32 shifts per CTA).
+    int fused = 0;
+    double fms[2] = {-1.0, -1.0};
+    if (best_sc && best_sc < 32) {
+        set_diag_shifts_trial(best_sc);
+        for (int on = 0; on < 2; ++on) {
+            set_fused_top_trial(on);
+            if (time_one(best, &fms[on]) != HSR_OK) return done(HSR_ERR_CUDA);
+        }
+        fused = fms[1] <= fms[0] ? 1 : 0;
+    }
     set_diag_shifts_trial(0);
+    set_fused_top_trial(-1);
     if (cudaMemcpyAsync(dwr, wr0, (size_t)nrhs * 8, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
         return done(HSR_ERR_CUDA);
@@ -1384,7 +1399,13 @@ int hsr_autotune_plain(int n, const double *dH, int lddH, int nrhs, double *dwr,
         g_plain_tune[n] = best;
     }
     if (best_sc) record_diag_shifts(nrhs, best_sc);
+    if (best_sc && best_sc < 32) record_fused_top(nrhs, fused != 0);
     if (shifts_per_cta) *shifts_per_cta = best_sc;
+    if (top_fused) *top_fused = fused;
+    if (fused_ms) {
+        fused_ms[0] = fms[0];
+        fused_ms[1] = fms[1];
+    }
     done(HSR_OK);
     return best;
 }

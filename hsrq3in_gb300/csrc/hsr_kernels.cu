@@ -1474,8 +1474,7 @@ cudaError_t launch_diag_narrow_fused(const DevProblem &P, const DevProblem &Pg, 
 // the wide form is used and the caller runs the two launches.
 bool launch_diag_fused(const DevProblem &P, const DevProblem &Pg, int J, int b, cudaStream_t st,
                        cudaError_t *err) {
-    const char *env = getenv("HSR_FUSED_TOP");          // 0: separate launches, for comparison
-    if (env && env[0] == '0') return false;
+    if (!fused_top_for(P.S)) return false;
     switch (diag_shifts_per_cta(P.S)) {
     case 8: *err = launch_diag_narrow_fused<8, kDiagWarpsNarrow>(P, Pg, J, b, st); return true;
     case 16: *err = launch_diag_narrow_fused<16, kDiagWarpsNarrow>(P, Pg, J, b, st); return true;
@@ -1483,18 +1482,51 @@ bool launch_diag_fused(const DevProblem &P, const DevProblem &Pg, int J, int b, 
     }
 }
 
-// Shifts per CTA recorded by the plain-path autotuner, by shift count, and a
-// per-thread trial value the autotuner sets while it times the candidates.
+// Shifts per CTA and top-GEMM form recorded by the plain-path autotuner, by
+// shift count, and per-thread trial values the autotuner sets while it times
+// the candidates.
 namespace {
 std::mutex g_spc_mu;
 std::map<int, int> g_spc_tuned;
+std::map<int, int> g_fused_tuned;
 thread_local int t_spc_trial = 0;
+thread_local int t_fused_trial = -1;
+
+// The entry of the nearest shift count within a factor of two, or 0.
+int nearest_tuned(const std::map<int, int> &m, int S) {
+    int best = 0;
+    double bd = 1e300;
+    for (auto &kv : m) {
+        const double d = std::fabs(std::log((double)kv.first / S));
+        if (d < bd) {
+            bd = d;
+            best = kv.second;
+        }
+    }
+    return bd <= std::log(2.0) ? best : 0;
+}
 }  // namespace
 
 void set_diag_shifts_trial(int sc) { t_spc_trial = sc; }
 void record_diag_shifts(int S, int sc) {
     std::lock_guard<std::mutex> g(g_spc_mu);
     g_spc_tuned[S] = sc;
+}
+void set_fused_top_trial(int on) { t_fused_trial = on; }
+void record_fused_top(int S, bool on) {
+    std::lock_guard<std::mutex> g(g_spc_mu);
+    g_fused_tuned[S] = on ? 1 : 2;
+}
+// Whether the narrow diagonal kernel also computes the top GEMM of its own
+// rows: HSR_FUSED_TOP (0 or 1) first, then the autotuner's trial value, then
+// its recorded choice for the nearest shift count within a factor of two,
+// else yes.  Either form gives the same result bit for bit.
+bool fused_top_for(int S) {
+    const char *env = getenv("HSR_FUSED_TOP");
+    if (env && (env[0] == '0' || env[0] == '1')) return env[0] == '1';
+    if (t_fused_trial >= 0) return t_fused_trial != 0;
+    std::lock_guard<std::mutex> g(g_spc_mu);
+    return nearest_tuned(g_fused_tuned, S) != 2;
 }
 
 // Shifts per diagonal CTA.  HSR_DIAG_SHIFTS_PER_CTA (8, 16 or 32) first,
@@ -1509,18 +1541,9 @@ int diag_shifts_per_cta(int S) {
     if (forced == 8 || forced == 16 || forced == 32) return forced;
     if (t_spc_trial) return t_spc_trial;
     {
-        // The tuned entry of the nearest shift count within a factor of two.
         std::lock_guard<std::mutex> g(g_spc_mu);
-        int best = 0;
-        double bd = 1e300;
-        for (auto &kv : g_spc_tuned) {
-            const double d = std::fabs(std::log((double)kv.first / S));
-            if (d < bd) {
-                bd = d;
-                best = kv.second;
-            }
-        }
-        if (best && bd <= std::log(2.0)) return best;
+        const int best = nearest_tuned(g_spc_tuned, S);
+        if (best) return best;
     }
     static const int sms = []() {
         int dev = 0, n = 0;

@@ -76,6 +76,12 @@ cudaError_t launch_diag(const DevProblem &P, int J, int b, double *gscratch, cud
 // the wide diagonal form applies; otherwise *err holds the launch status.
 bool launch_diag_fused(const DevProblem &P, const DevProblem &Pg, int J, int b, cudaStream_t st,
                        cudaError_t *err);
+// Top-GEMM form of the narrow diagonal kernel: fused (true) or a separate
+// launch -- the HSR_FUSED_TOP override, else this thread's autotuning trial
+// (-1: none), else the tuned entry of the nearest shift count, else fused.
+bool fused_top_for(int S);
+void set_fused_top_trial(int on);
+void record_fused_top(int S, bool on);
 // Shifts per CTA the diagonal kernel uses for S shifts: 8, 16 or 32 -- the
 // HSR_DIAG_SHIFTS_PER_CTA override, else this thread's autotuning trial, else
 // the tuned entry of the nearest shift count (record_diag_shifts), else a rule

@@ -253,18 +253,22 @@ int hsr_batch_plan_queue_info(const hsr_batch_plan *plan, int *engine, long *ite
  * problem (device pointers; dwr is restored, dvr overwritten) for each
  * candidate tlsz in `cand` (ms_out[i], optional, gets candidate i's time),
  * then, at the fastest tlsz, for 8, 16 and 32 shifts per diagonal CTA
- * (spc_ms[0..2], optional).  It records the fastest tlsz for order n and the
- * fastest shifts per CTA for nrhs shifts (*shifts_per_cta, optional), and
- * returns the tlsz.  A tlsz of 0 passed to tiled_inverse_iteration,
- * hsr_inverse_iteration_ex or hsr_inverse_iteration_device then selects the
- * recorded size of the nearest tuned order within a factor of two
- * (hsr_autotune_plain_tlsz), else a default by order; the diagonal kernel
- * likewise uses the recorded shifts per CTA of the nearest tuned shift count.
- * The reference takes tlsz from its caller only (main.c:40-44); no reference
- * counterpart. */
+ * (spc_ms[0..2], optional), and, where the fastest of those is 8 or 16,
+ * with the GEMM of each tile's own rows run inside the diagonal CTAs or as
+ * its own launch (fused_ms[1] and fused_ms[0], optional; -1 where it does
+ * not apply).  It records the fastest tlsz for order n, the fastest shifts
+ * per CTA and top-GEMM form for nrhs shifts (*shifts_per_cta, *top_fused,
+ * optional), and returns the tlsz.  A tlsz of 0 passed to
+ * tiled_inverse_iteration, hsr_inverse_iteration_ex or
+ * hsr_inverse_iteration_device then selects the recorded size of the nearest
+ * tuned order within a factor of two (hsr_autotune_plain_tlsz), else a
+ * default by order; the diagonal kernel likewise uses the recorded shifts per
+ * CTA and top-GEMM form of the nearest tuned shift count.  Every choice gives
+ * the same result bit for bit.  The reference takes tlsz from its caller only
+ * (main.c:40-44); no reference counterpart. */
 int hsr_autotune_plain(int n, const double *dH, int lddH, int nrhs, double *dwr, double *dvr, int lddvr,
                        const int *cand, int ncand, double *ms_out, int *shifts_per_cta, double *spc_ms,
-                       void *stream);
+                       int *top_fused, double *fused_ms, void *stream);
 int hsr_autotune_plain_tlsz(int n);
 
 /* Tile size for batches whose orders lie in [n_lo, n_hi]: the size that

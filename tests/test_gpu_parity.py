@@ -318,9 +318,13 @@ def test_plain_autotune_and_tlsz_zero(gpu_lib):
     dH[:, :n] = torch.from_numpy(np.ascontiguousarray(H.T)).to(dev)
     dwr = torch.from_numpy(wr.copy()).to(dev)
     dX = torch.empty((n, ld), dtype=torch.float64, device=dev)
-    best, ms, sc, sc_ms = hsr.autotune_plain(dH, dwr, dX, candidates=(32, 64, 96), detail=True)
+    best, ms, sc, sc_ms, fused, fz_ms = hsr.autotune_plain(dH, dwr, dX, candidates=(32, 64, 96), detail=True)
     assert best in (32, 64, 96) and all(0 < t < 1e299 for t in ms)
     assert sc in (8, 16, 32) and all(0 < t < 1e299 for t in sc_ms)
+    if sc < 32:
+        assert all(0 < t < 1e299 for t in fz_ms) and fused == (fz_ms[1] <= fz_ms[0])
+    else:
+        assert fz_ms == [-1.0, -1.0] and not fused
     assert np.array_equal(dwr.cpu().numpy(), wr)                 # restored
     assert _lib.load().hsr_autotune_plain_tlsz(n) == best
     a = hsr.inverse_iteration(H, wr, 0, 16)
