@@ -1290,17 +1290,17 @@ __device__ __forceinline__ void diag_body_narrow(const DevProblem &P, int J, int
 // result is bit-identical to the top GEMM launch it replaces and the tile's
 // rows are ready in this CTA without waiting for another kernel.
 //
-// Staged form: the H block (rows x b) and the CTA's columns of W and Zs move
-// through shared memory in chunks of kTopChunk k-columns, double-buffered
-// with cp.async (every request of a chunk in flight at once), so the FP64
-// sums read shared memory instead of paying a global-load latency every few
-// fmas.  Thread t takes column t % SC and rows g, g + G, ..., g + (EB-1) G
-// (g = t / SC, G = threads / SC), its sums in registers across the chunks;
-// a pass covers G * EB rows (72 with 8 shifts per CTA), a taller tile takes
-// more passes.  The two buffers, (rows + 2 SC) x kTopChunk doubles each, are
-// 10 KB at tlsz 64 -- no more than the diagonal solve's own shared memory,
-// which reuses them afterwards, so the CTA still fits beside two GEMM CTAs
-// on one SM; from 16 rows on they are no larger than the diagonal solve's.
+// The H block (rows x b) and the CTA's columns of W and Zs move through
+// shared memory in chunks of kTopChunk k-columns, double-buffered with
+// cp.async (every request of a chunk in flight at once), so the FP64 sums
+// read shared memory instead of paying a global-load latency every few fmas.
+// Thread t takes column t % SC and rows g, g + G, ..., g + (EB-1) G (g = t /
+// SC, G = threads / SC), its sums in registers across the chunks; a pass
+// covers G * EB rows (72 with 8 shifts per CTA), a taller tile takes more
+// passes.  The two buffers, (rows + 2 SC) x kTopChunk doubles each (10 KB at
+// tlsz 64), are no larger than the diagonal solve's own shared memory from
+// 16 rows on; the solve reuses them afterwards, so the CTA still fits beside
+// two GEMM CTAs on one SM.
 constexpr int kTopChunk = 8, kTopRowsPerThread = 6;
 template <int SC>
 __host__ __device__ constexpr size_t top_staged_bytes(int rows) {
