@@ -87,12 +87,23 @@ __global__ void k_tile_rowsums(DevProblem P, unsigned long long *Hn_bits,
     }
 }
 
-__global__ void k_full_rowsums(DevProblem P, unsigned long long *hinf_bits, int *nan_flag) {
+// One thread per row, 32 rows per CTA so the rows spread over many SMs; each
+// group of eight columns is loaded before it is added, in column order.
+__global__ void __launch_bounds__(32) k_full_rowsums(DevProblem P, unsigned long long *hinf_bits, int *nan_flag) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     double sum = 0.0;
     const double *row = P.H + i;
-    for (int c = 0; c < P.n; ++c) sum += absd(row[(size_t)c * P.ldh]);
+    const size_t ldh = (size_t)P.ldh;
+    int c = 0;
+    for (; c + 8 <= P.n; c += 8) {
+        double a[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) a[q] = row[(size_t)(c + q) * ldh];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) sum += absd(a[q]);
+    }
+    for (; c < P.n; ++c) sum += absd(row[(size_t)c * ldh]);
     if (sum != sum) atomicOr(nan_flag, 1);
     atomicMax(hinf_bits, (unsigned long long)__double_as_longlong(sum));
 }
@@ -102,7 +113,7 @@ cudaError_t launch_norms(const DevProblem &P, unsigned long long *Hn_bits,
                          int *nan_flag, cudaStream_t st) {
     dim3 g((P.n + 127) / 128, P.T);
     k_tile_rowsums<<<g, 128, 0, st>>>(P, Hn_bits, hn_bits, nan_flag);
-    k_full_rowsums<<<(P.n + 127) / 128, 128, 0, st>>>(P, hinf_bits, nan_flag);
+    k_full_rowsums<<<(P.n + 31) / 32, 32, 0, st>>>(P, hinf_bits, nan_flag);
     return cudaGetLastError();
 }
 
