@@ -93,26 +93,40 @@ __device__ __forceinline__ double scale_by(double a, double x) { return is_one(a
 // for two FP64 divisions.  Operands outside the common range (zero,
 // subnormal, infinite, NaN, a divisor whose significand is a power of two, a
 // quotient near the exponent limits) take the FP64 instruction.
+// The integer parts below also compile for the host (a test checks them
+// there against the host's IEEE division), with the FP32 seed from a
+// correctly rounded division and the high product from a 128-bit one.
 static __device__ __noinline__ double div_fp64(double a, double b) { return a / b; }
-__device__ __forceinline__ float rcp_approx_f32(float x) {
+__host__ __device__ __forceinline__ float rcp_approx_f32(float x) {
+#ifdef __CUDA_ARCH__
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
+#else
+    return 1.0f / x;
+#endif
+}
+__host__ __device__ __forceinline__ unsigned long long umulhi64(unsigned long long a, unsigned long long b) {
+#ifdef __CUDA_ARCH__
+    return __umul64hi(a, b);
+#else
+    return (unsigned long long)(((unsigned __int128)a * b) >> 64);
+#endif
 }
 // One Newton step for y ~ 2^116 / mb, mb in (2^52, 2^53): with the 128-bit
 // error E = 2^116 - mb y, y' = y + y E / 2^116.
-__device__ __forceinline__ unsigned long long ip_recip_step(unsigned long long mb, unsigned long long y) {
+__host__ __device__ __forceinline__ unsigned long long ip_recip_step(unsigned long long mb, unsigned long long y) {
     const unsigned long long lo = mb * y;
-    const unsigned long long hi = __umul64hi(mb, y);
+    const unsigned long long hi = umulhi64(mb, y);
     const long long ehi = (long long)((1ULL << 52) - hi) - (lo != 0ULL ? 1 : 0);
     const unsigned long long elo = 0ULL - lo;
     const long long e = (long long)(((unsigned long long)ehi << 12) | (elo >> 52));   // E / 2^52
     const unsigned long long ae = e < 0 ? (unsigned long long)(-e) : (unsigned long long)e;
-    const unsigned long long d = __umul64hi(y, ae);
+    const unsigned long long d = umulhi64(y, ae);
     return e < 0 ? y - d : y + d;
 }
 // y ~ 2^116 / mb within a few units (about 2^-62 relative).
-__device__ __forceinline__ unsigned long long ip_recip(unsigned long long mb) {
+__host__ __device__ __forceinline__ unsigned long long ip_recip(unsigned long long mb) {
     float r = rcp_approx_f32((float)(unsigned)(mb >> 29)) * 0x1p87f;
     r = fminf(r, 0x1.fffffep63f);
     unsigned long long y = (unsigned long long)r;
@@ -124,10 +138,11 @@ __device__ __forceinline__ unsigned long long ip_recip(unsigned long long mb) {
 // q estimates floor(ma 2^sh / mb) (54 bits) within two; the remainder
 // r = ma 2^sh - q mb, exact modulo 2^64 because |r| < 2^56, moves q to the
 // floor; its last bit and r != 0 round the 53-bit result to nearest even.
-__device__ __forceinline__ unsigned long long ip_quot(unsigned long long ma, unsigned long long mb,
-                                                      unsigned long long y, int ebias, unsigned long long sign) {
+__host__ __device__ __forceinline__ unsigned long long ip_quot(unsigned long long ma, unsigned long long mb,
+                                                               unsigned long long y, int ebias,
+                                                               unsigned long long sign) {
     const int sh = ma < mb ? 54 : 53;
-    const unsigned long long hi = __umul64hi(ma, y);
+    const unsigned long long hi = umulhi64(ma, y);
     const unsigned long long lo = ma * y;
     unsigned long long q = sh == 53 ? ((hi << 1) | (lo >> 63)) : ((hi << 2) | (lo >> 62));
     long long r = (long long)((ma << sh) - q * mb);
@@ -150,7 +165,7 @@ __device__ __forceinline__ unsigned long long ip_quot(unsigned long long ma, uns
     return sign | (((unsigned long long)(eo - 1) << 52) + Q);   // a carry out of Q raises the exponent
 }
 constexpr unsigned long long kSigMask = 0xfffffffffffffULL, kHidden = 1ULL << 52;
-__device__ __forceinline__ bool ip_div_ok(int ea, int eb, unsigned long long fb) {
+__host__ __device__ __forceinline__ bool ip_div_ok(int ea, int eb, unsigned long long fb) {
     const int eq = ea - eb + 1023;
     return ea != 0 && ea != 0x7ff && eb != 0 && eb != 0x7ff && fb != 0 && eq >= 2 && eq <= 2045;
 }
